@@ -1,0 +1,348 @@
+"""Benchmark: pair-interactions/s of the WCSPH dam-break step on GB300.
+
+Workload (default): the 3D dam break at dr = 0.0079 -- 4,096,766 fluid +
+1,649,867 wall particles (no lid), H = 4 dr, Wendland quintic, Tait EOS,
+artificial viscosity, XSPH, wall pressure, kick-drift-kick -- one `step` is
+one verlet_step! of the whole system (binning + density + wall pressure +
+force + kick).  Inputs are synthetic lattices generated with the reference's
+lattice rules; the 2.6 GB device-resident state is larger than L2, so no L2
+flush is needed between steps.
+
+Arms:
+  default            this library (FP64 drop-in path), one replica per GPU
+  --impl reference   the reference algorithm on the host cores (the C
+                     restatement; the Julia reference cannot run here)
+
+Prints one JSON line (rank 0).
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+PKG = os.path.join(ROOT, "smoothedparticles.jl_gb300")
+for _p in (ROOT, PKG, os.path.join(ROOT, "oracle")):
+    if _p not in sys.path:
+        sys.path.insert(0, _p)
+
+import numpy as np  # noqa: E402
+
+METRIC = "pair-interactions/s, 3D WCSPH 4M ptcl"
+UNIT = "pair-interactions/s"
+
+# Algorithmic FP64 flops per evaluated hit (add/sub/mul/compare = 1,
+# sqrt = 1, division = 1), counted from the operator formulas in
+# csrc/sph_pair64.cu, 3D:
+#   distance 9 (3 sub, 3 mul, 2 add, sqrt); W 9; rDW 6
+#   density hit        = distance + W + m*W + add                       = 20
+#   wall-pressure hit  = distance + W + g.d (5) + 6 accumulate ops      = 29
+#   force fluid hit    = distance + rDW + m* + dv (3) + v.d (5) + rho sum
+#                        + 2/(..) + compare + P-sum (2) + coefficient
+#                        + a += (6) + W + m* + *inv + XSPH (9)         = 56
+#   force wall hit     = distance + rDW + m* + P-sum + coefficient + a += (6) = 24
+#   viscosity active   = +5 (h*v.d, r^2+eta^2, division, -a c0 *, * 1/rho)
+FLOPS = dict(density=20, wall=29, force_fluid=56, force_wall=24, force_av=5)
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--dr", type=float, default=0.0079)
+    ap.add_argument("--dim", type=int, default=3)
+    ap.add_argument("--e2e-steps", type=int, default=3)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    return ap.parse_args()
+
+
+def dist_env():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", str(rank)))
+    return rank, world, local
+
+
+def make_case(args):
+    from sphgpu import geometry as G
+    return G.dam_break(args.dim, args.dr)
+
+
+def workload_name(case):
+    nf = case.n_fluid
+    return (f"{case.dim}D WCSPH dam break dr={case.dr:g}: {nf:,} fluid + {case.n - nf:,} wall "
+            f"particles, H={case.params['h']:.5g}, FP64 verlet_step!")
+
+
+class ClockSampler:
+    """nvidia-smi sampling during the timed region."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device: int):
+        self.device = device
+        self.proc = None
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.device}", f"--query-gpu={self.Q}",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except (FileNotFoundError, OSError):
+            self.proc = None
+        return self
+
+    def __exit__(self, *exc):
+        self.out = ""
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.out, _ = self.proc.communicate(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+                self.out, _ = self.proc.communicate()
+
+    def summary(self):
+        rows = []
+        for line in (self.out or "").strip().splitlines():
+            parts = [t.strip() for t in line.split(",")]
+            if len(parts) >= 9:
+                rows.append(parts)
+        if not rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        sm = [float(r[1]) for r in rows if r[1].replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in rows if r[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for r in rows for i in range(4) if r[5 + i].lower() == "active"})
+        return {"sm_mhz": statistics.median(sm) if sm else None,
+                "sm_max_mhz": max(mx) if mx else None, "reasons": reasons,
+                "samples": len(rows)}
+
+
+def cpu_baseline(case, budget_s=12.0):
+    """The oracle (C restatement of the reference's apply! path, OpenMP over
+    target particles) on the host cores: density + wall-pressure + force passes
+    over a contiguous block of fluid targets of the same system."""
+    import oracle
+    o = oracle.from_case(case)
+    t0 = time.perf_counter()
+    o.create_cell_list()
+    t_bin = time.perf_counter() - t0
+    nf = case.n_fluid
+    m = 20000
+    lo = nf // 2 - m // 2
+    t0 = time.perf_counter()
+    o.pair_passes_sample(lo, lo + m)
+    t_cal = time.perf_counter() - t0
+    m2 = int(min(nf, max(m, m * budget_s / max(t_cal, 1e-3))))
+    lo = max(0, nf // 2 - m2 // 2)
+    t0 = time.perf_counter()
+    pairs = o.pair_passes_sample(lo, lo + m2)
+    t = time.perf_counter() - t0
+    o.close()
+    return dict(value=pairs / t, unit=UNIT, cores=oracle.num_threads(), kind="port",
+                sample=(f"pair passes (density, wall pressure, force) over {m2:,} contiguous fluid "
+                        f"targets of the same {case.n:,}-particle system: {pairs:,} pairs in "
+                        f"{t:.2f} s; create_cell_list! of the full system {t_bin:.2f} s"))
+
+
+def run_reference(args):
+    rank, world, _ = dist_env()
+    if rank != 0:
+        return 0
+    import oracle
+    case = make_case(args)
+    o = oracle.from_case(case)
+    o.create_cell_list()
+    nf = case.n_fluid
+    m = 20000
+    lo0 = nf // 2
+    t0 = time.perf_counter()
+    o.pair_passes_sample(lo0, lo0 + m)
+    t_cal = time.perf_counter() - t0
+    m = int(min(nf // 4, max(m, m * 6.0 / max(t_cal, 1e-3))))  # ~6 s per step
+    pairs_tot, t_tot = 0, 0.0
+    for it in range(args.warmup + args.steps):
+        lo = (nf // 8 + it * m) % max(1, nf - m)
+        t0 = time.perf_counter()
+        p = o.pair_passes_sample(lo, lo + m)
+        dt = time.perf_counter() - t0
+        if it >= args.warmup:
+            pairs_tot += p
+            t_tot += dt
+    value = pairs_tot / t_tot
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT,
+        "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": 1e3 * t_tot / args.steps, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": workload_name(case), "particles": case.n},
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": oracle.num_threads(),
+                         "kind": "port",
+                         "sample": f"each step: density + wall-pressure + force passes over {m:,} "
+                                   "contiguous fluid targets (the Julia reference cannot run: no "
+                                   "Julia runtime on the box)"},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def run_ours(args):
+    import torch
+
+    import sphgpu
+    rank, world, local = dist_env()
+    if world > 1:
+        import torch.distributed as dist
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl")
+    dev = local
+    torch.cuda.set_device(dev)
+    case = make_case(args)
+    g = sphgpu.ParticleSystem(case.params, sphgpu.FP64, device=dev)
+    g.upload(case.x, case.v, type=case.type)
+    g.init_state()
+    stream = torch.cuda.ExternalStream(g.stream(), device=dev)
+    for _ in range(args.warmup):
+        g.step(1)
+    g.synchronize()
+    g.pair_count(reset=True)
+    g.pair_stats(reset=True)
+    g.reset_kernel_stats()
+    g.set_profiling(True)
+    l0 = g.launch_count()
+    if world > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize(dev)
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    with ClockSampler(dev) as clk:
+        e0.record(stream)
+        for _ in range(args.steps):
+            g.step(1)
+        e1.record(stream)
+        e1.synchronize()
+    torch.cuda.synchronize(dev)
+    ms = e0.elapsed_time(e1)
+    launches = g.launch_count() - l0
+    g.set_profiling(False)
+    pairs = g.pair_count(reset=True)
+    cats = g.pair_stats(reset=True)
+    kstats = g.kernel_stats()
+    g.synchronize()
+    ms_max = ms
+    pairs_all = pairs
+    if world > 1:
+        import torch.distributed as dist
+        t = torch.tensor([ms], device=f"cuda:{dev}")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms_max = float(t.item())
+        pt = torch.tensor([float(pairs)], device=f"cuda:{dev}", dtype=torch.float64)
+        dist.all_reduce(pt)
+        pairs_all = float(pt.item())
+    value = pairs_all / (ms_max * 1e-3)
+
+    # ---- end to end through the C ABI with pinned host buffers
+    n = g.n
+    pin = lambda shape, dt: torch.empty(shape, dtype=dt, pin_memory=True).numpy()
+    hx, hv, ha, hs = (pin((n, 3), torch.float64) for _ in range(4))
+    hrho, hP = pin((n,), torch.float64), pin((n,), torch.float64)
+    hx[:] = g.get("x"); hv[:] = g.get("v"); ha[:] = g.get("a"); hs[:] = g.get("xsph")
+    g.pair_count(reset=True)
+    torch.cuda.synchronize(dev)
+    t0 = time.perf_counter()
+    for _ in range(args.e2e_steps):
+        g.set("x", hx); g.set("v", hv); g.set("a", ha); g.set("xsph", hs)
+        g.step(1)
+        hx[:] = g.get("x"); hv[:] = g.get("v"); ha[:] = g.get("a")
+        hrho[:] = g.get("rho"); hP[:] = g.get("P")
+        hs[:] = g.get("xsph")
+    t_e2e = time.perf_counter() - t0
+    e2e_pairs = g.pair_count(reset=True)
+    e2e = {"value": e2e_pairs / t_e2e, "unit": UNIT,
+           "h2d_bytes_per_step": int(n * 4 * 24), "d2h_bytes_per_step": int(n * (4 * 24 + 2 * 8)),
+           "steps": args.e2e_steps,
+           "note": "per step: set x, v, a, xsph from pinned host arrays; sph_step; get x, v, a, "
+                   "xsph, rho, P into pinned host arrays (reference particle order)"}
+
+    # ---- roofline of the dominant kernel (the FP64 force pass)
+    names = {k: v for k, v in kstats.items() if v[1] > 0}
+    dom = max(names, key=lambda k: names[k][0])
+    dfma = sphgpu.pipe_peak("dfma", dev)
+    peak_tflops = 2.0 * dfma / 1e12
+    flops = {
+        "force": cats["force_fluid"] * FLOPS["force_fluid"] + cats["force_wall"] * FLOPS["force_wall"]
+        + cats["force_av"] * FLOPS["force_av"],
+        "density": cats["density"] * FLOPS["density"],
+        "wall_pressure": cats["wall"] * FLOPS["wall"],
+    }
+    kern_rows = {}
+    for k, (tms, nl) in names.items():
+        row = {"ms_total": round(tms, 3), "launches": nl, "ms_avg": round(tms / nl, 4),
+               "share": round(tms / max(1e-9, sum(v[0] for v in names.values())), 4)}
+        if k in flops:
+            row["tflops"] = round(flops[k] / (tms * 1e-3) / 1e12, 4)
+        kern_rows[k] = row
+    dom_ms = names[dom][0] / names[dom][1]
+    dom_flops = flops.get(dom, 0) / max(1, names[dom][1])
+    achieved = dom_flops / (dom_ms * 1e-3) / 1e12
+    roofline = {"bound": "fp64", "kernel": dom, "achieved": round(achieved, 4),
+                "peak": round(peak_tflops, 4), "unit": "TFLOP/s",
+                "frac": round(achieved / peak_tflops, 4),
+                "traffic": NCU_TRAFFIC.get(dom, {}).get("bytes_per_launch_scaled"),
+                "peak_source": "measured in this run: FP64 FMA issue rate x 2 (sph_pipe_peak)",
+                "flops_per_launch": dom_flops,
+                "note": "algorithmic flops count sqrt and division as 1 each; each costs ~10 FP64 "
+                        "pipe slots on GB300"}
+
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        cpu = cpu_baseline(case)
+
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": ms_max / args.steps, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": workload_name(case), "particles": case.n,
+                       "fluid": case.n_fluid, "pairs_per_step": pairs / args.steps,
+                       "l2": "no flush: 2.6 GB resident state > 129 MB L2",
+                       "replicas": world},
+            "steps_per_s": 1e3 * args.steps / ms_max,
+            "roofline": roofline, "kernels": kern_rows,
+            "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": launches,
+            "clocks": clk.summary(),
+        }
+        print(json.dumps(line), flush=True)
+    g.close()
+    if world > 1:
+        torch.distributed.destroy_process_group()
+    return 0
+
+
+# DRAM traffic per launch from the committed ncu summary (profiles/), scaled
+# to the full workload; filled from the capture.
+NCU_TRAFFIC: dict = {}
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        return run_reference(args)
+    return run_ours(args)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

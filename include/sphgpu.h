@@ -1,0 +1,212 @@
+/*
+ * sphgpu.h -- C ABI of the GB300 (sm_103a) neighbour search and pair loop
+ * that replaces SmoothedParticles.jl's cell-list / pair-loop layer.
+ *
+ * One handle = one ParticleSystem on one GPU.  Particle state lives in device
+ * memory as struct-of-arrays between calls; the handle owns one CUDA stream
+ * and every call is ordered on it.  Host arrays passed in or out are always in
+ * the reference's particle order (the index of a particle in sys.particles);
+ * inside the device the particles are kept sorted by cell.
+ *
+ * Every function returns an int status: SPH_OK (0) or a negative SPH_ERR_*.
+ * sph_last_error() gives a message for the last failure on a handle.  A handle
+ * must not be used from two threads at once; separate handles are independent.
+ * Operators are the built-in ones (SPH_OP_*): arbitrary Julia closures have no
+ * device counterpart and there is no CPU fallback.
+ *
+ * Reference paths below are relative to the SmoothedParticles.jl project.
+ */
+#ifndef SPHGPU_H
+#define SPHGPU_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define SPHGPU_ABI_VERSION 1
+
+/* ---- status codes */
+#define SPH_OK 0
+#define SPH_ERR_ARG -1         /* invalid argument (null pointer, bad op, size)    */
+#define SPH_ERR_CUDA -2        /* a CUDA runtime call failed                       */
+#define SPH_ERR_STATE -3       /* call out of order (e.g. pair pass on stale cells) */
+#define SPH_ERR_NOMEM -4       /* device allocation failed                         */
+#define SPH_ERR_DEVICE -5      /* a kernel reported an error (bounds, overflow)    */
+#define SPH_ERR_UNSUPPORTED -6 /* operator / mode combination not provided         */
+#define SPH_ERR_TIMEOUT -7     /* a bounded device wait gave up                    */
+#define SPH_ERR_BUDGET -8      /* request does not fit the memory budget          */
+
+/* ---- particle types (the `type` field of the reference's examples) */
+#define SPH_FLUID 0
+#define SPH_WALL 1
+
+/* ---- precision of the pair passes */
+#define SPH_PREC_FP64 0  /* FP64 throughout; bit-exact with the CPU restatement */
+#define SPH_PREC_MIXED 1 /* FP32 pair arithmetic on cell-relative positions,
+                            FP64 positions, integration and accumulators      */
+
+/* ---- built-in binary (pair) operators: apply!(sys, op!; self) */
+#define SPH_OP_DENSITY 1       /* rho_p     += m W(r_pq); fluid p, every q         */
+#define SPH_OP_DENSITY_REF 2   /* rho_ref_p += m W(r_pq); fluid p, every q         */
+#define SPH_OP_FORCE 3         /* fluid p: a_p += pressure (+ Monaghan viscosity
+                                  between fluid particles); xsph_p += XSPH term */
+#define SPH_OP_WALL_PRESSURE 4 /* wall p: P_p = (sum P_q W + sum rho_q (g.x_pq) W)
+                                  / sum W over fluid q (Adami et al. 2012)       */
+/* ---- built-in unary operators: apply!(sys, op!) */
+#define SPH_OP_RESET_RHO 10
+#define SPH_OP_RESET_RHO_REF 11
+#define SPH_OP_RESET_A 12     /* a = 0 and xsph = 0                            */
+#define SPH_OP_EOS 13         /* Tait: P = B((rho/rho_ref)^7 - 1)              */
+#define SPH_OP_KICK 14        /* v += dt/2 (a + g)  (fluid)                    */
+#define SPH_OP_DRIFT 15       /* x += dt (v + eps xsph)  (fluid)               */
+#define SPH_OP_HYDROSTATIC 16 /* rho_ref /= (1 + rho0 g (H_col - y) / B)^(1/7) */
+
+/* ---- functions for sum(sys, func, x) / sum(sys, func, p) */
+#define SPH_SUM_DENSITY 1  /* m W(r) over all q                      */
+#define SPH_SUM_KERNEL 2   /* W(r) over all q                        */
+#define SPH_SUM_PRESSURE 3 /* (m / rho_q) P_q W(r) over fluid q      */
+#define SPH_SUM_SHEPARD 4  /* (m / rho_q) W(r) over fluid q          */
+
+/* ---- fields for sph_get_field / sph_set_field */
+#define SPH_FIELD_X 1       /* double[n][3]                                   */
+#define SPH_FIELD_V 2       /* double[n][3]                                   */
+#define SPH_FIELD_A 3       /* double[n][3]                                   */
+#define SPH_FIELD_XSPH 4    /* double[n][3]                                   */
+#define SPH_FIELD_RHO 5     /* double[n]                                      */
+#define SPH_FIELD_RHO_REF 6 /* double[n]                                      */
+#define SPH_FIELD_P 7       /* double[n]; setting P also sets P/rho^2 (set RHO first) */
+#define SPH_FIELD_TYPE 8    /* int32[n]                                       */
+#define SPH_FIELD_OID 9     /* int64[n] index at upload time (read only)      */
+#define SPH_FIELD_KEY 10    /* int64[n] cell key of the last binning (read only) */
+
+/* Physical and geometric parameters of one system. */
+typedef struct sph_params {
+  int32_t dim;           /* 2 or 3: kernel normalisation and stored components */
+  int32_t precision;     /* SPH_PREC_FP64 or SPH_PREC_MIXED                    */
+  double h;              /* neighbour radius = kernel support (the reference's h) */
+  double domain_min[3];  /* bounding box of the domain (structs.jl:63)          */
+  double domain_max[3];
+  double mass;           /* particle mass m                                     */
+  double rho0;           /* reference density                                   */
+  double c0;             /* numerical speed of sound; Tait B = c0^2 rho0 / 7     */
+  double h_smooth;       /* smoothing length in the viscosity regulariser        */
+  double alpha;          /* artificial viscosity coefficient                     */
+  double eps_xsph;       /* XSPH coefficient                                     */
+  double gravity[3];
+  double dt;
+  double col_height;     /* free-surface height for SPH_OP_HYDROSTATIC           */
+  int32_t vertical_axis; /* 0-based axis along gravity                           */
+  int32_t reserved;
+} sph_params;
+
+typedef struct sph_system sph_system;
+
+/* ParticleSystem(T, domain, h) -- structs.jl:57-92.  Computes key_phase,
+ * key_lim, key_max, key_diff from the domain's bounding box and allocates the
+ * dense cell table on device `device`. */
+int sph_create(const sph_params* params, int device, sph_system** out);
+int sph_destroy(sph_system* sys);
+const char* sph_last_error(const sph_system* sys);
+int sph_abi_version(void);
+
+/* Geometry of the cell table (structs.jl:66-82): key_phase[3], key_lim[3],
+ * key_max, key_diff[27] (first n_diff used, in the reference's order). */
+int sph_geometry(const sph_system* sys, int64_t key_phase[3], int64_t key_lim[3],
+                 int64_t* key_max, int64_t key_diff[27], int32_t* n_diff);
+
+/* generate_particles! (grids.jl:253-258): replaces the particle set with n
+ * particles given in the reference's order.  x, v: n x 3 doubles (v may be
+ * NULL = 0); rho, rho_ref may be NULL (= 0); type may be NULL (= fluid).
+ * In 2D every z must be 0 (the reference's Rectangle has x3 in [0, 0]). */
+int sph_upload(sph_system* sys, int64_t n, const double* x, const double* v,
+               const double* rho, const double* rho_ref, const int32_t* type);
+int sph_num_particles(sph_system* sys, int64_t* n);
+/* ParticleField (structs.jl:118-125) as whole-array copies in reference order. */
+int sph_get_field(sph_system* sys, int field, void* host_out);
+int sph_set_field(sph_system* sys, int field, const void* host_in);
+
+/* create_cell_list! -- core.jl:51-90.  Removes particles outside the domain's
+ * bounding box (NaN included) with the reference's tail-fill compaction, bins
+ * the rest by cell key (counting sort + per-cell descending-index order) and
+ * reorders the device arrays by cell. */
+int sph_create_cell_list(sph_system* sys);
+
+/* apply!(sys, op!; self) -- core.jl:151-161 with a built-in operator; a pair
+ * operator runs _apply_binary! (core.jl:94-112) for every particle and, if
+ * self != 0, the self term op!(p, p, 0.0) after the neighbours. */
+int sph_apply(sph_system* sys, int op, int self);
+/* apply_unary! -- core.jl:138-142 with a built-in unary operator. */
+int sph_apply_unary(sph_system* sys, int op);
+
+/* sum(sys, func, x) -- core.jl:240-260, at nq points (x: nq x 3 doubles). */
+int sph_sum_point(sph_system* sys, int func, int64_t nq, const double* x, double* out);
+/* sum(sys, func, p) -- core.jl:271-291, for particles by reference index. */
+int sph_sum_particle(sph_system* sys, int func, int64_t nq, const int64_t* index,
+                     double* out);
+
+/* One verlet_step! (examples/collapse_symplectic.jl:170-180) per step: kick,
+ * drift, create_cell_list!, density sum with self term, Tait EOS, wall
+ * pressure, force, kick; the kick + drift run inside the binning's key kernel
+ * and the EOS inside the density pass. */
+int sph_step(sph_system* sys, int nsteps);
+/* Initial state of the dam break (collapse_symplectic.jl:186-191 plus the
+ * hydrostatic reference density): bin, rho_ref sum, hydrostatic scaling,
+ * density sum, EOS, wall pressure, force. */
+int sph_init_state(sph_system* sys);
+
+/* Pair interactions evaluated since the last reset: ordered pairs (p, q),
+ * p != q, r_pq <= h, counted per pair pass over the targets the pass's
+ * operator acts on (fluid targets; wall targets for the wall pressure).  This
+ * is the reference's action! call count (core.jl:105-108) without the calls
+ * on targets the operator ignores. */
+int sph_pair_count(sph_system* sys, uint64_t* pairs, int reset);
+/* Hits evaluated per category since the last reset (no reference counterpart;
+ * used to count algorithmic flops): [0] density sums, [1] wall pressure (fluid
+ * neighbours), [2] force fluid-fluid, [3] force fluid-wall, [4] force pairs
+ * with the viscosity term active; [5..7] unused. */
+int sph_pair_stats(sph_system* sys, uint64_t counts[8], int reset);
+/* Blocks until all work queued on the handle's stream is done and reports any
+ * device-side error flag. */
+int sph_synchronize(sph_system* sys);
+/* The handle's CUDA stream (a cudaStream_t), for callers that time or order
+ * their own work against it. */
+int sph_stream(sph_system* sys, void** stream);
+
+/* ---- diagnostics (no reference counterpart) */
+/* Cell key per particle (reference order) and every ordered neighbour pair in
+ * the reference's traversal order (target ascending; key_diff order;
+ * descending neighbour index), as (p, q) reference indices.  Writes up to cap
+ * pairs and the total count to *count. */
+int sph_debug_pairs(sph_system* sys, int64_t* pairs, int64_t cap, int64_t* count);
+/* Per-kernel timing with CUDA events on the handle's stream, enabled by
+ * sph_set_profiling(sys, 1).  kernel ids are SPH_KERNEL_*. */
+#define SPH_KERNEL_BIN_KEYS 0
+#define SPH_KERNEL_BIN_REMOVE 1
+#define SPH_KERNEL_BIN_SCAN 2
+#define SPH_KERNEL_BIN_SCATTER 3
+#define SPH_KERNEL_BIN_RANK 4
+#define SPH_KERNEL_BIN_GATHER 5
+#define SPH_KERNEL_DENSITY 6
+#define SPH_KERNEL_FORCE 7
+#define SPH_KERNEL_UNARY 8
+#define SPH_KERNEL_SUM 9
+#define SPH_KERNEL_IO 10
+#define SPH_KERNEL_WALL 11
+#define SPH_KERNEL_COUNT 12
+int sph_set_profiling(sph_system* sys, int on);
+int sph_kernel_stats(sph_system* sys, int kernel, double* total_ms, int64_t* launches);
+int sph_reset_kernel_stats(sph_system* sys);
+/* Kernels launched by this handle since creation. */
+int sph_launch_count(sph_system* sys, int64_t* launches);
+/* Issue-rate microbenchmark of one arithmetic pipe on `device` (no reference
+ * counterpart; the roofline denominators of the pair passes):
+ * which = 0 FP64 FMA, 1 FP32 FMA, 2 FP64 add.  Returns thread-instructions/s. */
+int sph_pipe_peak(int device, int which, double* instr_per_s);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

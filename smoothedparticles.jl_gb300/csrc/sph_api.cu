@@ -1,0 +1,730 @@
+// sph_api.cu -- the C ABI (include/sphgpu.h): handle, device memory, stream,
+// argument checking and the order of kernel launches for each call.
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "sph_launch.h"
+#include "sphgpu.h"
+
+using namespace sphgpu;
+
+struct sph_system {
+  sph_params params{};
+  int device = 0;
+  Geometry geo{};
+  Consts k{};
+  cudaStream_t stream = nullptr;
+  State cur{}, alt{};
+  BinScratch b{};
+  void* arena = nullptr;    // per-particle arrays (both SoA sets + scratch + staging)
+  void* cells = nullptr;    // cell tables and counters
+  void* staging = nullptr;  // host-transfer staging inside the arena
+  double* query = nullptr;  // sum() query buffer
+  size_t query_bytes = 0;
+  int cap = 0;              // particles the arena holds
+  int n_host = 0;           // upper bound of the device-resident count
+  bool cells_valid = false;
+  std::string err;
+  // launch accounting and optional per-kernel CUDA-event timing
+  bool profiling = false;
+  struct Pending {
+    int kid;
+    cudaEvent_t start, stop;
+  };
+  std::vector<Pending> pending;
+  std::vector<cudaEvent_t> pool;
+  cudaEvent_t open_start = nullptr;
+  double total_ms[SPH_KERNEL_COUNT] = {};
+  long long kernel_launches[SPH_KERNEL_COUNT] = {};
+  long long total_launches = 0;
+};
+
+namespace {
+
+int fail(sph_system* s, int code, const char* fmt, ...) {
+  if (s) {
+    char buf[512];
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(buf, sizeof buf, fmt, ap);
+    va_end(ap);
+    s->err = buf;
+  }
+  return code;
+}
+
+#define CK(call)                                                                      \
+  do {                                                                                \
+    cudaError_t e_ = (call);                                                          \
+    if (e_ != cudaSuccess)                                                            \
+      return fail(s, SPH_ERR_CUDA, "%s failed: %s", #call, cudaGetErrorString(e_));   \
+  } while (0)
+
+cudaEvent_t get_event(sph_system* s) {
+  if (!s->pool.empty()) {
+    cudaEvent_t e = s->pool.back();
+    s->pool.pop_back();
+    return e;
+  }
+  cudaEvent_t e = nullptr;
+  cudaEventCreate(&e);
+  return e;
+}
+
+void hook(void* owner, int kid, int phase, int kernels) {
+  sph_system* s = (sph_system*)owner;
+  if (phase == 0) {
+    if (s->profiling) {
+      s->open_start = get_event(s);
+      cudaEventRecord(s->open_start, s->stream);
+    }
+    return;
+  }
+  s->kernel_launches[kid] += kernels;
+  s->total_launches += kernels;
+  if (s->profiling && s->open_start) {
+    cudaEvent_t stop = get_event(s);
+    cudaEventRecord(stop, s->stream);
+    s->pending.push_back({kid, s->open_start, stop});
+    s->open_start = nullptr;
+  }
+}
+
+LaunchCtx ctx(sph_system* s) { return LaunchCtx{s->stream, s, hook}; }
+
+int flush_profile(sph_system* s) {
+  if (s->pending.empty()) return SPH_OK;
+  CK(cudaStreamSynchronize(s->stream));
+  for (auto& p : s->pending) {
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, p.start, p.stop);
+    s->total_ms[p.kid] += ms;
+    s->pool.push_back(p.start);
+    s->pool.push_back(p.stop);
+  }
+  s->pending.clear();
+  return SPH_OK;
+}
+
+size_t align_up(size_t v) { return (v + 255) & ~(size_t)255; }
+
+// Carves the arena for capacity C.  With base == nullptr only the size is
+// computed.
+size_t carve(sph_system* s, char* base, size_t C) {
+  size_t off = 0;
+  auto take = [&](size_t bytes) -> void* {
+    void* p = base ? base + off : nullptr;
+    off += align_up(bytes);
+    return p;
+  };
+  const int D = s->params.dim;
+  State* sets[2] = {&s->cur, &s->alt};
+  for (State* st : sets) {
+    for (int d = 0; d < 3; ++d) {
+      const bool use = d < D;
+      st->x[d] = use ? (double*)take(8 * C) : nullptr;
+      st->v[d] = use ? (double*)take(8 * C) : nullptr;
+      st->a[d] = use ? (double*)take(8 * C) : nullptr;
+      st->xs[d] = use ? (double*)take(8 * C) : nullptr;
+    }
+    st->rho = (double*)take(8 * C);
+    st->rho_ref = (double*)take(8 * C);
+    st->P = (double*)take(8 * C);
+    st->Pr = (double*)take(8 * C);
+    st->type = (int*)take(4 * C);
+    st->rid = (int*)take(4 * C);
+    st->cell = (int*)take(4 * C);
+    st->oid = (long long*)take(8 * C);
+    st->pl = (float4*)take(16 * C);
+  }
+  BinScratch& b = s->b;
+  b.keys = (int*)take(4 * C);
+  b.slots = (int*)take(4 * C);
+  b.perm_tmp = (int*)take(4 * C);
+  b.rid_tmp = (int*)take(4 * C);
+  b.perm = (int*)take(4 * C);
+  b.rid_sorted = (int*)take(4 * C);
+  b.flag_by_rid = (int*)take(4 * C);
+  b.rem_list = (int*)take(4 * C);
+  b.ident = (int*)take(4 * C);
+  b.moved_to = (int*)take(4 * C);
+  b.inv_rid = (int*)take(4 * C);
+  s->staging = take(72 * C + 64);
+  return off;
+}
+
+int ensure_capacity(sph_system* s, int n) {
+  if (n <= s->cap && s->arena) return SPH_OK;
+  if (s->arena) {
+    CK(cudaStreamSynchronize(s->stream));
+    CK(cudaFree(s->arena));
+    s->arena = nullptr;
+    s->cap = 0;
+  }
+  const size_t C = (size_t)(n > 0 ? n : 1);
+  const size_t bytes = carve(s, nullptr, C);
+  void* p = nullptr;
+  if (cudaMalloc(&p, bytes) != cudaSuccess) {
+    cudaGetLastError();
+    return fail(s, SPH_ERR_NOMEM, "cannot allocate %zu bytes of device memory for %d particles",
+                bytes, n);
+  }
+  s->arena = p;
+  carve(s, (char*)p, C);
+  s->cap = (int)C;
+  return SPH_OK;
+}
+
+int read_count(sph_system* s, int* n) {
+  CK(cudaMemcpyAsync(n, s->b.d_n, sizeof(int), cudaMemcpyDeviceToHost, s->stream));
+  CK(cudaStreamSynchronize(s->stream));
+  s->n_host = *n;
+  return SPH_OK;
+}
+
+int pair_pass(sph_system* s, int op, int self, int reset, int fuse_eos) {
+  cudaError_t e;
+  if (s->params.precision == SPH_PREC_MIXED)
+    e = launch_pair_mixed(ctx(s), s->cur, s->geo, s->k, s->b, s->n_host, op, self, reset, fuse_eos);
+  else
+    e = launch_pair_fp64(ctx(s), s->cur, s->geo, s->k, s->b, s->n_host, op, self, reset, fuse_eos);
+  if (e == cudaErrorNotSupported)
+    return fail(s, SPH_ERR_UNSUPPORTED, "pair operator %d is not provided in this precision", op);
+  if (e != cudaSuccess) return fail(s, SPH_ERR_CUDA, "pair pass launch: %s", cudaGetErrorString(e));
+  return SPH_OK;
+}
+
+int binning(sph_system* s, int step_mode, int gather_mode) {
+  cudaError_t e = launch_binning(ctx(s), s->cur, s->alt, s->geo, s->k, s->b, s->n_host, step_mode,
+                                 gather_mode);
+  if (e != cudaSuccess) return fail(s, SPH_ERR_CUDA, "binning launch: %s", cudaGetErrorString(e));
+  std::swap(s->cur, s->alt);
+  s->cells_valid = true;
+  return SPH_OK;
+}
+
+int unary(sph_system* s, int op) {
+  cudaError_t e = launch_unary(ctx(s), s->cur, s->k, s->b, s->n_host, op);
+  if (e != cudaSuccess) return fail(s, SPH_ERR_CUDA, "unary launch: %s", cudaGetErrorString(e));
+  if (op == SPH_OP_DRIFT) s->cells_valid = false;
+  return SPH_OK;
+}
+
+bool vector_field(int f) {
+  return f == SPH_FIELD_X || f == SPH_FIELD_V || f == SPH_FIELD_A || f == SPH_FIELD_XSPH;
+}
+
+size_t field_bytes(int f, size_t n) {
+  if (vector_field(f)) return 24 * n;
+  if (f == SPH_FIELD_TYPE) return 4 * n;
+  return 8 * n;
+}
+
+struct DeviceGuard {
+  int prev = -1;
+  explicit DeviceGuard(int dev) {
+    cudaGetDevice(&prev);
+    if (prev != dev) cudaSetDevice(dev);
+  }
+  ~DeviceGuard() {
+    int cur = -1;
+    cudaGetDevice(&cur);
+    if (prev >= 0 && cur != prev) cudaSetDevice(prev);
+  }
+};
+
+}  // namespace
+
+extern "C" {
+
+int sph_abi_version(void) { return SPHGPU_ABI_VERSION; }
+
+const char* sph_last_error(const sph_system* s) { return s ? s->err.c_str() : "null handle"; }
+
+int sph_create(const sph_params* p, int device, sph_system** out) {
+  if (!p || !out) return SPH_ERR_ARG;
+  *out = nullptr;
+  if (p->dim != 2 && p->dim != 3) return SPH_ERR_ARG;
+  if (!(p->h > 0.0)) return SPH_ERR_ARG;  // structs.jl:59
+  if (p->precision != SPH_PREC_FP64 && p->precision != SPH_PREC_MIXED) return SPH_ERR_ARG;
+  if (p->vertical_axis < 0 || p->vertical_axis >= p->dim) return SPH_ERR_ARG;
+  for (int d = 0; d < 3; ++d)
+    if (!(p->domain_min[d] <= p->domain_max[d])) return SPH_ERR_ARG;
+  if (p->dim == 2 && (p->domain_min[2] > 0.0 || p->domain_max[2] < 0.0)) return SPH_ERR_ARG;
+  int ndev = 0;
+  if (cudaGetDeviceCount(&ndev) != cudaSuccess || device < 0 || device >= ndev) {
+    cudaGetLastError();
+    return SPH_ERR_CUDA;
+  }
+  sph_system* s = new sph_system();
+  s->params = *p;
+  s->device = device;
+  DeviceGuard guard(device);
+  // structs.jl:64-82
+  const double H = p->h;
+  long long key_max = 1;
+  for (int d = 0; d < 3; ++d) {
+    s->geo.key_phase[d] = (long long)std::floor(p->domain_min[d] / H);
+    s->geo.key_lim[d] = (long long)std::floor(p->domain_max[d] / H) - s->geo.key_phase[d] + 1;
+    key_max *= s->geo.key_lim[d];
+  }
+  if (key_max <= 0 || key_max > 0x7fffffffLL - 8) {
+    delete s;
+    return SPH_ERR_ARG;  // the cell table must be indexable with int32
+  }
+  s->geo.key_max = (int)key_max;
+  int nd = 0;
+  const long long L0 = s->geo.key_lim[0], L1 = s->geo.key_lim[1];
+  if (s->geo.key_lim[2] == 1) {
+    for (int di = -1; di <= 1; ++di)
+      for (int dj = -1; dj <= 1; ++dj) s->geo.key_diff[nd++] = (int)(di + L0 * dj);
+  } else {
+    for (int di = -1; di <= 1; ++di)
+      for (int dj = -1; dj <= 1; ++dj)
+        for (int dk = -1; dk <= 1; ++dk) s->geo.key_diff[nd++] = (int)(di + L0 * (dj + L1 * dk));
+  }
+  s->geo.n_diff = nd;
+  // derived constants: same expressions as the CPU restatement
+  Consts& k = s->k;
+  k.dim = p->dim;
+  k.h = H;
+  k.inv_h = 1.0 / H;
+  const double h2 = H * H;
+  if (p->dim == 2) {
+    k.cw = 2.228169203286535 / h2;
+    k.cr = -44.563384065730695 / (h2 * h2);
+  } else {
+    k.cw = 3.3422538049298023 / (h2 * H);
+    k.cr = -66.84507609859604 / ((h2 * h2) * H);
+  }
+  k.mass = p->mass;
+  k.rho0 = p->rho0;
+  k.B = ((p->c0 * p->c0) * p->rho0) / 7.0;
+  k.hdt = 0.5 * p->dt;
+  k.dt = p->dt;
+  k.eta2 = 0.01 * (p->h_smooth * p->h_smooth);
+  k.alpha_c0 = p->alpha * p->c0;
+  k.h_smooth = p->h_smooth;
+  k.eps_xsph = p->eps_xsph;
+  k.gmag = std::fabs(p->gravity[p->vertical_axis]);
+  k.col_height = p->col_height;
+  k.vaxis = p->vertical_axis;
+  for (int d = 0; d < 3; ++d) {
+    k.g[d] = p->gravity[d];
+    k.dmin[d] = p->domain_min[d];
+    k.dmax[d] = p->domain_max[d];
+  }
+  const double band = 1.0 / 16384.0;  // 2^-14, see sph_pair64.cu
+  k.hf = (float)H;
+  k.s_lo = (float)(h2 * (1.0 - band));
+  k.s_hi = (float)(h2 * (1.0 + band));
+  k.inv_hf = (float)k.inv_h;
+  k.cwf = (float)k.cw;
+  k.crf = (float)k.cr;
+  k.massf = (float)k.mass;
+  k.eta2f = (float)k.eta2;
+  k.alpha_c0f = (float)k.alpha_c0;
+  k.h_smoothf = (float)k.h_smooth;
+  k.rho0f = (float)k.rho0;
+  for (int d = 0; d < 3; ++d) k.gf[d] = (float)k.g[d];
+
+  if (cudaStreamCreateWithFlags(&s->stream, cudaStreamNonBlocking) != cudaSuccess) {
+    cudaGetLastError();
+    delete s;
+    return SPH_ERR_CUDA;
+  }
+  const size_t nb = (size_t)s->geo.key_max + 3;
+  const size_t scan_ints = scan_tmp_ints((int)nb) + 64;
+  size_t bytes = align_up(4 * nb) * 2 + align_up(4 * scan_ints) + 2048;
+  void* cells = nullptr;
+  if (cudaMalloc(&cells, bytes) != cudaSuccess) {
+    cudaGetLastError();
+    cudaStreamDestroy(s->stream);
+    delete s;
+    return SPH_ERR_NOMEM;
+  }
+  s->cells = cells;
+  char* c = (char*)cells;
+  s->b.counts = (int*)c;
+  c += align_up(4 * nb);
+  s->b.cell_start = (int*)c;
+  c += align_up(4 * nb);
+  s->b.scan_tmp = (int*)c;
+  c += align_up(4 * scan_ints);
+  s->b.d_n = (int*)c;
+  s->b.d_nrem = (int*)(c + 256);
+  s->b.d_err = (int*)(c + 512);
+  s->b.d_pairs = (unsigned long long*)(c + 768);
+  s->b.d_cat = (unsigned long long*)(c + 1024);
+  if (cudaMemsetAsync(cells, 0, bytes, s->stream) != cudaSuccess ||
+      cudaStreamSynchronize(s->stream) != cudaSuccess) {
+    cudaGetLastError();
+    cudaFree(cells);
+    cudaStreamDestroy(s->stream);
+    delete s;
+    return SPH_ERR_CUDA;
+  }
+  *out = s;
+  return SPH_OK;
+}
+
+int sph_destroy(sph_system* s) {
+  if (!s) return SPH_ERR_ARG;
+  DeviceGuard guard(s->device);
+  cudaStreamSynchronize(s->stream);
+  for (auto& p : s->pending) {
+    cudaEventDestroy(p.start);
+    cudaEventDestroy(p.stop);
+  }
+  for (auto e : s->pool) cudaEventDestroy(e);
+  if (s->open_start) cudaEventDestroy(s->open_start);
+  if (s->arena) cudaFree(s->arena);
+  if (s->cells) cudaFree(s->cells);
+  if (s->query) cudaFree(s->query);
+  cudaStreamDestroy(s->stream);
+  delete s;
+  return SPH_OK;
+}
+
+int sph_geometry(const sph_system* s, int64_t key_phase[3], int64_t key_lim[3], int64_t* key_max,
+                 int64_t key_diff[27], int32_t* n_diff) {
+  if (!s || !key_phase || !key_lim || !key_max || !key_diff || !n_diff) return SPH_ERR_ARG;
+  for (int d = 0; d < 3; ++d) {
+    key_phase[d] = s->geo.key_phase[d];
+    key_lim[d] = s->geo.key_lim[d];
+  }
+  *key_max = s->geo.key_max;
+  for (int i = 0; i < s->geo.n_diff; ++i) key_diff[i] = s->geo.key_diff[i];
+  *n_diff = s->geo.n_diff;
+  return SPH_OK;
+}
+
+int sph_upload(sph_system* s, int64_t n, const double* x, const double* v, const double* rho,
+               const double* rho_ref, const int32_t* type) {
+  if (!s) return SPH_ERR_ARG;
+  if (n < 0 || n > 0x7fffffffLL - 64) return fail(s, SPH_ERR_ARG, "invalid particle count %lld", (long long)n);
+  if (n > 0 && !x) return fail(s, SPH_ERR_ARG, "x is null");
+  if (s->params.dim == 2) {
+    for (int64_t i = 0; i < n; ++i)
+      if (x[3 * i + 2] != 0.0 || (v && v[3 * i + 2] != 0.0))
+        return fail(s, SPH_ERR_ARG, "2D system: particle %lld has a nonzero z component", (long long)i);
+  }
+  if (type)
+    for (int64_t i = 0; i < n; ++i)
+      if (type[i] != SPH_FLUID && type[i] != SPH_WALL)
+        return fail(s, SPH_ERR_ARG, "particle %lld has unknown type %d", (long long)i, type[i]);
+  DeviceGuard guard(s->device);
+  int rc = ensure_capacity(s, (int)n);
+  if (rc) return rc;
+  char* st = (char*)s->staging;
+  const size_t N = (size_t)n;
+  double* dx = (double*)st;
+  double* dv = (double*)(st + 24 * N);
+  double* drho = (double*)(st + 48 * N);
+  double* drr = (double*)(st + 56 * N);
+  int* dtype = (int*)(st + 64 * N);
+  if (n > 0) {
+    CK(cudaMemcpyAsync(dx, x, 24 * N, cudaMemcpyHostToDevice, s->stream));
+    if (v) CK(cudaMemcpyAsync(dv, v, 24 * N, cudaMemcpyHostToDevice, s->stream));
+    if (rho) CK(cudaMemcpyAsync(drho, rho, 8 * N, cudaMemcpyHostToDevice, s->stream));
+    if (rho_ref) CK(cudaMemcpyAsync(drr, rho_ref, 8 * N, cudaMemcpyHostToDevice, s->stream));
+    if (type) CK(cudaMemcpyAsync(dtype, type, 4 * N, cudaMemcpyHostToDevice, s->stream));
+  }
+  cudaError_t e = launch_upload(ctx(s), s->cur, s->k, s->b, (int)n, dx, v ? dv : nullptr,
+                                rho ? drho : nullptr, rho_ref ? drr : nullptr,
+                                type ? dtype : nullptr);
+  if (e != cudaSuccess) return fail(s, SPH_ERR_CUDA, "upload: %s", cudaGetErrorString(e));
+  CK(cudaStreamSynchronize(s->stream));
+  s->n_host = (int)n;
+  s->cells_valid = false;
+  return SPH_OK;
+}
+
+int sph_num_particles(sph_system* s, int64_t* n) {
+  if (!s || !n) return SPH_ERR_ARG;
+  DeviceGuard guard(s->device);
+  int c = 0;
+  int rc = read_count(s, &c);
+  if (rc) return rc;
+  *n = c;
+  return SPH_OK;
+}
+
+int sph_get_field(sph_system* s, int field, void* out) {
+  if (!s || !out) return SPH_ERR_ARG;
+  if (field < SPH_FIELD_X || field > SPH_FIELD_KEY) return fail(s, SPH_ERR_ARG, "unknown field %d", field);
+  DeviceGuard guard(s->device);
+  int n = 0;
+  int rc = read_count(s, &n);
+  if (rc) return rc;
+  if (n == 0) return SPH_OK;
+  cudaError_t e = launch_field(ctx(s), s->cur, s->k, s->b, s->n_host, field, 0, s->staging);
+  if (e != cudaSuccess) return fail(s, SPH_ERR_CUDA, "field: %s", cudaGetErrorString(e));
+  CK(cudaMemcpyAsync(out, s->staging, field_bytes(field, n), cudaMemcpyDeviceToHost, s->stream));
+  CK(cudaStreamSynchronize(s->stream));
+  return SPH_OK;
+}
+
+int sph_set_field(sph_system* s, int field, const void* in) {
+  if (!s || !in) return SPH_ERR_ARG;
+  if (field < SPH_FIELD_X || field > SPH_FIELD_TYPE)
+    return fail(s, SPH_ERR_ARG, "field %d cannot be set", field);
+  DeviceGuard guard(s->device);
+  int n = 0;
+  int rc = read_count(s, &n);
+  if (rc) return rc;
+  if (n == 0) return SPH_OK;
+  if (s->params.dim == 2 && (field == SPH_FIELD_X || field == SPH_FIELD_V)) {
+    const double* v = (const double*)in;
+    for (int i = 0; i < n; ++i)
+      if (v[3 * i + 2] != 0.0)
+        return fail(s, SPH_ERR_ARG, "2D system: particle %d has a nonzero z component", i);
+  }
+  if (field == SPH_FIELD_TYPE) {
+    const int32_t* t = (const int32_t*)in;
+    for (int i = 0; i < n; ++i)
+      if (t[i] != SPH_FLUID && t[i] != SPH_WALL)
+        return fail(s, SPH_ERR_ARG, "particle %d has unknown type %d", i, t[i]);
+  }
+  CK(cudaMemcpyAsync(s->staging, in, field_bytes(field, n), cudaMemcpyHostToDevice, s->stream));
+  cudaError_t e = launch_field(ctx(s), s->cur, s->k, s->b, s->n_host, field, 1, s->staging);
+  if (e != cudaSuccess) return fail(s, SPH_ERR_CUDA, "field: %s", cudaGetErrorString(e));
+  CK(cudaStreamSynchronize(s->stream));
+  if (field == SPH_FIELD_X) s->cells_valid = false;
+  return SPH_OK;
+}
+
+int sph_create_cell_list(sph_system* s) {
+  if (!s) return SPH_ERR_ARG;
+  DeviceGuard guard(s->device);
+  return binning(s, 0, kGatherAll);
+}
+
+int sph_apply(sph_system* s, int op, int self) {
+  if (!s) return SPH_ERR_ARG;
+  if (op != SPH_OP_DENSITY && op != SPH_OP_DENSITY_REF && op != SPH_OP_FORCE &&
+      op != SPH_OP_WALL_PRESSURE) {
+    if (op >= SPH_OP_RESET_RHO && op <= SPH_OP_HYDROSTATIC) return sph_apply_unary(s, op);
+    return fail(s, SPH_ERR_ARG, "unknown operator %d", op);
+  }
+  if (!s->cells_valid)
+    return fail(s, SPH_ERR_STATE, "positions changed since create_cell_list!; call it first");
+  DeviceGuard guard(s->device);
+  return pair_pass(s, op, self ? 1 : 0, 0, 0);
+}
+
+int sph_apply_unary(sph_system* s, int op) {
+  if (!s) return SPH_ERR_ARG;
+  if (op < SPH_OP_RESET_RHO || op > SPH_OP_HYDROSTATIC)
+    return fail(s, SPH_ERR_ARG, "unknown unary operator %d", op);
+  DeviceGuard guard(s->device);
+  return unary(s, op);
+}
+
+static int sum_common(sph_system* s, int func, int64_t nq, const double* x, const int64_t* idx,
+                      double* out) {
+  if (!s || (nq > 0 && !out) || nq < 0) return SPH_ERR_ARG;
+  if (func < SPH_SUM_DENSITY || func > SPH_SUM_SHEPARD) return fail(s, SPH_ERR_ARG, "unknown sum function %d", func);
+  if (!s->cells_valid) return fail(s, SPH_ERR_STATE, "cell list is stale; call create_cell_list! first");
+  if (nq == 0) return SPH_OK;
+  if (nq > 0x7fffffffLL / 4) return fail(s, SPH_ERR_ARG, "too many query points");
+  DeviceGuard guard(s->device);
+  int n = 0;
+  if (idx) {
+    int rc = read_count(s, &n);
+    if (rc) return rc;
+    for (int64_t i = 0; i < nq; ++i)
+      if (idx[i] < 0 || idx[i] >= n) return fail(s, SPH_ERR_ARG, "particle index %lld out of range", (long long)idx[i]);
+  }
+  const size_t need = (size_t)nq * 32;
+  if (need > s->query_bytes) {
+    if (s->query) CK(cudaFree(s->query));
+    s->query = nullptr;
+    s->query_bytes = 0;
+    if (cudaMalloc(&s->query, need) != cudaSuccess) {
+      cudaGetLastError();
+      return fail(s, SPH_ERR_NOMEM, "cannot allocate the query buffer");
+    }
+    s->query_bytes = need;
+  }
+  double* dq = s->query;                         // nq x 3 points or nq indices
+  double* dout = s->query + 3 * (size_t)nq;      // nq results
+  if (idx)
+    CK(cudaMemcpyAsync(dq, idx, 8 * (size_t)nq, cudaMemcpyHostToDevice, s->stream));
+  else
+    CK(cudaMemcpyAsync(dq, x, 24 * (size_t)nq, cudaMemcpyHostToDevice, s->stream));
+  cudaError_t e = launch_sum(ctx(s), s->cur, s->geo, s->k, s->b, func, (int)nq,
+                             idx ? nullptr : dq, idx ? (const long long*)dq : nullptr, dout);
+  if (e != cudaSuccess) return fail(s, SPH_ERR_CUDA, "sum: %s", cudaGetErrorString(e));
+  CK(cudaMemcpyAsync(out, dout, 8 * (size_t)nq, cudaMemcpyDeviceToHost, s->stream));
+  CK(cudaStreamSynchronize(s->stream));
+  return SPH_OK;
+}
+
+int sph_sum_point(sph_system* s, int func, int64_t nq, const double* x, double* out) {
+  if (nq > 0 && !x) return SPH_ERR_ARG;
+  return sum_common(s, func, nq, x, nullptr, out);
+}
+
+int sph_sum_particle(sph_system* s, int func, int64_t nq, const int64_t* index, double* out) {
+  if (nq > 0 && !index) return SPH_ERR_ARG;
+  return sum_common(s, func, nq, nullptr, index, out);
+}
+
+int sph_step(sph_system* s, int nsteps) {
+  if (!s || nsteps < 0) return SPH_ERR_ARG;
+  DeviceGuard guard(s->device);
+  for (int it = 0; it < nsteps; ++it) {
+    int rc = binning(s, 1, kGatherStep);  // kick + drift + create_cell_list!
+    if (rc) return rc;
+    rc = pair_pass(s, SPH_OP_DENSITY, 1, 1, 1);  // reset_rho!, find_rho!(self), EOS
+    if (rc) return rc;
+    rc = pair_pass(s, SPH_OP_WALL_PRESSURE, 0, 0, 0);
+    if (rc) return rc;
+    rc = pair_pass(s, SPH_OP_FORCE, 0, 1, 0);  // reset_a!, internal_force!
+    if (rc) return rc;
+    rc = unary(s, SPH_OP_KICK);
+    if (rc) return rc;
+  }
+  return SPH_OK;
+}
+
+int sph_init_state(sph_system* s) {
+  if (!s) return SPH_ERR_ARG;
+  DeviceGuard guard(s->device);
+  int rc = binning(s, 0, kGatherAll);
+  if (!rc) rc = unary(s, SPH_OP_RESET_RHO_REF);
+  if (!rc) rc = pair_pass(s, SPH_OP_DENSITY_REF, 1, 0, 0);
+  if (!rc) rc = unary(s, SPH_OP_HYDROSTATIC);
+  if (!rc) rc = unary(s, SPH_OP_RESET_RHO);
+  if (!rc) rc = pair_pass(s, SPH_OP_DENSITY, 1, 0, 0);
+  if (!rc) rc = unary(s, SPH_OP_EOS);
+  if (!rc) rc = pair_pass(s, SPH_OP_WALL_PRESSURE, 0, 0, 0);
+  if (!rc) rc = unary(s, SPH_OP_RESET_A);
+  if (!rc) rc = pair_pass(s, SPH_OP_FORCE, 0, 0, 0);
+  return rc;
+}
+
+int sph_pair_count(sph_system* s, uint64_t* pairs, int reset) {
+  if (!s || !pairs) return SPH_ERR_ARG;
+  DeviceGuard guard(s->device);
+  unsigned long long v = 0;
+  CK(cudaMemcpyAsync(&v, s->b.d_pairs, sizeof v, cudaMemcpyDeviceToHost, s->stream));
+  if (reset) CK(cudaMemsetAsync(s->b.d_pairs, 0, sizeof v, s->stream));
+  CK(cudaStreamSynchronize(s->stream));
+  *pairs = v;
+  return SPH_OK;
+}
+
+int sph_pair_stats(sph_system* s, uint64_t counts[8], int reset) {
+  if (!s || !counts) return SPH_ERR_ARG;
+  DeviceGuard guard(s->device);
+  unsigned long long v[kNumCat];
+  CK(cudaMemcpyAsync(v, s->b.d_cat, sizeof v, cudaMemcpyDeviceToHost, s->stream));
+  if (reset) CK(cudaMemsetAsync(s->b.d_cat, 0, sizeof v, s->stream));
+  CK(cudaStreamSynchronize(s->stream));
+  for (int i = 0; i < kNumCat; ++i) counts[i] = v[i];
+  return SPH_OK;
+}
+
+int sph_synchronize(sph_system* s) {
+  if (!s) return SPH_ERR_ARG;
+  DeviceGuard guard(s->device);
+  CK(cudaStreamSynchronize(s->stream));
+  int errbits = 0;
+  CK(cudaMemcpyAsync(&errbits, s->b.d_err, sizeof(int), cudaMemcpyDeviceToHost, s->stream));
+  CK(cudaStreamSynchronize(s->stream));
+  if (errbits) {
+    CK(cudaMemsetAsync(s->b.d_err, 0, sizeof(int), s->stream));
+    CK(cudaStreamSynchronize(s->stream));
+    return fail(s, SPH_ERR_DEVICE, "device error bits 0x%x", errbits);
+  }
+  return SPH_OK;
+}
+
+int sph_stream(sph_system* s, void** stream) {
+  if (!s || !stream) return SPH_ERR_ARG;
+  *stream = (void*)s->stream;
+  return SPH_OK;
+}
+
+int sph_debug_pairs(sph_system* s, int64_t* pairs, int64_t cap, int64_t* count) {
+  if (!s || !count || cap < 0 || (cap > 0 && !pairs)) return SPH_ERR_ARG;
+  if (!s->cells_valid) return fail(s, SPH_ERR_STATE, "cell list is stale; call create_cell_list! first");
+  DeviceGuard guard(s->device);
+  int n = 0;
+  int rc = read_count(s, &n);
+  if (rc) return rc;
+  *count = 0;
+  if (n == 0) return SPH_OK;
+  int* dcounts = (int*)s->staging;
+  long long* doff = (long long*)((char*)s->staging + align_up(4 * (size_t)n));
+  cudaError_t e = launch_debug_pairs(ctx(s), s->cur, s->geo, s->k, s->b, s->n_host, 0, dcounts,
+                                     nullptr, nullptr, 0);
+  if (e != cudaSuccess) return fail(s, SPH_ERR_CUDA, "pairs: %s", cudaGetErrorString(e));
+  std::vector<int> hc(n);
+  std::vector<long long> ho(n);
+  CK(cudaMemcpyAsync(hc.data(), dcounts, 4 * (size_t)n, cudaMemcpyDeviceToHost, s->stream));
+  CK(cudaStreamSynchronize(s->stream));
+  long long total = 0;
+  for (int i = 0; i < n; ++i) {
+    ho[i] = total;
+    total += hc[i];
+  }
+  *count = total;
+  if (cap == 0) return SPH_OK;
+  CK(cudaMemcpyAsync(doff, ho.data(), 8 * (size_t)n, cudaMemcpyHostToDevice, s->stream));
+  const long long m = total < cap ? total : cap;
+  long long* dpairs = nullptr;
+  if (cudaMalloc(&dpairs, 16 * (size_t)(m > 0 ? m : 1)) != cudaSuccess) {
+    cudaGetLastError();
+    return fail(s, SPH_ERR_NOMEM, "cannot allocate the pair list");
+  }
+  e = launch_debug_pairs(ctx(s), s->cur, s->geo, s->k, s->b, s->n_host, 1, dcounts, doff, dpairs, m);
+  cudaError_t e2 = cudaMemcpyAsync(pairs, dpairs, 16 * (size_t)m, cudaMemcpyDeviceToHost, s->stream);
+  cudaError_t e3 = cudaStreamSynchronize(s->stream);
+  cudaFree(dpairs);
+  if (e != cudaSuccess || e2 != cudaSuccess || e3 != cudaSuccess)
+    return fail(s, SPH_ERR_CUDA, "pair list transfer failed");
+  return SPH_OK;
+}
+
+int sph_set_profiling(sph_system* s, int on) {
+  if (!s) return SPH_ERR_ARG;
+  s->profiling = on != 0;
+  return SPH_OK;
+}
+
+int sph_kernel_stats(sph_system* s, int kernel, double* total_ms, int64_t* launches) {
+  if (!s || kernel < 0 || kernel >= SPH_KERNEL_COUNT) return SPH_ERR_ARG;
+  DeviceGuard guard(s->device);
+  int rc = flush_profile(s);
+  if (rc) return rc;
+  if (total_ms) *total_ms = s->total_ms[kernel];
+  if (launches) *launches = s->kernel_launches[kernel];
+  return SPH_OK;
+}
+
+int sph_reset_kernel_stats(sph_system* s) {
+  if (!s) return SPH_ERR_ARG;
+  DeviceGuard guard(s->device);
+  int rc = flush_profile(s);
+  if (rc) return rc;
+  for (int i = 0; i < SPH_KERNEL_COUNT; ++i) {
+    s->total_ms[i] = 0.0;
+    s->kernel_launches[i] = 0;
+  }
+  return SPH_OK;
+}
+
+int sph_launch_count(sph_system* s, int64_t* launches) {
+  if (!s || !launches) return SPH_ERR_ARG;
+  *launches = s->total_launches;
+  return SPH_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,149 @@
+// sph_common.cuh -- device-side data layout and helpers shared by the kernels.
+//
+// Layout in HBM (struct of arrays, sorted by cell after every binning):
+//   x[d], v[d], a[d], xs[d]   double, one array per component (d < DIM)
+//   rho, rho_ref, P, Pr       double (Pr = P / rho^2, precomputed per particle)
+//   type, rid, cell           int32 (rid = index in the reference's particle
+//                             order; cell = 1-based linear cell key)
+//   oid                       int64 (index at upload time)
+//   pl                        float4: position relative to the origin of the
+//                             particle's own cell (FP32) and the type bits in .w
+// Two such sets (cur / alt) are ping-ponged by the reorder gather.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+namespace sphgpu {
+
+constexpr int kFluid = 0;
+constexpr int kWall = 1;
+
+// device error bits (sticky until read by sph_synchronize)
+constexpr int kErrBounds = 1;     // a cell or particle index left its table
+constexpr int kErrKeyRange = 2;   // a particle inside the box produced a key outside 1..key_max
+
+struct State {
+  double* x[3];
+  double* v[3];
+  double* a[3];
+  double* xs[3];
+  double* rho;
+  double* rho_ref;
+  double* P;
+  double* Pr;
+  int* type;
+  int* rid;
+  int* cell;
+  long long* oid;
+  float4* pl;
+};
+
+// Cell-table geometry (structs.jl:66-82).  key_max and key_diff fit int32
+// (checked when the system is created).
+struct Geometry {
+  long long key_phase[3];
+  long long key_lim[3];
+  int key_max;
+  int n_diff;
+  int key_diff[27];
+};
+
+// Constants derived once on the host, with the same expressions as the oracle.
+struct Consts {
+  double h, inv_h, cw, cr;
+  double mass, rho0, B, hdt, dt, eta2, alpha_c0, h_smooth, eps_xsph;
+  double gmag, col_height;
+  double g[3];
+  double dmin[3], dmax[3];
+  int vaxis;
+  int dim;
+  // FP32 candidate classification (see the pair kernels): a candidate whose
+  // FP32 squared distance lies below s_lo is inside the support, above s_hi
+  // outside; in between the FP64 test decides.
+  float hf, s_lo, s_hi;
+  // FP32 copies for the mixed-precision pair arithmetic
+  float inv_hf, cwf, crf, massf, eta2f, alpha_c0f, h_smoothf, rho0f;
+  float gf[3];
+};
+
+// Scratch of the binning (counting sort by cell key).
+struct BinScratch {
+  int* keys;        // per particle (storage order before the sort)
+  int* slots;       // rank of the particle inside its cell's bucket (atomic)
+  int* counts;      // key_max + 3 bucket counts
+  int* cell_start;  // key_max + 3 exclusive prefix sums of counts
+  int* perm_tmp;    // bucketed old index
+  int* rid_tmp;     // bucketed reference index (after removal remap)
+  int* perm;        // final old index for every new slot
+  int* rid_sorted;  // final reference index for every new slot
+  int* flag_by_rid; // removal flags indexed by reference index
+  int* rem_list;    // removed reference indices, ascending
+  int* ident;       // identity permutation used by the tail-fill replay
+  int* moved_to;    // new reference index of a survivor moved from the tail
+  int* inv_rid;     // storage index of every reference index
+  int* d_n;         // particle count (device-resident)
+  int* d_nrem;      // particles removed by the last binning
+  int* d_err;       // error bits
+  int* scan_tmp;    // block sums of the scans
+  unsigned long long* d_pairs;
+  // hits per category: [0] density sums, [1] wall pressure (fluid q),
+  // [2] force fluid-fluid, [3] force fluid-wall, [4] force with viscosity
+  unsigned long long* d_cat;
+};
+
+constexpr int kCatDensity = 0;
+constexpr int kCatWall = 1;
+constexpr int kCatForceFluid = 2;
+constexpr int kCatForceWall = 3;
+constexpr int kCatForceAV = 4;
+constexpr int kNumCat = 8;
+
+__device__ __forceinline__ void decode_key(const Geometry& g, int key, int& cx, int& cy, int& cz) {
+  const int k0 = key - 1;
+  const int l0 = (int)g.key_lim[0];
+  const int l1 = (int)g.key_lim[1];
+  cx = k0 % l0;
+  const int t = k0 / l0;
+  cy = t % l1;
+  cz = t / l1;
+}
+
+// kernels.jl:108-115 / :156-163 in the evaluation order written in the oracle
+__device__ __forceinline__ double ker_w(const Consts& k, double r) {
+  const double x = r * k.inv_h;
+  if (x > 1.0) return 0.0;
+  const double t = 1.0 - x;
+  const double t2 = t * t;
+  const double t4 = t2 * t2;
+  return (k.cw * t4) * (1.0 + 4.0 * x);
+}
+// kernels.jl:140-147 / :188-195
+__device__ __forceinline__ double ker_rdw(const Consts& k, double r) {
+  const double x = r * k.inv_h;
+  if (x > 1.0) return 0.0;
+  const double t = 1.0 - x;
+  const double t2 = t * t;
+  return k.cr * (t2 * t);
+}
+
+// structs.jl:97-106 for an arbitrary point: -1 when a coordinate is NaN,
+// infinite or outside the Int64 range (the reference's try/catch).
+__device__ __forceinline__ long long find_key_point(const Geometry& g, const Consts& k,
+                                                    const double x[3]) {
+  long long ijk[3];
+  for (int d = 0; d < 3; ++d) {
+    const double f = floor(x[d] / k.h);
+    if (!(f >= -9223372036854775808.0 && f < 9223372036854775808.0)) return -1;
+    ijk[d] = 1 + (long long)f - g.key_phase[d];
+  }
+  return ijk[0] + g.key_lim[0] * (ijk[1] - 1) + g.key_lim[0] * g.key_lim[1] * (ijk[2] - 1);
+}
+
+__device__ __forceinline__ unsigned lanemask_lt() {
+  unsigned m;
+  asm("mov.u32 %0, %%lanemask_lt;" : "=r"(m));
+  return m;
+}
+
+}  // namespace sphgpu

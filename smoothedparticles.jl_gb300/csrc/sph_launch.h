@@ -1,0 +1,73 @@
+// sph_launch.h -- host-side launchers of the device kernels (one per kernel
+// family); the C ABI in sph_api.cu strings them together.
+#pragma once
+
+#include "sph_common.cuh"
+
+namespace sphgpu {
+
+// Launch context: the stream plus an optional hook called around every kernel
+// launch (profiling events and the launch counter live in the API layer).
+struct LaunchCtx {
+  cudaStream_t stream;
+  void* owner;
+  // phase 0 before the launches of one kernel family, phase 1 after them;
+  // `kernels` (phase 1 only) is how many kernels were launched in between.
+  void (*mark)(void* owner, int kernel, int phase, int kernels);
+};
+
+inline void mark(const LaunchCtx& c, int kernel, int phase, int kernels = 1) {
+  if (c.mark) c.mark(c.owner, kernel, phase, kernels);
+}
+
+// Fields moved by the reorder gather.
+constexpr int kGatherAll = 1;   // every field (create_cell_list!)
+constexpr int kGatherStep = 0;  // only what survives a fused step (x, v, rho_ref, ids)
+
+// ---- binning (sph_bin.cu)
+// Whole create_cell_list!: keys (optionally with the fused kick + drift),
+// removal replay, counting sort by cell, per-cell descending reference-index
+// order, reorder gather cur -> alt.  `cap` bounds the particle count.
+cudaError_t launch_binning(const LaunchCtx& c, const State& cur, const State& alt,
+                           const Geometry& g, const Consts& k, const BinScratch& b, int cap,
+                           int step_mode, int gather_mode);
+// Exclusive prefix sum of len ints (in and out may not alias).
+cudaError_t launch_scan(const LaunchCtx& c, const int* in, int* out, int len, int* tmp);
+size_t scan_tmp_ints(int len);
+
+// ---- FP64 pair passes (sph_pair64.cu)
+// op: SPH_OP_DENSITY / SPH_OP_DENSITY_REF / SPH_OP_FORCE.  reset: start the
+// accumulators at 0 (the folded reset_*! of a step) instead of the stored
+// values; fuse_eos: apply the Tait EOS in the density epilogue.
+cudaError_t launch_pair_fp64(const LaunchCtx& c, const State& s, const Geometry& g,
+                             const Consts& k, const BinScratch& b, int cap, int op, int self,
+                             int reset, int fuse_eos);
+// ---- mixed-precision pair passes (sph_pair32.cu)
+cudaError_t launch_pair_mixed(const LaunchCtx& c, const State& s, const Geometry& g,
+                              const Consts& k, const BinScratch& b, int cap, int op, int self,
+                              int reset, int fuse_eos);
+// sum(sys, func, x) at nq device points (x: nq x 3) or, when rid_query is not
+// null, at particles given by reference index.
+cudaError_t launch_sum(const LaunchCtx& c, const State& s, const Geometry& g, const Consts& k,
+                       const BinScratch& b, int func, int nq, const double* x,
+                       const long long* rid_query, double* out);
+// Neighbour pairs in the reference order: pass 0 counts per reference index,
+// pass 1 writes (rid_p, rid_q) at offsets[rid_p].
+cudaError_t launch_debug_pairs(const LaunchCtx& c, const State& s, const Geometry& g,
+                               const Consts& k, const BinScratch& b, int cap, int pass,
+                               int* counts, const long long* offsets, long long* pairs,
+                               long long cap_pairs);
+
+// ---- unary operators and field transfer (sph_unary.cu)
+cudaError_t launch_unary(const LaunchCtx& c, const State& s, const Consts& k,
+                         const BinScratch& b, int cap, int op);
+// Upload: staging (reference order, AoS n x 3 for vectors) -> SoA state.
+cudaError_t launch_upload(const LaunchCtx& c, const State& s, const Consts& k,
+                          const BinScratch& b, int n, const double* x, const double* v,
+                          const double* rho, const double* rho_ref, const int* type);
+// Field copy between the SoA state and a reference-ordered staging buffer.
+// dir 0: state -> staging, 1: staging -> state.
+cudaError_t launch_field(const LaunchCtx& c, const State& s, const Consts& k,
+                         const BinScratch& b, int cap, int field, int dir, void* staging);
+
+}  // namespace sphgpu

@@ -1,0 +1,318 @@
+"""sphgpu -- host-side mirror of SmoothedParticles.jl's cell-list / pair-loop
+surface over the GB300 C ABI (include/sphgpu.h).
+
+Names follow the reference (src/SmoothedParticles.jl:9-72) with Julia's ``!``
+dropped: ``ParticleSystem`` (structs.jl:57), ``create_cell_list``
+(core.jl:51), ``apply`` (core.jl:151), ``apply_unary`` (core.jl:138),
+``apply_binary`` (core.jl:125), ``sum`` (core.jl:240, :271) and
+``ParticleField`` (structs.jl:118).  Operators are the built-in ones below;
+arbitrary closures have no device counterpart and nothing runs on the CPU.
+Errors raise ``SphError`` (the reference throws Julia exceptions).
+"""
+from __future__ import annotations
+
+import ctypes as C
+from dataclasses import dataclass
+
+import numpy as np
+
+from . import _lib as L
+from ._lib import (SPH_FLUID as FLUID, SPH_WALL as WALL, SPH_PREC_FP64 as FP64,
+                   SPH_PREC_MIXED as MIXED)
+
+__all__ = ["ParticleSystem", "ParticleField", "create_cell_list", "apply", "apply_unary",
+           "apply_binary", "sum", "SphError", "Operator", "SumFunction", "FLUID", "WALL",
+           "FP64", "MIXED", "find_rho", "find_rho0", "internal_force", "find_pressure",
+           "reset_rho", "reset_rho0", "reset_a", "accelerate", "move", "hydrostatic",
+           "DENSITY", "KERNEL", "PRESSURE", "SHEPARD", "wall_pressure"]
+
+
+class SphError(RuntimeError):
+    def __init__(self, code: int, msg: str):
+        super().__init__(f"sphgpu error {code}: {msg}")
+        self.code = code
+
+
+@dataclass(frozen=True)
+class Operator:
+    """A built-in operator; ``binary`` mirrors hasmethod(op!, (T, T, Float64))."""
+    name: str
+    op: int
+    binary: bool
+
+
+@dataclass(frozen=True)
+class SumFunction:
+    name: str
+    func: int
+
+
+# pair operators (the examples' find_rho!, find_rho0!, internal_force!)
+find_rho = Operator("find_rho!", L.SPH_OP_DENSITY, True)
+find_rho0 = Operator("find_rho0!", L.SPH_OP_DENSITY_REF, True)
+internal_force = Operator("internal_force!", L.SPH_OP_FORCE, True)
+wall_pressure = Operator("wall_pressure!", L.SPH_OP_WALL_PRESSURE, True)
+# unary operators
+find_pressure = Operator("find_pressure!", L.SPH_OP_EOS, False)
+reset_rho = Operator("reset_rho!", L.SPH_OP_RESET_RHO, False)
+reset_rho0 = Operator("reset_rho0!", L.SPH_OP_RESET_RHO_REF, False)
+reset_a = Operator("reset_a!", L.SPH_OP_RESET_A, False)
+accelerate = Operator("accelerate!", L.SPH_OP_KICK, False)
+move = Operator("move!", L.SPH_OP_DRIFT, False)
+hydrostatic = Operator("hydrostatic!", L.SPH_OP_HYDROSTATIC, False)
+# functions for sum()
+DENSITY = SumFunction("density", L.SPH_SUM_DENSITY)
+KERNEL = SumFunction("kernel", L.SPH_SUM_KERNEL)
+PRESSURE = SumFunction("pressure", L.SPH_SUM_PRESSURE)
+SHEPARD = SumFunction("shepard", L.SPH_SUM_SHEPARD)
+
+_FIELDS = {"x": L.SPH_FIELD_X, "v": L.SPH_FIELD_V, "a": L.SPH_FIELD_A,
+           "xsph": L.SPH_FIELD_XSPH, "rho": L.SPH_FIELD_RHO, "rho0": L.SPH_FIELD_RHO_REF,
+           "rho_ref": L.SPH_FIELD_RHO_REF, "P": L.SPH_FIELD_P, "type": L.SPH_FIELD_TYPE,
+           "oid": L.SPH_FIELD_OID, "key": L.SPH_FIELD_KEY}
+_VECTOR = {L.SPH_FIELD_X, L.SPH_FIELD_V, L.SPH_FIELD_A, L.SPH_FIELD_XSPH}
+
+
+def _ptr(a):
+    return None if a is None else C.c_void_p(a.ctypes.data)
+
+
+class ParticleSystem:
+    """ParticleSystem(T, domain, h) (structs.jl:57-92) on one GPU.
+
+    ``params`` holds the domain bounding box, the neighbour radius ``h`` (the
+    kernel support) and the physical constants of the built-in operators.
+    """
+
+    def __init__(self, params: dict, precision: int = FP64, device: int = 0):
+        self._lib = L.load()
+        self.params = dict(params)
+        self.precision = precision
+        p = L.make_params(L.sph_params, params, precision)
+        h = C.c_void_p()
+        rc = self._lib.sph_create(C.byref(p), int(device), C.byref(h))
+        if rc != 0:
+            raise SphError(rc, "sph_create failed (invalid parameters or no CUDA device)")
+        self._h = h
+        self.dim = int(params["dim"])
+
+    # -- lifetime
+    def close(self):
+        if getattr(self, "_h", None):
+            self._lib.sph_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def _check(self, rc: int):
+        if rc != 0:
+            msg = self._lib.sph_last_error(self._h)
+            raise SphError(rc, msg.decode() if msg else "")
+
+    # -- geometry and particles
+    def geometry(self):
+        kp = (C.c_int64 * 3)()
+        kl = (C.c_int64 * 3)()
+        km = C.c_int64()
+        kd = (C.c_int64 * 27)()
+        nd = C.c_int32()
+        self._check(self._lib.sph_geometry(self._h, kp, kl, C.byref(km), kd, C.byref(nd)))
+        return dict(key_phase=tuple(kp), key_lim=tuple(kl), key_max=km.value,
+                    key_diff=list(kd)[: nd.value])
+
+    def upload(self, x, v=None, rho=None, rho_ref=None, type=None):
+        """generate_particles! (grids.jl:253-258): replaces the particle set."""
+        x = np.ascontiguousarray(x, dtype=np.float64).reshape(-1, 3)
+        n = x.shape[0]
+        v = None if v is None else np.ascontiguousarray(v, dtype=np.float64).reshape(n, 3)
+        rho = None if rho is None else np.ascontiguousarray(rho, dtype=np.float64).reshape(n)
+        rr = None if rho_ref is None else np.ascontiguousarray(rho_ref, dtype=np.float64).reshape(n)
+        t = None if type is None else np.ascontiguousarray(type, dtype=np.int32).reshape(n)
+        self._keep = (x, v, rho, rr, t)
+        self._check(self._lib.sph_upload(self._h, n, _ptr(x), _ptr(v), _ptr(rho), _ptr(rr), _ptr(t)))
+        self._keep = None
+
+    @property
+    def n(self) -> int:
+        c = C.c_int64()
+        self._check(self._lib.sph_num_particles(self._h, C.byref(c)))
+        return c.value
+
+    def get(self, name: str) -> np.ndarray:
+        f = _FIELDS[name]
+        n = self.n
+        if f in _VECTOR:
+            out = np.empty((n, 3), np.float64)
+        elif f == L.SPH_FIELD_TYPE:
+            out = np.empty(n, np.int32)
+        elif f in (L.SPH_FIELD_OID, L.SPH_FIELD_KEY):
+            out = np.empty(n, np.int64)
+        else:
+            out = np.empty(n, np.float64)
+        if n:
+            self._check(self._lib.sph_get_field(self._h, f, _ptr(out)))
+        return out
+
+    def set(self, name: str, values):
+        f = _FIELDS[name]
+        n = self.n
+        if f in _VECTOR:
+            a = np.ascontiguousarray(values, dtype=np.float64).reshape(n, 3)
+        elif f == L.SPH_FIELD_TYPE:
+            a = np.ascontiguousarray(values, dtype=np.int32).reshape(n)
+        else:
+            a = np.ascontiguousarray(values, dtype=np.float64).reshape(n)
+        if n:
+            self._check(self._lib.sph_set_field(self._h, f, _ptr(a)))
+
+    # -- the per-step path
+    def create_cell_list(self):
+        self._check(self._lib.sph_create_cell_list(self._h))
+
+    def apply(self, op: Operator, self_term: bool = False):
+        self._check(self._lib.sph_apply(self._h, op.op, 1 if self_term else 0))
+
+    def apply_unary(self, op: Operator):
+        self._check(self._lib.sph_apply_unary(self._h, op.op))
+
+    def sum_points(self, func: SumFunction, x) -> np.ndarray:
+        x = np.ascontiguousarray(x, dtype=np.float64).reshape(-1, 3)
+        out = np.empty(x.shape[0], np.float64)
+        self._check(self._lib.sph_sum_point(self._h, func.func, x.shape[0], _ptr(x), _ptr(out)))
+        return out
+
+    def sum_particles(self, func: SumFunction, index) -> np.ndarray:
+        idx = np.ascontiguousarray(index, dtype=np.int64).reshape(-1)
+        out = np.empty(idx.shape[0], np.float64)
+        self._check(self._lib.sph_sum_particle(self._h, func.func, idx.shape[0], _ptr(idx), _ptr(out)))
+        return out
+
+    def step(self, nsteps: int = 1):
+        """verlet_step! (collapse_symplectic.jl:170-180), nsteps times."""
+        self._check(self._lib.sph_step(self._h, int(nsteps)))
+
+    def init_state(self):
+        """The dam-break initialisation (collapse_symplectic.jl:186-191 + hydrostatic)."""
+        self._check(self._lib.sph_init_state(self._h))
+
+    # -- accounting and diagnostics
+    def pair_count(self, reset: bool = False) -> int:
+        c = C.c_uint64()
+        self._check(self._lib.sph_pair_count(self._h, C.byref(c), 1 if reset else 0))
+        return c.value
+
+    def synchronize(self):
+        self._check(self._lib.sph_synchronize(self._h))
+
+    def stream(self) -> int:
+        p = C.c_void_p()
+        self._check(self._lib.sph_stream(self._h, C.byref(p)))
+        return p.value or 0
+
+    def debug_pairs(self) -> np.ndarray:
+        cnt = C.c_int64()
+        self._check(self._lib.sph_debug_pairs(self._h, None, 0, C.byref(cnt)))
+        out = np.empty((cnt.value, 2), np.int64)
+        if cnt.value:
+            self._check(self._lib.sph_debug_pairs(self._h, _ptr(out), cnt.value, C.byref(cnt)))
+        return out
+
+    def set_profiling(self, on: bool = True):
+        self._check(self._lib.sph_set_profiling(self._h, 1 if on else 0))
+
+    def kernel_stats(self) -> dict:
+        out = {}
+        for k, name in enumerate(L.KERNEL_NAMES):
+            ms = C.c_double()
+            nl = C.c_int64()
+            self._check(self._lib.sph_kernel_stats(self._h, k, C.byref(ms), C.byref(nl)))
+            out[name] = (ms.value, nl.value)
+        return out
+
+    def reset_kernel_stats(self):
+        self._check(self._lib.sph_reset_kernel_stats(self._h))
+
+    def launch_count(self) -> int:
+        c = C.c_int64()
+        self._check(self._lib.sph_launch_count(self._h, C.byref(c)))
+        return c.value
+
+    def pair_stats(self, reset: bool = False) -> dict:
+        """Hits per category: density, wall (pressure pass), force_fluid,
+        force_wall, force_av."""
+        v = (C.c_uint64 * 8)()
+        self._check(self._lib.sph_pair_stats(self._h, v, 1 if reset else 0))
+        return dict(density=v[0], wall=v[1], force_fluid=v[2], force_wall=v[3], force_av=v[4])
+
+
+def pipe_peak(which: str, device: int = 0) -> float:
+    """Measured issue rate (thread-instructions/s) of 'dfma', 'ffma' or 'dadd'."""
+    lib = L.load()
+    out = C.c_double()
+    rc = lib.sph_pipe_peak(device, {"dfma": 0, "ffma": 1, "dadd": 2}[which], C.byref(out))
+    if rc != 0:
+        raise SphError(rc, "sph_pipe_peak failed")
+    return out.value
+
+
+class ParticleField:
+    """ParticleField(sys, :var) (structs.jl:118-125) as a whole-array view."""
+
+    def __init__(self, sys: ParticleSystem, var: str):
+        self.sys = sys
+        self.var = var
+
+    def __array__(self, dtype=None, copy=None):
+        a = self.sys.get(self.var)
+        return a if dtype is None else a.astype(dtype)
+
+    def __len__(self):
+        return self.sys.n
+
+    def __getitem__(self, i):
+        return self.sys.get(self.var)[i]
+
+
+def create_cell_list(sys: ParticleSystem):
+    """create_cell_list!(sys) -- core.jl:51-90."""
+    sys.create_cell_list()
+
+
+def apply(sys: ParticleSystem, op: Operator, self: bool = False):
+    """apply!(sys, op!; self) -- core.jl:151-161: binary or unary by operator."""
+    if op.binary:
+        sys.apply(op, self)
+    else:
+        sys.apply_unary(op)
+
+
+def apply_binary(sys: ParticleSystem, op: Operator):
+    """apply_binary!(sys, op!) -- core.jl:125-129."""
+    if not op.binary:
+        raise SphError(L.SPH_ERR_ARG, f"{op.name} is not a pair operator")
+    sys.apply(op, False)
+
+
+def apply_unary(sys: ParticleSystem, op: Operator):
+    """apply_unary!(sys, op!) -- core.jl:138-142."""
+    if op.binary:
+        raise SphError(L.SPH_ERR_ARG, f"{op.name} is not a unary operator")
+    sys.apply_unary(op)
+
+
+def sum(sys: ParticleSystem, func: SumFunction, x=None, particles=None):
+    """sum(sys, func, x) (core.jl:240-260) at points, or sum(sys, func, p)
+    (core.jl:271-291) for particles given by reference index."""
+    if particles is not None:
+        return sys.sum_particles(func, particles)
+    return sys.sum_points(func, x)

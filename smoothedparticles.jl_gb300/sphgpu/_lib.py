@@ -1,0 +1,159 @@
+"""ctypes binding of libsphgpu.so (the C ABI declared in include/sphgpu.h).
+
+The library is built in-tree (``smoothedparticles.jl_gb300/libsphgpu.so``) by
+``sphgpu.build.build_library``.  Loading fails loudly when it is missing: there
+is no CPU fallback for any operation.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+PKG_ROOT = os.path.dirname(HERE)
+LIB_PATH = os.path.join(PKG_ROOT, "libsphgpu.so")
+
+# status codes
+SPH_OK = 0
+SPH_ERR_ARG = -1
+SPH_ERR_CUDA = -2
+SPH_ERR_STATE = -3
+SPH_ERR_NOMEM = -4
+SPH_ERR_DEVICE = -5
+SPH_ERR_UNSUPPORTED = -6
+SPH_ERR_TIMEOUT = -7
+SPH_ERR_BUDGET = -8
+
+SPH_FLUID = 0
+SPH_WALL = 1
+SPH_PREC_FP64 = 0
+SPH_PREC_MIXED = 1
+
+SPH_OP_DENSITY = 1
+SPH_OP_DENSITY_REF = 2
+SPH_OP_FORCE = 3
+SPH_OP_WALL_PRESSURE = 4
+SPH_OP_RESET_RHO = 10
+SPH_OP_RESET_RHO_REF = 11
+SPH_OP_RESET_A = 12
+SPH_OP_EOS = 13
+SPH_OP_KICK = 14
+SPH_OP_DRIFT = 15
+SPH_OP_HYDROSTATIC = 16
+
+SPH_SUM_DENSITY = 1
+SPH_SUM_KERNEL = 2
+SPH_SUM_PRESSURE = 3
+SPH_SUM_SHEPARD = 4
+
+SPH_FIELD_X = 1
+SPH_FIELD_V = 2
+SPH_FIELD_A = 3
+SPH_FIELD_XSPH = 4
+SPH_FIELD_RHO = 5
+SPH_FIELD_RHO_REF = 6
+SPH_FIELD_P = 7
+SPH_FIELD_TYPE = 8
+SPH_FIELD_OID = 9
+SPH_FIELD_KEY = 10
+
+KERNEL_NAMES = ["bin_keys", "bin_remove", "bin_scan", "bin_scatter", "bin_rank", "bin_gather",
+                "density", "force", "unary", "sum", "io", "wall_pressure"]
+SPH_KERNEL_COUNT = len(KERNEL_NAMES)
+
+
+class sph_params(C.Structure):
+    _fields_ = [
+        ("dim", C.c_int32),
+        ("precision", C.c_int32),
+        ("h", C.c_double),
+        ("domain_min", C.c_double * 3),
+        ("domain_max", C.c_double * 3),
+        ("mass", C.c_double),
+        ("rho0", C.c_double),
+        ("c0", C.c_double),
+        ("h_smooth", C.c_double),
+        ("alpha", C.c_double),
+        ("eps_xsph", C.c_double),
+        ("gravity", C.c_double * 3),
+        ("dt", C.c_double),
+        ("col_height", C.c_double),
+        ("vertical_axis", C.c_int32),
+        ("reserved", C.c_int32),
+    ]
+
+
+def make_params(cls, p: dict, precision: int = 0):
+    """Fills a params structure (``sph_params`` or the oracle's twin) from a dict."""
+    s = cls()
+    s.dim = int(p["dim"])
+    s.precision = int(precision)
+    s.h = float(p["h"])
+    for d in range(3):
+        s.domain_min[d] = float(p["domain_min"][d])
+        s.domain_max[d] = float(p["domain_max"][d])
+        s.gravity[d] = float(p["gravity"][d])
+    for name in ("mass", "rho0", "c0", "h_smooth", "alpha", "eps_xsph", "dt", "col_height"):
+        setattr(s, name, float(p[name]))
+    s.vertical_axis = int(p["vertical_axis"])
+    s.reserved = 0
+    return s
+
+
+_P = C.c_void_p
+_I64 = C.c_int64
+_I32 = C.c_int32
+_DP = C.POINTER(C.c_double)
+
+# name -> (restype, argtypes)
+PROTOTYPES = {
+    "sph_abi_version": (C.c_int, []),
+    "sph_last_error": (C.c_char_p, [_P]),
+    "sph_create": (C.c_int, [C.POINTER(sph_params), C.c_int, C.POINTER(_P)]),
+    "sph_destroy": (C.c_int, [_P]),
+    "sph_geometry": (C.c_int, [_P, C.POINTER(_I64), C.POINTER(_I64), C.POINTER(_I64),
+                               C.POINTER(_I64), C.POINTER(_I32)]),
+    "sph_upload": (C.c_int, [_P, _I64, _P, _P, _P, _P, _P]),
+    "sph_num_particles": (C.c_int, [_P, C.POINTER(_I64)]),
+    "sph_get_field": (C.c_int, [_P, C.c_int, _P]),
+    "sph_set_field": (C.c_int, [_P, C.c_int, _P]),
+    "sph_create_cell_list": (C.c_int, [_P]),
+    "sph_apply": (C.c_int, [_P, C.c_int, C.c_int]),
+    "sph_apply_unary": (C.c_int, [_P, C.c_int]),
+    "sph_sum_point": (C.c_int, [_P, C.c_int, _I64, _P, _P]),
+    "sph_sum_particle": (C.c_int, [_P, C.c_int, _I64, _P, _P]),
+    "sph_step": (C.c_int, [_P, C.c_int]),
+    "sph_init_state": (C.c_int, [_P]),
+    "sph_pair_count": (C.c_int, [_P, C.POINTER(C.c_uint64), C.c_int]),
+    "sph_synchronize": (C.c_int, [_P]),
+    "sph_stream": (C.c_int, [_P, C.POINTER(_P)]),
+    "sph_debug_pairs": (C.c_int, [_P, _P, _I64, C.POINTER(_I64)]),
+    "sph_set_profiling": (C.c_int, [_P, C.c_int]),
+    "sph_kernel_stats": (C.c_int, [_P, C.c_int, C.POINTER(C.c_double), C.POINTER(_I64)]),
+    "sph_reset_kernel_stats": (C.c_int, [_P]),
+    "sph_launch_count": (C.c_int, [_P, C.POINTER(_I64)]),
+    "sph_pair_stats": (C.c_int, [_P, C.POINTER(C.c_uint64), C.c_int]),
+    "sph_pipe_peak": (C.c_int, [C.c_int, C.c_int, C.POINTER(C.c_double)]),
+}
+
+_lib = None
+
+
+def load(path: str | None = None):
+    """Loads libsphgpu.so (once) and declares every prototype."""
+    global _lib
+    if _lib is not None and path is None:
+        return _lib
+    p = path or os.environ.get("SPHGPU_LIB", LIB_PATH)
+    if not os.path.exists(p):
+        raise RuntimeError(
+            f"libsphgpu.so not found at {p}: build it first (sphgpu.build.build_library()); "
+            "there is no CPU fallback")
+    lib = C.CDLL(p)
+    for name, (res, args) in PROTOTYPES.items():
+        f = getattr(lib, name)
+        f.restype = res
+        f.argtypes = args
+    if path is None:
+        _lib = lib
+    return lib
