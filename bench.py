@@ -198,24 +198,10 @@ def run_reference(args):
     return 0
 
 
-def run_ours(args):
-    import torch
-
-    import sphgpu
-    rank, world, local = dist_env()
-    if world > 1:
-        import torch.distributed as dist
-        torch.cuda.set_device(local)
-        dist.init_process_group("nccl")
-    dev = local
-    torch.cuda.set_device(dev)
-    case = make_case(args)
-    g = sphgpu.ParticleSystem(case.params, sphgpu.FP64, device=dev)
-    g.upload(case.x, case.v, type=case.type)
-    g.init_state()
+def timed_steps(g, torch, dev, steps, world):
+    """K steps between CUDA events on the handle's stream (after a barrier),
+    with per-kernel event timing and nvidia-smi clock sampling."""
     stream = torch.cuda.ExternalStream(g.stream(), device=dev)
-    for _ in range(args.warmup):
-        g.step(1)
     g.synchronize()
     g.pair_count(reset=True)
     g.pair_stats(reset=True)
@@ -229,82 +215,164 @@ def run_ours(args):
     e1 = torch.cuda.Event(enable_timing=True)
     with ClockSampler(dev) as clk:
         e0.record(stream)
-        for _ in range(args.steps):
+        for _ in range(steps):
             g.step(1)
         e1.record(stream)
         e1.synchronize()
     torch.cuda.synchronize(dev)
     ms = e0.elapsed_time(e1)
-    launches = g.launch_count() - l0
+    out = dict(ms=ms, launches=g.launch_count() - l0, clocks=clk.summary())
     g.set_profiling(False)
-    pairs = g.pair_count(reset=True)
-    cats = g.pair_stats(reset=True)
-    kstats = g.kernel_stats()
+    out["pairs"] = g.pair_count(reset=True)
+    out["cats"] = g.pair_stats(reset=True)
+    out["kernels"] = {k: v for k, v in g.kernel_stats().items() if v[1] > 0}
     g.synchronize()
-    ms_max = ms
-    pairs_all = pairs
-    if world > 1:
-        import torch.distributed as dist
-        t = torch.tensor([ms], device=f"cuda:{dev}")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms_max = float(t.item())
-        pt = torch.tensor([float(pairs)], device=f"cuda:{dev}", dtype=torch.float64)
-        dist.all_reduce(pt)
-        pairs_all = float(pt.item())
-    value = pairs_all / (ms_max * 1e-3)
+    return out
 
-    # ---- end to end through the C ABI with pinned host buffers
-    n = g.n
-    pin = lambda shape, dt: torch.empty(shape, dtype=dt, pin_memory=True).numpy()
-    hx, hv, ha, hs = (pin((n, 3), torch.float64) for _ in range(4))
-    hrho, hP = pin((n,), torch.float64), pin((n,), torch.float64)
-    hx[:] = g.get("x"); hv[:] = g.get("v"); ha[:] = g.get("a"); hs[:] = g.get("xsph")
-    g.pair_count(reset=True)
-    torch.cuda.synchronize(dev)
-    t0 = time.perf_counter()
-    for _ in range(args.e2e_steps):
-        g.set("x", hx); g.set("v", hv); g.set("a", ha); g.set("xsph", hs)
-        g.step(1)
-        hx[:] = g.get("x"); hv[:] = g.get("v"); ha[:] = g.get("a")
-        hrho[:] = g.get("rho"); hP[:] = g.get("P")
-        hs[:] = g.get("xsph")
-    t_e2e = time.perf_counter() - t0
-    e2e_pairs = g.pair_count(reset=True)
-    e2e = {"value": e2e_pairs / t_e2e, "unit": UNIT,
-           "h2d_bytes_per_step": int(n * 4 * 24), "d2h_bytes_per_step": int(n * (4 * 24 + 2 * 8)),
-           "steps": args.e2e_steps,
-           "note": "per step: set x, v, a, xsph from pinned host arrays; sph_step; get x, v, a, "
-                   "xsph, rho, P into pinned host arrays (reference particle order)"}
 
-    # ---- roofline of the dominant kernel (the FP64 force pass)
-    names = {k: v for k, v in kstats.items() if v[1] > 0}
-    dom = max(names, key=lambda k: names[k][0])
-    dfma = sphgpu.pipe_peak("dfma", dev)
-    peak_tflops = 2.0 * dfma / 1e12
+def kernel_table(kst, cats):
     flops = {
         "force": cats["force_fluid"] * FLOPS["force_fluid"] + cats["force_wall"] * FLOPS["force_wall"]
         + cats["force_av"] * FLOPS["force_av"],
         "density": cats["density"] * FLOPS["density"],
         "wall_pressure": cats["wall"] * FLOPS["wall"],
     }
-    kern_rows = {}
-    for k, (tms, nl) in names.items():
+    tot = sum(v[0] for v in kst.values())
+    rows = {}
+    for k, (tms, nl) in kst.items():
         row = {"ms_total": round(tms, 3), "launches": nl, "ms_avg": round(tms / nl, 4),
-               "share": round(tms / max(1e-9, sum(v[0] for v in names.values())), 4)}
+               "share": round(tms / max(1e-9, tot), 4)}
         if k in flops:
+            row["flops_per_launch"] = flops[k] / nl
             row["tflops"] = round(flops[k] / (tms * 1e-3) / 1e12, 4)
-        kern_rows[k] = row
-    dom_ms = names[dom][0] / names[dom][1]
-    dom_flops = flops.get(dom, 0) / max(1, names[dom][1])
-    achieved = dom_flops / (dom_ms * 1e-3) / 1e12
+        rows[k] = row
+    return rows
+
+
+def field_errors(ref, got):
+    """Per-field error of `got` against `ref` (dicts of reference-ordered arrays)."""
+    out = {}
+    for f in ("rho", "P", "a", "xsph", "x", "v"):
+        a, b = ref[f], got[f]
+        if a.ndim == 2:
+            diff = np.linalg.norm(a - b, axis=1)
+            scale = np.linalg.norm(a, axis=1)
+        else:
+            diff = np.abs(a - b)
+            scale = np.abs(a)
+        out[f] = {"max_abs": float(diff.max()), "rel_norm": float(
+            np.linalg.norm(diff) / max(1e-300, np.linalg.norm(scale))),
+            "max_rel": float((diff / np.maximum(scale, 1e-300)).max()) if f in ("rho", "x") else None}
+    return out
+
+
+def run_ours(args):
+    import torch
+
+    import sphgpu
+    rank, world, local = dist_env()
+    if world > 1:
+        import torch.distributed as dist
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl")
+    dev = local
+    torch.cuda.set_device(dev)
+    case = make_case(args)
+    fields = ("x", "v", "a", "xsph", "rho", "P")
+
+    # ---- FP64 drop-in: device-resident steps
+    g = sphgpu.ParticleSystem(case.params, sphgpu.FP64, device=dev)
+    g.upload(case.x, case.v, type=case.type)
+    g.init_state()
+    for _ in range(args.warmup):
+        g.step(1)
+    snap = {f: g.get(f) for f in ("x", "v", "a", "xsph")}  # state entering the timed run
+    r64 = timed_steps(g, torch, dev, args.steps, world)
+    ms_max, pairs_all = r64["ms"], r64["pairs"]
+    if world > 1:
+        import torch.distributed as dist
+        t = torch.tensor([ms_max], device=f"cuda:{dev}")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms_max = float(t.item())
+        pt = torch.tensor([float(pairs_all)], device=f"cuda:{dev}", dtype=torch.float64)
+        dist.all_reduce(pt)
+        pairs_all = float(pt.item())
+    value = pairs_all / (ms_max * 1e-3)
+    final64 = {f: g.get(f) for f in fields}
+
+    # ---- end to end through the C ABI with pinned host buffers
+    n = g.n
+    pin = lambda shape: torch.empty(shape, dtype=torch.float64, pin_memory=True).numpy()
+    h = {f: pin((n, 3)) for f in ("x", "v", "a", "xsph")}
+    h["rho"], h["P"] = pin((n,)), pin((n,))
+    for f in ("x", "v", "a", "xsph"):
+        g.get(f, out=h[f])
+    g.pair_count(reset=True)
+    torch.cuda.synchronize(dev)
+    t0 = time.perf_counter()
+    for _ in range(args.e2e_steps):
+        for f in ("x", "v", "a", "xsph"):
+            g.set(f, h[f])
+        g.step(1)
+        for f in fields:
+            g.get(f, out=h[f])
+    t_e2e = time.perf_counter() - t0
+    e2e = {"value": g.pair_count(reset=True) / t_e2e, "unit": UNIT,
+           "h2d_bytes_per_step": int(n * 4 * 24), "d2h_bytes_per_step": int(n * (4 * 24 + 2 * 8)),
+           "steps": args.e2e_steps,
+           "note": "per step: set x, v, a, xsph from pinned host arrays; sph_step; get x, v, a, "
+                   "xsph, rho, P into pinned host arrays (reference particle order)"}
+    g.close()
+
+    # ---- mixed precision: same workload, same state entering the timed run
+    gm = sphgpu.ParticleSystem(case.params, sphgpu.MIXED, device=dev)
+    gm.upload(case.x, case.v, type=case.type)
+    gm.init_state()
+    for _ in range(args.warmup):
+        gm.step(1)
+    for f in ("x", "v", "a", "xsph"):
+        gm.set(f, snap[f])
+    rmx = timed_steps(gm, torch, dev, args.steps, world)
+    final_mx = {f: gm.get(f) for f in fields}
+    mixed = {"value": rmx["pairs"] / (rmx["ms"] * 1e-3), "ms_per_step": rmx["ms"] / args.steps,
+             "speedup_vs_fp64": (rmx["pairs"] / rmx["ms"]) / (r64["pairs"] / r64["ms"]),
+             "dtype": "fp32 pair arithmetic, fp64 positions/integration/accumulators",
+             "error_vs_fp64_after_steps": field_errors(final64, final_mx),
+             "kernels": kernel_table(rmx["kernels"], rmx["cats"]),
+             "gpu_launches": rmx["launches"], "clocks": rmx["clocks"]}
+    # one step from identical FP64 state: the per-step error of the mixed arithmetic
+    gm.set("x", final64["x"]); gm.set("v", final64["v"])
+    gm.set("a", final64["a"]); gm.set("xsph", final64["xsph"])
+    gm.step(1)
+    one_mx = {f: gm.get(f) for f in fields}
+    gm.close()
+    g = sphgpu.ParticleSystem(case.params, sphgpu.FP64, device=dev)
+    g.upload(case.x, case.v, type=case.type)
+    g.init_state()
+    g.set("x", final64["x"]); g.set("v", final64["v"])
+    g.set("a", final64["a"]); g.set("xsph", final64["xsph"])
+    g.step(1)
+    one_64 = {f: g.get(f) for f in fields}
+    g.close()
+    mixed["error_vs_fp64_one_step"] = field_errors(one_64, one_mx)
+
+    # ---- roofline of the dominant kernel of the FP64 step (the force pass)
+    kt = kernel_table(r64["kernels"], r64["cats"])
+    dom = max((k for k in kt if "tflops" in kt[k]), key=lambda k: kt[k]["ms_total"])
+    dfma = sphgpu.pipe_peak("dfma", dev)
+    ffma = sphgpu.pipe_peak("ffma", dev)
+    peak_tflops = 2.0 * dfma / 1e12
+    achieved = kt[dom]["flops_per_launch"] / (kt[dom]["ms_avg"] * 1e-3) / 1e12
     roofline = {"bound": "fp64", "kernel": dom, "achieved": round(achieved, 4),
                 "peak": round(peak_tflops, 4), "unit": "TFLOP/s",
                 "frac": round(achieved / peak_tflops, 4),
-                "traffic": NCU_TRAFFIC.get(dom, {}).get("bytes_per_launch_scaled"),
-                "peak_source": "measured in this run: FP64 FMA issue rate x 2 (sph_pipe_peak)",
-                "flops_per_launch": dom_flops,
-                "note": "algorithmic flops count sqrt and division as 1 each; each costs ~10 FP64 "
-                        "pipe slots on GB300"}
+                "traffic": NCU_TRAFFIC.get(dom),
+                "peak_source": "measured in this run: FP64 FMA issue rate x 2 (sph_pipe_peak); "
+                               "MEASURED_PEAKS.json has no FP64 figure",
+                "fp32_peak_tflops": round(2.0 * ffma / 1e12, 3),
+                "flops_per_launch": kt[dom]["flops_per_launch"],
+                "note": "algorithmic flops count sqrt and division as 1 each; on GB300 each costs "
+                        "~10 FP64 pipe slots, and the FP64 parity path cannot fuse mul+add"}
 
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
@@ -317,16 +385,15 @@ def run_ours(args):
             "ms_per_step": ms_max / args.steps, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f64", "data": "synthetic",
             "config": {"workload": workload_name(case), "particles": case.n,
-                       "fluid": case.n_fluid, "pairs_per_step": pairs / args.steps,
+                       "fluid": case.n_fluid, "pairs_per_step": r64["pairs"] / args.steps,
                        "l2": "no flush: 2.6 GB resident state > 129 MB L2",
                        "replicas": world},
             "steps_per_s": 1e3 * args.steps / ms_max,
-            "roofline": roofline, "kernels": kern_rows,
-            "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": launches,
-            "clocks": clk.summary(),
+            "roofline": roofline, "kernels": kt, "mixed": mixed,
+            "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": r64["launches"],
+            "clocks": r64["clocks"],
         }
         print(json.dumps(line), flush=True)
-    g.close()
     if world > 1:
         torch.distributed.destroy_process_group()
     return 0

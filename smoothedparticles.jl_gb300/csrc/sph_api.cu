@@ -28,6 +28,7 @@ struct sph_system {
   int cap = 0;              // particles the arena holds
   int n_host = 0;           // upper bound of the device-resident count
   bool cells_valid = false;
+  bool aux_fresh = false;  // FP32 neighbour copies current (mixed precision)
   std::string err;
   // launch accounting and optional per-kernel CUDA-event timing
   bool profiling = false;
@@ -141,6 +142,8 @@ size_t carve(sph_system* s, char* base, size_t C) {
     st->oid = (long long*)take(8 * C);
     st->pl = (float4*)take(16 * C);
   }
+  s->cur.vr = s->alt.vr = (float4*)take(16 * C);
+  s->cur.rhof = s->alt.rhof = (float*)take(4 * C);
   BinScratch& b = s->b;
   b.keys = (int*)take(4 * C);
   b.slots = (int*)take(4 * C);
@@ -189,12 +192,16 @@ int read_count(sph_system* s, int* n) {
 int pair_pass(sph_system* s, int op, int self, int reset, int fuse_eos) {
   cudaError_t e;
   if (s->params.precision == SPH_PREC_MIXED)
-    e = launch_pair_mixed(ctx(s), s->cur, s->geo, s->k, s->b, s->n_host, op, self, reset, fuse_eos);
+    e = launch_pair_mixed(ctx(s), s->cur, s->geo, s->k, s->b, s->n_host, op, self, reset, fuse_eos,
+                          s->aux_fresh ? 1 : 0);
   else
     e = launch_pair_fp64(ctx(s), s->cur, s->geo, s->k, s->b, s->n_host, op, self, reset, fuse_eos);
   if (e == cudaErrorNotSupported)
     return fail(s, SPH_ERR_UNSUPPORTED, "pair operator %d is not provided in this precision", op);
   if (e != cudaSuccess) return fail(s, SPH_ERR_CUDA, "pair pass launch: %s", cudaGetErrorString(e));
+  // a fused density pass leaves the FP32 copies of the fluid current; a
+  // non-fused one changes rho without P, so the copies are stale
+  if (op == SPH_OP_DENSITY) s->aux_fresh = fuse_eos != 0;
   return SPH_OK;
 }
 
@@ -204,6 +211,7 @@ int binning(sph_system* s, int step_mode, int gather_mode) {
   if (e != cudaSuccess) return fail(s, SPH_ERR_CUDA, "binning launch: %s", cudaGetErrorString(e));
   std::swap(s->cur, s->alt);
   s->cells_valid = true;
+  s->aux_fresh = false;
   return SPH_OK;
 }
 
@@ -211,6 +219,7 @@ int unary(sph_system* s, int op) {
   cudaError_t e = launch_unary(ctx(s), s->cur, s->k, s->b, s->n_host, op);
   if (e != cudaSuccess) return fail(s, SPH_ERR_CUDA, "unary launch: %s", cudaGetErrorString(e));
   if (op == SPH_OP_DRIFT) s->cells_valid = false;
+  s->aux_fresh = false;
   return SPH_OK;
 }
 
@@ -441,6 +450,7 @@ int sph_upload(sph_system* s, int64_t n, const double* x, const double* v, const
   CK(cudaStreamSynchronize(s->stream));
   s->n_host = (int)n;
   s->cells_valid = false;
+  s->aux_fresh = false;
   return SPH_OK;
 }
 
@@ -495,6 +505,7 @@ int sph_set_field(sph_system* s, int field, const void* in) {
   if (e != cudaSuccess) return fail(s, SPH_ERR_CUDA, "field: %s", cudaGetErrorString(e));
   CK(cudaStreamSynchronize(s->stream));
   if (field == SPH_FIELD_X) s->cells_valid = false;
+  s->aux_fresh = false;
   return SPH_OK;
 }
 

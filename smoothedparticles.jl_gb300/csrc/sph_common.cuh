@@ -37,6 +37,10 @@ struct State {
   int* cell;
   long long* oid;
   float4* pl;
+  // FP32 neighbour data of the mixed-precision path, rebuilt every step after
+  // the binning (so not ping-ponged): (vx, vy, vz, P/rho^2) and rho
+  float4* vr;
+  float* rhof;
 };
 
 // Cell-table geometry (structs.jl:66-82).  key_max and key_diff fit int32
@@ -138,6 +142,22 @@ __device__ __forceinline__ long long find_key_point(const Geometry& g, const Con
     ijk[d] = 1 + (long long)f - g.key_phase[d];
   }
   return ijk[0] + g.key_lim[0] * (ijk[1] - 1) + g.key_lim[0] * g.key_lim[1] * (ijk[2] - 1);
+}
+
+// The reference's distance test, r = sqrt((d1*d1 + d2*d2) + d3*d3) and
+// r > h (core.jl:8-10, :105; algebra.jl:49-60), with round-to-nearest
+// intrinsics so that no compiler contraction can change a rounding: the
+// FP64 band test gives the same answer in every translation unit.
+template <int DIM>
+__device__ __forceinline__ bool within_rn(const State& s, const Consts& k, const double* xp, int q) {
+  const double d0 = __dsub_rn(xp[0], __ldg(&s.x[0][q]));
+  const double d1 = __dsub_rn(xp[1], __ldg(&s.x[1][q]));
+  double ss = __dadd_rn(__dmul_rn(d0, d0), __dmul_rn(d1, d1));
+  if (DIM == 3) {
+    const double d2 = __dsub_rn(xp[2], __ldg(&s.x[2][q]));
+    ss = __dadd_rn(ss, __dmul_rn(d2, d2));
+  }
+  return !(__dsqrt_rn(ss) > k.h);
 }
 
 __device__ __forceinline__ unsigned lanemask_lt() {

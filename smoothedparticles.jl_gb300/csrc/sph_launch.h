@@ -43,9 +43,12 @@ cudaError_t launch_pair_fp64(const LaunchCtx& c, const State& s, const Geometry&
                              const Consts& k, const BinScratch& b, int cap, int op, int self,
                              int reset, int fuse_eos);
 // ---- mixed-precision pair passes (sph_pair32.cu)
+// aux_fresh: the FP32 neighbour copies (vr, rhof) of the fluid particles are
+// current (written by a fused density pass since the last state change);
+// otherwise the wall-pressure and force passes rebuild them first.
 cudaError_t launch_pair_mixed(const LaunchCtx& c, const State& s, const Geometry& g,
                               const Consts& k, const BinScratch& b, int cap, int op, int self,
-                              int reset, int fuse_eos);
+                              int reset, int fuse_eos, int aux_fresh);
 // sum(sys, func, x) at nq device points (x: nq x 3) or, when rid_query is not
 // null, at particles given by reference index.
 cudaError_t launch_sum(const LaunchCtx& c, const State& s, const Geometry& g, const Consts& k,

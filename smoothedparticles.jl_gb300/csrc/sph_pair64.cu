@@ -52,13 +52,6 @@ __device__ __forceinline__ double dist2_64(const State& s, const double* xp, int
   return ss;
 }
 
-template <int DIM>
-__device__ __forceinline__ bool exact_within(const State& s, const Consts& k, const double* xp,
-                                             int q) {
-  double d[3];
-  return !(sqrt(dist2_64<DIM>(s, xp, q, d)) > k.h);  // core.jl:105
-}
-
 __device__ __forceinline__ void warp_add(unsigned long long* dst, int v) {
   const int sum = __reduce_add_sync(0xffffffffu, v);
   if ((threadIdx.x & 31) == 0 && sum) atomicAdd(dst, (unsigned long long)sum);
@@ -165,7 +158,7 @@ __global__ void __launch_bounds__(kPairThreads) pair64_kernel(State s, Geometry 
           ss = ss + dz * dz;
         }
         if (ss > k.s_hi || q == i) continue;
-        if (!(ss < k.s_lo) && !exact_within<DIM>(s, k, xp, q)) continue;
+        if (!(ss < k.s_lo) && !within_rn<DIM>(s, k, xp, q)) continue;
         ++pairs;
         const int tq = __float_as_int(pq.w);
         if (OP == SPH_OP_WALL_PRESSURE) {
@@ -375,7 +368,7 @@ __global__ void __launch_bounds__(128) debug_pairs_kernel(State s, Geometry g, C
         ss = ss + dz * dz;
       }
       if (ss > k.s_hi || q == i) continue;
-      if (!(ss < k.s_lo) && !exact_within<DIM>(s, k, xp, q)) continue;
+      if (!(ss < k.s_lo) && !within_rn<DIM>(s, k, xp, q)) continue;
       if (pass && pos < cap_pairs) {
         pairs[2 * pos] = rid;
         pairs[2 * pos + 1] = s.rid[q];

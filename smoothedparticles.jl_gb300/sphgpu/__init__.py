@@ -148,17 +148,23 @@ class ParticleSystem:
         self._check(self._lib.sph_num_particles(self._h, C.byref(c)))
         return c.value
 
-    def get(self, name: str) -> np.ndarray:
+    def get(self, name: str, out: np.ndarray | None = None) -> np.ndarray:
+        """Whole field in reference order; ``out`` (e.g. a pinned host array of
+        the right shape and dtype) receives the data without an extra copy."""
         f = _FIELDS[name]
         n = self.n
         if f in _VECTOR:
-            out = np.empty((n, 3), np.float64)
+            shape, dt = (n, 3), np.float64
         elif f == L.SPH_FIELD_TYPE:
-            out = np.empty(n, np.int32)
+            shape, dt = (n,), np.int32
         elif f in (L.SPH_FIELD_OID, L.SPH_FIELD_KEY):
-            out = np.empty(n, np.int64)
+            shape, dt = (n,), np.int64
         else:
-            out = np.empty(n, np.float64)
+            shape, dt = (n,), np.float64
+        if out is None:
+            out = np.empty(shape, dt)
+        elif out.shape != shape or out.dtype != dt or not out.flags.c_contiguous:
+            raise ValueError(f"out must be a C-contiguous {dt.__name__} array of shape {shape}")
         if n:
             self._check(self._lib.sph_get_field(self._h, f, _ptr(out)))
         return out
