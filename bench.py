@@ -340,20 +340,21 @@ def run_ours(args):
              "error_vs_fp64_after_steps": field_errors(final64, final_mx),
              "kernels": kernel_table(rmx["kernels"], rmx["cats"]),
              "gpu_launches": rmx["launches"], "clocks": rmx["clocks"]}
-    # one step from identical FP64 state: the per-step error of the mixed arithmetic
-    gm.set("x", final64["x"]); gm.set("v", final64["v"])
-    gm.set("a", final64["a"]); gm.set("xsph", final64["xsph"])
-    gm.step(1)
-    one_mx = {f: gm.get(f) for f in fields}
-    gm.close()
+    # one step from an identical FP64 state (reference density included): the
+    # per-step error of the mixed arithmetic
     g = sphgpu.ParticleSystem(case.params, sphgpu.FP64, device=dev)
     g.upload(case.x, case.v, type=case.type)
     g.init_state()
-    g.set("x", final64["x"]); g.set("v", final64["v"])
-    g.set("a", final64["a"]); g.set("xsph", final64["xsph"])
-    g.step(1)
+    rho_ref64 = g.get("rho_ref")
+    for sysm in (g, gm):
+        for f in ("x", "v", "a", "xsph"):
+            sysm.set(f, final64[f])
+        sysm.set("rho_ref", rho_ref64)
+        sysm.step(1)
     one_64 = {f: g.get(f) for f in fields}
+    one_mx = {f: gm.get(f) for f in fields}
     g.close()
+    gm.close()
     mixed["error_vs_fp64_one_step"] = field_errors(one_64, one_mx)
 
     # ---- roofline of the dominant kernel of the FP64 step (the force pass)

@@ -171,7 +171,9 @@ __global__ void __launch_bounds__(kThreads32) pair32_kernel(State s, Geometry g,
         const float kt = kt32(k, r);
         if (e >= 0) ++c0; else ++c1;
         if (OP == SPH_OP_DENSITY || OP == SPH_OP_DENSITY_REF) {
-          f0 += kw32(k, r, kt);
+          // the shape t^4 (1 + 4x) only; m * C_w is applied in FP64 per batch
+          const float t2 = kt * kt;
+          f0 += (t2 * t2) * (5.f - 4.f * kt);
         } else if (OP == SPH_OP_WALL_PRESSURE) {
           const float w = kw32(k, r, kt);
           float gd = k.gf[0] * h.x + k.gf[1] * h.y;
@@ -212,7 +214,7 @@ __global__ void __launch_bounds__(kThreads32) pair32_kernel(State s, Geometry g,
         }
       }
       if (OP == SPH_OP_DENSITY || OP == SPH_OP_DENSITY_REF) {
-        acc += k.mass * (double)f0;
+        acc += (k.mass * k.cw) * (double)f0;
       } else if (OP == SPH_OP_WALL_PRESSURE) {
         wp += (double)f0;
         wg += (double)f1;
