@@ -400,9 +400,10 @@ def run_ours(args):
     return 0
 
 
-# DRAM traffic per launch from the committed ncu summary (profiles/), scaled
-# to the full workload; filled from the capture.
-NCU_TRAFFIC: dict = {}
+# DRAM bytes (read + write) per launch of the FP64 force kernel from the ncu
+# capture summarised in profiles/pair64_force_3d_dr0.02.md (28,297,984 B for
+# 517,040 particles), scaled by particle count to the 5,746,633-particle case.
+NCU_TRAFFIC: dict = {"force": int(28297984 * 5746633 / 517040)}
 
 
 def main():
