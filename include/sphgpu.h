@@ -201,6 +201,36 @@ int sph_kernel_stats(sph_system* sys, int kernel, double* total_ms, int64_t* lau
 int sph_reset_kernel_stats(sph_system* sys);
 /* Kernels launched by this handle since creation. */
 int sph_launch_count(sph_system* sys, int64_t* launches);
+/* ---- allocation-free cell-list build (no counterpart in the reference)
+ *
+ * For callers that must not have the library allocate device memory: a host
+ * whose GPU memory is owned by its own pool or budget (CUDA.jl's allocator, a
+ * serving process that admits work against a fixed HBM budget) cannot let a
+ * library cudaMalloc behind its back -- the allocation escapes the pool's
+ * accounting, may fail mid-run, and cudaMalloc/cudaFree synchronise the
+ * device.  sph_cell_list_noalloc allocates nothing.  Its scratch is one
+ * static device array of about 21 MB that every GPU which loads the library
+ * holds until the process exits; every call shares it, so calls that overlap
+ * on the GPU (different streams, or concurrent host threads) race.  The first
+ * call on a device looks up the array's device address (cudaGetSymbolAddress)
+ * with that device current; make that first call before any stream capture.
+ *
+ * Inputs: params (h and domain_min/max are used), n particles, d_x = device
+ * array of n x 3 doubles.  Outputs (device memory owned by the caller):
+ * d_cell_start[key_max + 2] and d_order[n].  Cell k (1-based key as in
+ * find_key) holds d_order[d_cell_start[k] .. d_cell_start[k+1]), particle
+ * indices in descending order, as create_cell_list! builds its cells when no
+ * particle is removed.  Particles outside the domain's bounding box (NaN
+ * included) are not binned; they follow in d_order[d_cell_start[key_max+1]
+ * .. n), in descending index order.  Work is queued on `stream` (a
+ * cudaStream_t; NULL = default stream) and the call returns without waiting.
+ * Returns SPH_ERR_BUDGET if n > SPH_NOALLOC_MAX_PARTICLES or key_max >
+ * SPH_NOALLOC_MAX_CELLS. */
+#define SPH_NOALLOC_MAX_PARTICLES (1 << 20)
+#define SPH_NOALLOC_MAX_CELLS (1 << 20)
+int sph_cell_list_noalloc(const sph_params* params, int64_t n, const double* d_x,
+                          int32_t* d_cell_start, int32_t* d_order, void* stream);
+
 /* Issue-rate microbenchmark of one arithmetic pipe on `device` (no reference
  * counterpart; the roofline denominators of the pair passes):
  * which = 0 FP64 FMA, 1 FP32 FMA, 2 FP64 add.  Returns thread-instructions/s. */

@@ -134,6 +134,7 @@ PROTOTYPES = {
     "sph_launch_count": (C.c_int, [_P, C.POINTER(_I64)]),
     "sph_pair_stats": (C.c_int, [_P, C.POINTER(C.c_uint64), C.c_int]),
     "sph_pipe_peak": (C.c_int, [C.c_int, C.c_int, C.POINTER(C.c_double)]),
+    "sph_cell_list_noalloc": (C.c_int, [C.POINTER(sph_params), _I64, _P, _P, _P, _P]),
 }
 
 _lib = None
