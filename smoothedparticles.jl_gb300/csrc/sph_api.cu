@@ -29,6 +29,7 @@ struct sph_system {
   int n_host = 0;           // upper bound of the device-resident count
   bool cells_valid = false;
   bool aux_fresh = false;  // FP32 neighbour copies current (mixed precision)
+  bool lists_valid = false;  // hit lists of the last density pass match cells and positions
   std::string err;
   // launch accounting and optional per-kernel CUDA-event timing
   bool profiling = false;
@@ -156,6 +157,16 @@ size_t carve(sph_system* s, char* base, size_t C) {
   b.ident = (int*)take(4 * C);
   b.moved_to = (int*)take(4 * C);
   b.inv_rid = (int*)take(4 * C);
+  b.max_items = max_work_items((int)C, s->geo.key_max);
+  b.items = (int2*)take(8 * (size_t)b.max_items);
+  b.item_partial = (int*)take(4 * (size_t)b.max_items);
+  // hits per target: ~256 in the 3D lattice interior (H = 4 dr), ~68 in 2D
+  // (H = 4.8 dr); the capacity leaves room for compression, and an overflow
+  // only sends that warp back to a full traversal
+  b.hit_cap = D == 3 ? 384 : 160;
+  b.hit_stride = (int)C;
+  b.hits = (int*)take(4 * C * (size_t)b.hit_cap);
+  b.hit_count = (int*)take(4 * C);
   s->staging = take(72 * C + 64);
   return off;
 }
@@ -193,15 +204,18 @@ int pair_pass(sph_system* s, int op, int self, int reset, int fuse_eos) {
   cudaError_t e;
   if (s->params.precision == SPH_PREC_MIXED)
     e = launch_pair_mixed(ctx(s), s->cur, s->geo, s->k, s->b, s->n_host, op, self, reset, fuse_eos,
-                          s->aux_fresh ? 1 : 0);
+                          s->aux_fresh ? 1 : 0, s->lists_valid ? 1 : 0);
   else
-    e = launch_pair_fp64(ctx(s), s->cur, s->geo, s->k, s->b, s->n_host, op, self, reset, fuse_eos);
+    e = launch_pair_fp64(ctx(s), s->cur, s->geo, s->k, s->b, s->n_host, op, self, reset, fuse_eos,
+                         s->lists_valid ? 1 : 0);
   if (e == cudaErrorNotSupported)
     return fail(s, SPH_ERR_UNSUPPORTED, "pair operator %d is not provided in this precision", op);
   if (e != cudaSuccess) return fail(s, SPH_ERR_CUDA, "pair pass launch: %s", cudaGetErrorString(e));
   // a fused density pass leaves the FP32 copies of the fluid current; a
   // non-fused one changes rho without P, so the copies are stale
   if (op == SPH_OP_DENSITY) s->aux_fresh = fuse_eos != 0;
+  // the density passes keep every fluid target's hit list for the force pass
+  if (op == SPH_OP_DENSITY || op == SPH_OP_DENSITY_REF) s->lists_valid = true;
   return SPH_OK;
 }
 
@@ -212,13 +226,17 @@ int binning(sph_system* s, int step_mode, int gather_mode) {
   std::swap(s->cur, s->alt);
   s->cells_valid = true;
   s->aux_fresh = false;
+  s->lists_valid = false;
   return SPH_OK;
 }
 
 int unary(sph_system* s, int op) {
   cudaError_t e = launch_unary(ctx(s), s->cur, s->k, s->b, s->n_host, op);
   if (e != cudaSuccess) return fail(s, SPH_ERR_CUDA, "unary launch: %s", cudaGetErrorString(e));
-  if (op == SPH_OP_DRIFT) s->cells_valid = false;
+  if (op == SPH_OP_DRIFT) {
+    s->cells_valid = false;
+    s->lists_valid = false;
+  }
   s->aux_fresh = false;
   return SPH_OK;
 }
@@ -348,7 +366,7 @@ int sph_create(const sph_params* p, int device, sph_system** out) {
   }
   const size_t nb = (size_t)s->geo.key_max + 3;
   const size_t scan_ints = scan_tmp_ints((int)nb) + 64;
-  size_t bytes = align_up(4 * nb) * 2 + align_up(4 * scan_ints) + 2048;
+  size_t bytes = align_up(4 * nb) * 3 + align_up(4 * scan_ints) + 2048;
   void* cells = nullptr;
   if (cudaMalloc(&cells, bytes) != cudaSuccess) {
     cudaGetLastError();
@@ -361,6 +379,8 @@ int sph_create(const sph_params* p, int device, sph_system** out) {
   s->b.counts = (int*)c;
   c += align_up(4 * nb);
   s->b.cell_start = (int*)c;
+  c += align_up(4 * nb);
+  s->b.item_off = (int*)c;
   c += align_up(4 * nb);
   s->b.scan_tmp = (int*)c;
   c += align_up(4 * scan_ints);
@@ -415,7 +435,8 @@ int sph_geometry(const sph_system* s, int64_t key_phase[3], int64_t key_lim[3], 
 int sph_upload(sph_system* s, int64_t n, const double* x, const double* v, const double* rho,
                const double* rho_ref, const int32_t* type) {
   if (!s) return SPH_ERR_ARG;
-  if (n < 0 || n > 0x7fffffffLL - 64) return fail(s, SPH_ERR_ARG, "invalid particle count %lld", (long long)n);
+  // the pair passes pack a particle index into 27 bits of a queue entry
+  if (n < 0 || n >= (1LL << 27)) return fail(s, SPH_ERR_ARG, "invalid particle count %lld (limit 2^27 - 1)", (long long)n);
   if (n > 0 && !x) return fail(s, SPH_ERR_ARG, "x is null");
   if (s->params.dim == 2) {
     for (int64_t i = 0; i < n; ++i)
@@ -451,6 +472,7 @@ int sph_upload(sph_system* s, int64_t n, const double* x, const double* v, const
   s->n_host = (int)n;
   s->cells_valid = false;
   s->aux_fresh = false;
+  s->lists_valid = false;
   return SPH_OK;
 }
 
@@ -505,6 +527,7 @@ int sph_set_field(sph_system* s, int field, const void* in) {
   if (e != cudaSuccess) return fail(s, SPH_ERR_CUDA, "field: %s", cudaGetErrorString(e));
   CK(cudaStreamSynchronize(s->stream));
   if (field == SPH_FIELD_X) s->cells_valid = false;
+  if (field == SPH_FIELD_X || field == SPH_FIELD_TYPE) s->lists_valid = false;
   s->aux_fresh = false;
   return SPH_OK;
 }

@@ -236,6 +236,24 @@ __global__ void __launch_bounds__(kThreads) bin_gather_kernel(State cur, State a
   }
 }
 
+// ---- pair-pass work list: cell k gets ceil(c_k / 32) items of <= 32 targets
+__global__ void __launch_bounds__(kThreads) items_count_kernel(Geometry g, BinScratch b) {
+  const int k = blockIdx.x * kThreads + threadIdx.x;  // 0 .. key_max + 2
+  if (k > g.key_max + 2) return;
+  int c = 0;
+  if (k >= 1 && k <= g.key_max) c = (b.cell_start[k + 1] - b.cell_start[k] + 31) >> 5;
+  b.counts[k] = c;  // the bucket counts are no longer needed once the starts exist
+}
+
+__global__ void __launch_bounds__(kThreads) items_write_kernel(Geometry g, BinScratch b) {
+  const int k = blockIdx.x * kThreads + threadIdx.x + 1;
+  if (k > g.key_max) return;
+  const int st = b.cell_start[k];
+  const int c = b.cell_start[k + 1] - st;
+  int off = b.item_off[k];
+  for (int t = 0; t < c; t += 32, ++off) b.items[off] = make_int2(st + t, min(32, c - t));
+}
+
 // ---- generic exclusive scan (3 kernels)
 constexpr int kScanThreads = 512;
 constexpr int kScanItems = 8;
@@ -333,6 +351,15 @@ cudaError_t launch_binning(const LaunchCtx& c, const State& cur, const State& al
   const int rank_blocks = (g.key_max + (kThreads / 32) - 1) / (kThreads / 32);
   bin_rank_kernel<<<rank_blocks, kThreads, 0, c.stream>>>(g, b);
   mark(c, SPH_KERNEL_BIN_RANK, 1);
+  // work list of the pair passes (cells are final once the starts exist)
+  mark(c, SPH_KERNEL_BIN_SCAN, 0);
+  items_count_kernel<<<(nbuckets + kThreads - 1) / kThreads, kThreads, 0, c.stream>>>(g, b);
+  mark(c, SPH_KERNEL_BIN_SCAN, 1);
+  e = launch_scan(c, b.counts, b.item_off, nbuckets, b.scan_tmp);
+  if (e != cudaSuccess) return e;
+  mark(c, SPH_KERNEL_BIN_SCAN, 0);
+  items_write_kernel<<<(g.key_max + kThreads - 1) / kThreads, kThreads, 0, c.stream>>>(g, b);
+  mark(c, SPH_KERNEL_BIN_SCAN, 1);
   mark(c, SPH_KERNEL_BIN_GATHER, 0);
   if (k.dim == 2)
     bin_gather_kernel<2><<<blocks, kThreads, 0, c.stream>>>(cur, alt, g, k, b, gather_mode);

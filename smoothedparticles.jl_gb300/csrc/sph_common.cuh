@@ -94,7 +94,26 @@ struct BinScratch {
   // hits per category: [0] density sums, [1] wall pressure (fluid q),
   // [2] force fluid-fluid, [3] force fluid-wall, [4] force with viscosity
   unsigned long long* d_cat;
+  // pair-pass work list: one item per group of <= 32 targets of one cell
+  int2* items;      // (first target, count)
+  int* item_off;    // key_max + 3: exclusive prefix of items per cell
+  int max_items;    // capacity of `items`
+  // hit lists: target i's hits are hits[t * hit_stride + i], t < hit_count[i]
+  // (entry = neighbour index | neighbour-cell number << 27), written by the
+  // density passes and read back by the force pass of the same binning
+  int* hits;
+  int* hit_count;
+  int* item_partial;  // 1 when an item's list overflowed hit_cap
+  int hit_cap;
+  int hit_stride;
 };
+
+// Upper bound of the work-list length for n particles (every cell with
+// particles contributes ceil(c/32) <= c/32 + 1 items).
+inline int max_work_items(int n, int key_max) {
+  const long long b = (long long)n / 32 + (long long)(n < key_max ? n : key_max) + 2;
+  return (int)b;
+}
 
 constexpr int kCatDensity = 0;
 constexpr int kCatWall = 1;

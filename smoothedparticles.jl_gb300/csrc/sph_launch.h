@@ -39,16 +39,19 @@ size_t scan_tmp_ints(int len);
 // op: SPH_OP_DENSITY / SPH_OP_DENSITY_REF / SPH_OP_FORCE.  reset: start the
 // accumulators at 0 (the folded reset_*! of a step) instead of the stored
 // values; fuse_eos: apply the Tait EOS in the density epilogue.
+// lists_valid: the hit lists of the last density pass belong to the current
+// binning and positions, so the force pass may read them instead of
+// traversing again.
 cudaError_t launch_pair_fp64(const LaunchCtx& c, const State& s, const Geometry& g,
                              const Consts& k, const BinScratch& b, int cap, int op, int self,
-                             int reset, int fuse_eos);
+                             int reset, int fuse_eos, int lists_valid);
 // ---- mixed-precision pair passes (sph_pair32.cu)
 // aux_fresh: the FP32 neighbour copies (vr, rhof) of the fluid particles are
 // current (written by a fused density pass since the last state change);
 // otherwise the wall-pressure and force passes rebuild them first.
 cudaError_t launch_pair_mixed(const LaunchCtx& c, const State& s, const Geometry& g,
                               const Consts& k, const BinScratch& b, int cap, int op, int self,
-                              int reset, int fuse_eos, int aux_fresh);
+                              int reset, int fuse_eos, int aux_fresh, int lists_valid);
 // sum(sys, func, x) at nq device points (x: nq x 3) or, when rid_query is not
 // null, at particles given by reference index.
 cudaError_t launch_sum(const LaunchCtx& c, const State& s, const Geometry& g, const Consts& k,

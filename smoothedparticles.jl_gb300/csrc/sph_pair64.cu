@@ -6,19 +6,11 @@
 // written, in the order the CPU restatement uses, so results are bit-identical
 // to it (IEEE division and square root are correctly rounded on both sides).
 //
-// Pair pass structure (one thread per target particle, targets in cell order,
-// so the lanes of a warp mostly share one cell and walk the same candidates):
-//   scan    : walk the 3^d neighbour cells in key_diff order and each cell's
-//             particles in stored (descending reference index) order.  Each
-//             candidate is classified with FP32 arithmetic on cell-relative
-//             positions; only candidates inside a thin band around the
-//             support radius are re-tested with the reference's FP64
-//             expression.  Hits go to a per-thread queue in shared memory.
-//   process : the queued hits are evaluated in FP64, in queue order, so each
-//             target's sums are formed in exactly the reference's order.
-// The FP64 pipe is the bound of this pass (1/58 of the FP32 rate on GB300),
-// and the split keeps every FP64 instruction on a hit with the warp's lanes
-// busy, instead of one FP64 distance per candidate.
+// Traversal: sph_cellwarp.cuh (cell-aligned warps, shared-memory staged
+// candidates, FP32 classification with an FP64 band test, per-lane hit
+// queues processed in order).  The FP64 pipe is the bound of these passes
+// (1/58 of the FP32 rate on GB300); the queues keep each FP64 instruction on
+// a hit, with the warp's lanes processing their hits together.
 //
 // Why the FP32 classification is exact: positions are stored relative to
 // their cell's origin, |xl| < 1.02 h; the neighbour-cell offset is an integer
@@ -28,6 +20,7 @@
 // than 2^-18 h^2.  The band [h^2 (1 - 2^-14), h^2 (1 + 2^-14)] is 16x wider
 // than that, and outside the band the reference's test sqrt(fl64(s)) > h
 // cannot disagree with the FP32 decision.
+#include "sph_cellwarp.cuh"
 #include "sph_launch.h"
 #include "sphgpu.h"
 
@@ -35,8 +28,6 @@ namespace sphgpu {
 
 namespace {
 
-constexpr int kPairThreads = 128;
-constexpr int kQueue = 32;
 
 template <int DIM>
 __device__ __forceinline__ double dist2_64(const State& s, const double* xp, int q, double* d) {
@@ -52,39 +43,140 @@ __device__ __forceinline__ double dist2_64(const State& s, const double* xp, int
   return ss;
 }
 
-__device__ __forceinline__ void warp_add(unsigned long long* dst, int v) {
-  const int sum = __reduce_add_sync(0xffffffffu, v);
-  if ((threadIdx.x & 31) == 0 && sum) atomicAdd(dst, (unsigned long long)sum);
-}
+// The operator bodies on a hit, in FP64 (list entry = q | neighbour cell << 27;
+// the force looks up whether q is a wall).
+template <int DIM, int OP>
+struct Proc64 {
+  const State& s;
+  const Consts& k;
+  double xp[3];
+  double vp[3];
+  double rhop, prp;
+  double acc, ax, ay, az, sx, sy, sz, wp, wg, ws;
+  int c0, c1, c2;
 
-// Pair and per-category hit counters (c0: the operator's main hits; for the
-// force c0 = fluid neighbours, c1 = wall neighbours, c2 = viscosity active).
-template <int OP>
-__device__ __forceinline__ void count_hits(const BinScratch& b, int pairs, int c0, int c1, int c2) {
-  warp_add(b.d_pairs, pairs);
-  if (OP == SPH_OP_FORCE) {
-    warp_add(b.d_cat + kCatForceFluid, c0);
-    warp_add(b.d_cat + kCatForceWall, c1);
-    warp_add(b.d_cat + kCatForceAV, c2);
-  } else if (OP == SPH_OP_WALL_PRESSURE) {
-    warp_add(b.d_cat + kCatWall, c0);
-  } else {
-    warp_add(b.d_cat + kCatDensity, c0);
+  __device__ Proc64(const State& s_, const Consts& k_) : s(s_), k(k_) {
+    acc = ax = ay = az = sx = sy = sz = wp = wg = ws = 0.0;
+    rhop = prp = 0.0;
+    vp[0] = vp[1] = vp[2] = 0.0;
+    c0 = c1 = c2 = 0;
   }
-}
+
+  __device__ __forceinline__ int entry(int q, int c, int tq) const {
+    if (OP == SPH_OP_WALL_PRESSURE && tq != kFluid) return kCwSkip;
+    return q | (c << kCwCellBits);
+  }
+
+  __device__ __forceinline__ void process(const int* list, int stride, int cnt) {
+    for (int t = 0; t < cnt; ++t) {
+      const int q = __ldg(&list[(size_t)t * stride]) & kCwIndexMask;
+      double d[3];
+      const double ss = dist2_64<DIM>(s, xp, q, d);
+      const double r = sqrt(ss);
+      const bool fluid = OP != SPH_OP_FORCE || __ldg(&s.type[q]) == kFluid;
+      if (fluid) ++c0; else ++c1;
+      if (OP == SPH_OP_DENSITY || OP == SPH_OP_DENSITY_REF) {
+        acc = acc + k.mass * ker_w(k, r);
+      } else if (OP == SPH_OP_WALL_PRESSURE) {
+        // Adami, Hu & Adams (2012) wall pressure, g . (x_w - x_f)
+        const double w = ker_w(k, r);
+        double gd = k.g[0] * d[0] + k.g[1] * d[1];
+        if (DIM == 3) gd = gd + k.g[2] * d[2];
+        wp = wp + __ldg(&s.P[q]) * w;
+        wg = wg + (__ldg(&s.rho[q]) * gd) * w;
+        ws = ws + w;
+      } else if (fluid) {
+        // pressure (collapse_symplectic.jl:114-118) + Monaghan viscosity + XSPH
+        const double ker = k.mass * ker_rdw(k, r);
+        double vq[3];
+        vq[0] = __ldg(&s.v[0][q]);
+        vq[1] = __ldg(&s.v[1][q]);
+        vq[2] = DIM == 3 ? __ldg(&s.v[2][q]) : 0.0;
+        const double dv0 = vp[0] - vq[0];
+        const double dv1 = vp[1] - vq[1];
+        double vdx = dv0 * d[0] + dv1 * d[1];
+        if (DIM == 3) {
+          const double dv2 = vp[2] - vq[2];
+          vdx = vdx + dv2 * d[2];
+        }
+        const double rhoq = __ldg(&s.rho[q]);
+        const double inv_rb = 2.0 / (rhop + rhoq);
+        double pi = 0.0;
+        if (vdx < 0.0) {
+          const double mu = (k.h_smooth * vdx) / (ss + k.eta2);
+          pi = (-k.alpha_c0 * mu) * inv_rb;
+          ++c2;
+        }
+        const double cf = -ker * ((prp + __ldg(&s.Pr[q])) + pi);
+        ax = ax + cf * d[0];
+        ay = ay + cf * d[1];
+        if (DIM == 3) az = az + cf * d[2];
+        const double wx = (k.mass * ker_w(k, r)) * inv_rb;
+        sx = sx + wx * (vq[0] - vp[0]);
+        sy = sy + wx * (vq[1] - vp[1]);
+        if (DIM == 3) sz = sz + wx * (vq[2] - vp[2]);
+      } else {
+        // wall neighbour: pressure term with the wall pressure
+        const double ker = k.mass * ker_rdw(k, r);
+        const double cf = -ker * (prp + __ldg(&s.Pr[q]));
+        ax = ax + cf * d[0];
+        ay = ay + cf * d[1];
+        if (DIM == 3) az = az + cf * d[2];
+      }
+    }
+  }
+};
 
 template <int DIM, int OP>
-__global__ void __launch_bounds__(kPairThreads) pair64_kernel(State s, Geometry g, Consts k,
-                                                              BinScratch b, int self, int reset,
-                                                              int fuse_eos) {
-  __shared__ int queue[kQueue][kPairThreads];
-  const int tid = threadIdx.x;
-  const int n = *b.d_n;
-  const int i = blockIdx.x * kPairThreads + tid;
+__global__ void __launch_bounds__(kCwThreads) pair64_kernel(State s, Geometry g, Consts k,
+                                                            BinScratch b, int self, int reset,
+                                                            int fuse_eos, int list_mode) {
+  __shared__ CwShared shared[kCwWarps];
+  const int lane = threadIdx.x & 31;
+  const int w = threadIdx.x >> 5;
+  const int item = blockIdx.x * kCwWarps + w;
+  int first = 0, count = 0;
+  if (!cw_item(b, g, item, first, count)) return;  // warp-uniform
+  const int i = first + lane;
+  const bool valid = lane < count;
+  const int ti = valid ? s.type[i] : -1;
   // the wall pressure acts on wall targets, every other operator on fluid ones
   const int want = OP == SPH_OP_WALL_PRESSURE ? kWall : kFluid;
-  int pairs = 0, c0 = 0, c1 = 0, c2 = 0;
-  if (i < n && s.type[i] != want) {
+  CwTarget t;
+  t.active = valid && ti == want;
+  t.i = i;
+  t.key = s.cell[first];
+  decode_key(g, t.key, t.cx, t.cy, t.cz);
+  t.pi4 = valid ? s.pl[i] : make_float4(0.f, 0.f, 0.f, 0.f);
+  t.xp[0] = valid ? s.x[0][i] : 0.0;
+  t.xp[1] = valid ? s.x[1][i] : 0.0;
+  t.xp[2] = (DIM == 3 && valid) ? s.x[2][i] : 0.0;
+  Proc64<DIM, OP> p(s, k);
+  p.xp[0] = t.xp[0];
+  p.xp[1] = t.xp[1];
+  p.xp[2] = t.xp[2];
+  if (t.active) {
+    // accumulators start at the stored value (apply! accumulates) or at 0
+    if (OP == SPH_OP_DENSITY) {
+      if (!reset) p.acc = s.rho[i];
+    } else if (OP == SPH_OP_DENSITY_REF) {
+      if (!reset) p.acc = s.rho_ref[i];
+    } else if (OP == SPH_OP_FORCE) {
+      if (!reset) {
+        p.ax = s.a[0][i]; p.ay = s.a[1][i];
+        p.sx = s.xs[0][i]; p.sy = s.xs[1][i];
+        if (DIM == 3) { p.az = s.a[2][i]; p.sz = s.xs[2][i]; }
+      }
+#pragma unroll
+      for (int d = 0; d < DIM; ++d) p.vp[d] = s.v[d][i];
+      p.rhop = s.rho[i];
+      p.prp = s.Pr[i];
+    }
+  }
+  int pairs = 0;
+  cw_pass<DIM, OP>(s, g, k, b, shared[w], lane, item, t, p, pairs, list_mode);
+
+  if (valid && !t.active) {
     // a folded reset_*! still zeroes the targets the operator skips
     if (reset) {
       if (OP == SPH_OP_DENSITY) {
@@ -96,138 +188,10 @@ __global__ void __launch_bounds__(kPairThreads) pair64_kernel(State s, Geometry 
         for (int d = 0; d < DIM; ++d) { s.a[d][i] = 0.0; s.xs[d][i] = 0.0; }
       }
     }
-  } else if (i < n) {
-    const int key = s.cell[i];
-    int cx, cy, cz;
-    decode_key(g, key, cx, cy, cz);
-    const float4 pi4 = s.pl[i];
-    double xp[3];
-    xp[0] = s.x[0][i];
-    xp[1] = s.x[1][i];
-    xp[2] = DIM == 3 ? s.x[2][i] : 0.0;
-    // accumulators start at the stored value (apply! accumulates) or at 0
-    double acc = 0.0;
-    double ax = 0.0, ay = 0.0, az = 0.0, sx = 0.0, sy = 0.0, sz = 0.0;
-    double wp = 0.0, wg = 0.0, ws = 0.0;
-    double vp[3] = {0.0, 0.0, 0.0};
-    double rhop = 0.0, prp = 0.0;
-    if (OP == SPH_OP_DENSITY) {
-      if (!reset) acc = s.rho[i];
-    } else if (OP == SPH_OP_DENSITY_REF) {
-      if (!reset) acc = s.rho_ref[i];
-    } else if (OP == SPH_OP_FORCE) {
-      if (!reset) {
-        ax = s.a[0][i]; ay = s.a[1][i];
-        sx = s.xs[0][i]; sy = s.xs[1][i];
-        if (DIM == 3) { az = s.a[2][i]; sz = s.xs[2][i]; }
-      }
-#pragma unroll
-      for (int d = 0; d < DIM; ++d) vp[d] = s.v[d][i];
-      rhop = s.rho[i];
-      prp = s.Pr[i];
-    }
-
-    int c = 0, j = 0, jend = 0;
-    float ox = 0.f, oy = 0.f, oz = 0.f;
-    bool more = true;
-    while (more) {
-      // ---- scan: fill this thread's queue
-      int cnt = 0;
-      while (cnt < kQueue) {
-        if (j >= jend) {
-          if (c >= g.n_diff) { more = false; break; }
-          const int nk = key + g.key_diff[c];
-          ++c;
-          if (nk < 1 || nk > g.key_max) continue;  // core.jl:98
-          j = __ldg(&b.cell_start[nk]);
-          jend = __ldg(&b.cell_start[nk + 1]);
-          int qx, qy, qz;
-          decode_key(g, nk, qx, qy, qz);
-          ox = (float)(qx - cx) * k.hf;
-          oy = (float)(qy - cy) * k.hf;
-          oz = (float)(qz - cz) * k.hf;
-          continue;
-        }
-        const int q = j++;
-        const float4 pq = __ldg(&s.pl[q]);
-        const float dx = (pi4.x - pq.x) - ox;
-        const float dy = (pi4.y - pq.y) - oy;
-        float ss = dx * dx + dy * dy;
-        if (DIM == 3) {
-          const float dz = (pi4.z - pq.z) - oz;
-          ss = ss + dz * dz;
-        }
-        if (ss > k.s_hi || q == i) continue;
-        if (!(ss < k.s_lo) && !within_rn<DIM>(s, k, xp, q)) continue;
-        ++pairs;
-        const int tq = __float_as_int(pq.w);
-        if (OP == SPH_OP_WALL_PRESSURE) {
-          if (tq == kFluid) queue[cnt++][tid] = q;
-        } else if (OP == SPH_OP_FORCE) {
-          queue[cnt++][tid] = tq == kFluid ? q : -q - 1;
-        } else {
-          queue[cnt++][tid] = q;
-        }
-      }
-      // ---- process: FP64, in queue (= reference) order
-      for (int t = 0; t < cnt; ++t) {
-        const int e = queue[t][tid];
-        const int q = e >= 0 ? e : -e - 1;
-        double d[3];
-        const double ss = dist2_64<DIM>(s, xp, q, d);
-        const double r = sqrt(ss);
-        if (e >= 0) ++c0; else ++c1;
-        if (OP == SPH_OP_DENSITY || OP == SPH_OP_DENSITY_REF) {
-          acc = acc + k.mass * ker_w(k, r);
-        } else if (OP == SPH_OP_WALL_PRESSURE) {
-          const double w = ker_w(k, r);
-          double gd = k.g[0] * d[0] + k.g[1] * d[1];
-          if (DIM == 3) gd = gd + k.g[2] * d[2];
-          wp = wp + __ldg(&s.P[q]) * w;
-          wg = wg + (__ldg(&s.rho[q]) * gd) * w;
-          ws = ws + w;
-        } else if (e >= 0) {
-          // pressure (collapse_symplectic.jl:114-118) + Monaghan viscosity + XSPH
-          const double ker = k.mass * ker_rdw(k, r);
-          double vq[3];
-          vq[0] = __ldg(&s.v[0][q]);
-          vq[1] = __ldg(&s.v[1][q]);
-          vq[2] = DIM == 3 ? __ldg(&s.v[2][q]) : 0.0;
-          const double dv0 = vp[0] - vq[0];
-          const double dv1 = vp[1] - vq[1];
-          double vdx = dv0 * d[0] + dv1 * d[1];
-          if (DIM == 3) {
-            const double dv2 = vp[2] - vq[2];
-            vdx = vdx + dv2 * d[2];
-          }
-          const double rhoq = __ldg(&s.rho[q]);
-          const double inv_rb = 2.0 / (rhop + rhoq);
-          double pi = 0.0;
-          if (vdx < 0.0) {
-            const double mu = (k.h_smooth * vdx) / (ss + k.eta2);
-            pi = (-k.alpha_c0 * mu) * inv_rb;
-            ++c2;
-          }
-          const double cf = -ker * ((prp + __ldg(&s.Pr[q])) + pi);
-          ax = ax + cf * d[0];
-          ay = ay + cf * d[1];
-          if (DIM == 3) az = az + cf * d[2];
-          const double wx = (k.mass * ker_w(k, r)) * inv_rb;
-          sx = sx + wx * (vq[0] - vp[0]);
-          sy = sy + wx * (vq[1] - vp[1]);
-          if (DIM == 3) sz = sz + wx * (vq[2] - vp[2]);
-        } else {
-          // wall neighbour: pressure term with the wall pressure
-          const double ker = k.mass * ker_rdw(k, r);
-          const double cf = -ker * (prp + __ldg(&s.Pr[q]));
-          ax = ax + cf * d[0];
-          ay = ay + cf * d[1];
-          if (DIM == 3) az = az + cf * d[2];
-        }
-      }
-    }
-    // ---- epilogue: self term (core.jl:155-157), fused EOS, stores
+  } else if (t.active) {
+    // epilogue: self term (core.jl:155-157), fused EOS, stores
     if (OP == SPH_OP_DENSITY || OP == SPH_OP_DENSITY_REF) {
+      double acc = p.acc;
       if (self) acc = acc + k.mass * ker_w(k, 0.0);
       if (OP == SPH_OP_DENSITY) {
         s.rho[i] = acc;
@@ -244,22 +208,23 @@ __global__ void __launch_bounds__(kPairThreads) pair64_kernel(State s, Geometry 
         s.rho_ref[i] = acc;
       }
     } else if (OP == SPH_OP_WALL_PRESSURE) {
-      const double P = ws > 0.0 ? (wp + wg) / ws : 0.0;
+      const double P = p.ws > 0.0 ? (p.wp + p.wg) / p.ws : 0.0;
       s.P[i] = P;
       s.Pr[i] = P / (k.rho0 * k.rho0);
       s.rho[i] = k.rho0;
     } else {
+      double ax = p.ax, ay = p.ay, az = p.az, sx = p.sx, sy = p.sy, sz = p.sz;
       if (self) {
         const double ker = k.mass * ker_rdw(k, 0.0);
-        const double inv_rb = 2.0 / (rhop + rhop);
-        const double cf = -ker * ((prp + prp) + 0.0);
+        const double inv_rb = 2.0 / (p.rhop + p.rhop);
+        const double cf = -ker * ((p.prp + p.prp) + 0.0);
         const double wx = (k.mass * ker_w(k, 0.0)) * inv_rb;
         ax = ax + cf * 0.0;
         ay = ay + cf * 0.0;
         az = az + cf * 0.0;
-        sx = sx + wx * (vp[0] - vp[0]);
-        sy = sy + wx * (vp[1] - vp[1]);
-        sz = sz + wx * (vp[2] - vp[2]);
+        sx = sx + wx * (p.vp[0] - p.vp[0]);
+        sy = sy + wx * (p.vp[1] - p.vp[1]);
+        sz = sz + wx * (p.vp[2] - p.vp[2]);
       }
       s.a[0][i] = ax;
       s.a[1][i] = ay;
@@ -271,7 +236,7 @@ __global__ void __launch_bounds__(kPairThreads) pair64_kernel(State s, Geometry 
       }
     }
   }
-  count_hits<OP>(b, pairs, c0, c1, c2);
+  cw_count<OP>(b, pairs, p.c0, p.c1, p.c2);
 }
 
 // sum(sys, func, x) (core.jl:240-260) / sum(sys, func, p) (core.jl:271-291):
@@ -379,28 +344,27 @@ __global__ void __launch_bounds__(128) debug_pairs_kernel(State s, Geometry g, C
   }
   if (!pass) counts[rid] = cnt;
 }
-
 template <int DIM>
 cudaError_t launch_pair_dim(const LaunchCtx& c, const State& s, const Geometry& g,
-                            const Consts& k, const BinScratch& b, int cap, int op, int self,
-                            int reset, int fuse_eos) {
-  const int blocks = (cap + kPairThreads - 1) / kPairThreads;
+                            const Consts& k, const BinScratch& b, int, int op, int self,
+                            int reset, int fuse_eos, int list_mode) {
+  const int blocks = (b.max_items + kCwWarps - 1) / kCwWarps;
   const int kid = op == SPH_OP_FORCE           ? SPH_KERNEL_FORCE
                   : op == SPH_OP_WALL_PRESSURE ? SPH_KERNEL_WALL
                                                : SPH_KERNEL_DENSITY;
   mark(c, kid, 0);
   switch (op) {
     case SPH_OP_DENSITY:
-      pair64_kernel<DIM, SPH_OP_DENSITY><<<blocks, kPairThreads, 0, c.stream>>>(s, g, k, b, self, reset, fuse_eos);
+      pair64_kernel<DIM, SPH_OP_DENSITY><<<blocks, kCwThreads, 0, c.stream>>>(s, g, k, b, self, reset, fuse_eos, 1);
       break;
     case SPH_OP_DENSITY_REF:
-      pair64_kernel<DIM, SPH_OP_DENSITY_REF><<<blocks, kPairThreads, 0, c.stream>>>(s, g, k, b, self, reset, 0);
+      pair64_kernel<DIM, SPH_OP_DENSITY_REF><<<blocks, kCwThreads, 0, c.stream>>>(s, g, k, b, self, reset, 0, 1);
       break;
     case SPH_OP_WALL_PRESSURE:
-      pair64_kernel<DIM, SPH_OP_WALL_PRESSURE><<<blocks, kPairThreads, 0, c.stream>>>(s, g, k, b, 0, 0, 0);
+      pair64_kernel<DIM, SPH_OP_WALL_PRESSURE><<<blocks, kCwThreads, 0, c.stream>>>(s, g, k, b, 0, 0, 0, 0);
       break;
     default:
-      pair64_kernel<DIM, SPH_OP_FORCE><<<blocks, kPairThreads, 0, c.stream>>>(s, g, k, b, self, reset, 0);
+      pair64_kernel<DIM, SPH_OP_FORCE><<<blocks, kCwThreads, 0, c.stream>>>(s, g, k, b, self, reset, 0, list_mode);
       break;
   }
   mark(c, kid, 1);
@@ -411,10 +375,11 @@ cudaError_t launch_pair_dim(const LaunchCtx& c, const State& s, const Geometry& 
 
 cudaError_t launch_pair_fp64(const LaunchCtx& c, const State& s, const Geometry& g,
                              const Consts& k, const BinScratch& b, int cap, int op, int self,
-                             int reset, int fuse_eos) {
+                             int reset, int fuse_eos, int lists_valid) {
   if (cap <= 0) return cudaSuccess;
-  return k.dim == 2 ? launch_pair_dim<2>(c, s, g, k, b, cap, op, self, reset, fuse_eos)
-                    : launch_pair_dim<3>(c, s, g, k, b, cap, op, self, reset, fuse_eos);
+  const int lm = lists_valid ? 2 : 0;
+  return k.dim == 2 ? launch_pair_dim<2>(c, s, g, k, b, cap, op, self, reset, fuse_eos, lm)
+                    : launch_pair_dim<3>(c, s, g, k, b, cap, op, self, reset, fuse_eos, lm);
 }
 
 cudaError_t launch_sum(const LaunchCtx& c, const State& s, const Geometry& g, const Consts& k,
