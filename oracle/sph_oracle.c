@@ -322,8 +322,10 @@ static int64_t binary_one(orc_system* s, int op, int64_t p) {
       double d[3];
       const double r = sqrt(dist2(xp, s->x[q], d));
       if (r > H || p == q) continue; /* core.jl:105 */
-      ++pairs;
       const int tq = s->type[q];
+      /* pairs the operator acts on: every neighbour, except that the wall
+       * pressure only sums fluid neighbours */
+      if (op != ORC_OP_WALL_PRESSURE || tq == ORC_FLUID) ++pairs;
       if (op == ORC_OP_DENSITY || op == ORC_OP_DENSITY_REF) {
         acc = acc + m * ker_w(s, r);
       } else if (op == ORC_OP_WALL_PRESSURE) {

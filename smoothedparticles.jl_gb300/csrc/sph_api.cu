@@ -164,8 +164,7 @@ size_t carve(sph_system* s, char* base, size_t C) {
   // (H = 4.8 dr); the capacity leaves room for compression, and an overflow
   // only sends that warp back to a full traversal
   b.hit_cap = D == 3 ? 384 : 160;
-  b.hit_stride = (int)C;
-  b.hits = (int*)take(4 * C * (size_t)b.hit_cap);
+  b.hits = (int*)take(4 * (size_t)b.hit_cap * C);
   b.hit_count = (int*)take(4 * C);
   s->staging = take(72 * C + 64);
   return off;
@@ -349,6 +348,11 @@ int sph_create(const sph_params* p, int device, sph_system** out) {
   k.hf = (float)H;
   k.s_lo = (float)(h2 * (1.0 - band));
   k.s_hi = (float)(h2 * (1.0 + band));
+  // largest double whose correctly rounded square root is <= H
+  double smax = h2;
+  while (std::sqrt(smax) > H) smax = std::nextafter(smax, 0.0);
+  while (std::sqrt(std::nextafter(smax, HUGE_VAL)) <= H) smax = std::nextafter(smax, HUGE_VAL);
+  k.s_max = smax;
   k.inv_hf = (float)k.inv_h;
   k.cwf = (float)k.cw;
   k.crf = (float)k.cr;
@@ -366,7 +370,7 @@ int sph_create(const sph_params* p, int device, sph_system** out) {
   }
   const size_t nb = (size_t)s->geo.key_max + 3;
   const size_t scan_ints = scan_tmp_ints((int)nb) + 64;
-  size_t bytes = align_up(4 * nb) * 3 + align_up(4 * scan_ints) + 2048;
+  size_t bytes = align_up(4 * nb) * 4 + align_up(4 * scan_ints) + 2048;
   void* cells = nullptr;
   if (cudaMalloc(&cells, bytes) != cudaSuccess) {
     cudaGetLastError();
@@ -381,6 +385,8 @@ int sph_create(const sph_params* p, int device, sph_system** out) {
   s->b.cell_start = (int*)c;
   c += align_up(4 * nb);
   s->b.item_off = (int*)c;
+  c += align_up(4 * nb);
+  s->b.cell_fluid = (int*)c;
   c += align_up(4 * nb);
   s->b.scan_tmp = (int*)c;
   c += align_up(4 * scan_ints);

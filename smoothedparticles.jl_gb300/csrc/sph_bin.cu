@@ -229,6 +229,10 @@ __global__ void __launch_bounds__(kThreads) bin_gather_kernel(State cur, State a
   alt.cell[dst] = key;
   alt.pl[dst] = make_float4(xl[0], xl[1], xl[2], __int_as_float(t));
   b.inv_rid[rid] = dst;
+  if (t == kFluid) {  // fluid per cell, one atomic per cell and warp
+    const unsigned peers = __match_any_sync(__activemask(), key);
+    if ((int)(threadIdx.x & 31) == __ffs(peers) - 1) atomicAdd(&b.cell_fluid[key], __popc(peers));
+  }
   if (gather_all) {
     alt.rho[dst] = cur.rho[src];
     alt.P[dst] = cur.P[src];
@@ -332,6 +336,8 @@ cudaError_t launch_binning(const LaunchCtx& c, const State& cur, const State& al
   cudaError_t e = cudaMemsetAsync(b.counts, 0, sizeof(int) * (size_t)nbuckets, c.stream);
   if (e != cudaSuccess) return e;
   e = cudaMemsetAsync(b.d_nrem, 0, sizeof(int), c.stream);
+  if (e != cudaSuccess) return e;
+  e = cudaMemsetAsync(b.cell_fluid, 0, sizeof(int) * (size_t)nbuckets, c.stream);
   if (e != cudaSuccess) return e;
   mark(c, SPH_KERNEL_BIN_KEYS, 0);
   if (k.dim == 2)

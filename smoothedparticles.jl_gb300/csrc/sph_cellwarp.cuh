@@ -12,15 +12,13 @@
 // A candidate is classified in FP32; only candidates within a thin band around
 // the support radius take the reference's FP64 test (proof in sph_pair64.cu).
 //
-// Hits are appended, in traversal order, to the target's column of the hit
-// list in global memory (entry t of target i at hits[t * stride + i]; the
-// warp's 32 consecutive targets make each append one coalesced 128-byte
-// row).  After the traversal every lane processes its own list in order, so
-// each target's sums are formed in exactly the reference's order, and the
-// lanes' lists have nearly equal lengths (the FP64 work runs with full
-// warps).  The force pass of the same binning reads the lists back instead of
-// traversing again.  A list that would exceed hit_cap is processed early and
-// its item is marked partial (the force pass then traverses that item).
+// Hits are appended, in traversal order, to the target's list in global
+// memory (see cw_list).  After the traversal every lane processes its own
+// list in order, so each target's sums are formed in exactly the reference's
+// order, and the lanes' lists have nearly equal lengths (the FP64 work runs
+// with full warps).  The force pass of the same binning reads the lists back
+// instead of traversing again.  A list that would exceed hit_cap is processed
+// early and its item is marked partial (the force pass then traverses it).
 #pragma once
 
 #include "sph_common.cuh"
@@ -34,9 +32,13 @@ constexpr int kCwCellBits = 27;             // entry = index | neighbour cell <<
 constexpr int kCwIndexMask = (1 << kCwCellBits) - 1;
 constexpr int kCwSkip = -1;
 
+constexpr int kCwBand = 16;  // band candidates a lane may defer
+
 struct CwShared {
-  float4 buf[32];      // staged candidates of the current neighbour cell
-  float4 offs[27];     // offset of each neighbour cell from the target cell
+  float4 buf[32];             // staged candidates of the current neighbour cell
+  float4 offs[27];            // offset of each neighbour cell from the target cell
+  int ring[8][32];            // the last < 8 list entries of each lane, column = lane
+  short band[kCwBand][32];    // list positions of a lane's unresolved band candidates
 };
 
 struct CwTarget {
@@ -66,63 +68,144 @@ __device__ __forceinline__ void cw_offsets(const Geometry& g, const Consts& k, C
   __syncwarp();
 }
 
+// Target i's list is the contiguous segment hits[i * hit_cap ...].  Appends go
+// through an 8-entry ring per lane in shared memory and reach global memory
+// as whole 32-byte sectors (no partially written sectors for the L2 to fill
+// from DRAM); the process phase reads each list sequentially.
+__device__ __forceinline__ int* cw_list(const BinScratch& b, int i) {
+  return b.hits + (size_t)i * b.hit_cap;
+}
+constexpr int kCwRow = 1;  // elements between consecutive entries of one list
+
+__device__ __forceinline__ void cw_flush8(const CwShared& sh, int lane, int* dst) {
+  const int4 a = make_int4(sh.ring[0][lane], sh.ring[1][lane], sh.ring[2][lane], sh.ring[3][lane]);
+  const int4 c = make_int4(sh.ring[4][lane], sh.ring[5][lane], sh.ring[6][lane], sh.ring[7][lane]);
+  reinterpret_cast<int4*>(dst)[0] = a;
+  reinterpret_cast<int4*>(dst)[1] = c;
+}
+
+// writes the ring's pending entries [cnt & ~7, cnt) to the list
+__device__ __forceinline__ void cw_flush_tail(const CwShared& sh, int lane, int* list, int cnt) {
+  for (int r = cnt & ~7; r < cnt; ++r) list[r] = sh.ring[r & 7][lane];
+}
+
+// The reference's FP64 distance test for a candidate in the FP32 band; kept
+// out of line so the compiler cannot evaluate it speculatively for every
+// candidate.
+template <int DIM>
+__device__ __noinline__ bool cw_band_test(const State& s, const Consts& k, const double* xp, int q) {
+  return within_rn<DIM>(s, k, xp, q);
+}
+
+// Band candidates are appended to the list provisionally and tested here, all
+// lanes together: on the lattices of the benchmarks many candidates lie
+// exactly at r = h (i^2 + j^2 + k^2 = 16 in 3D), and testing each where it is
+// found would run the FP64 test one lane at a time.  A rejected candidate's
+// entry becomes kCwSkip.
+template <int DIM>
+__device__ __forceinline__ void cw_resolve(const State& s, const Consts& k, CwShared& sh, int lane,
+                                           const CwTarget& t, int* list, int cnt, int& nb) {
+  const int kmax = __reduce_max_sync(0xffffffffu, nb);
+  for (int kk = 0; kk < kmax; ++kk) {
+    if (kk < nb) {
+      const int p = sh.band[kk][lane];
+      const bool in_ring = p >= (cnt & ~7);
+      const int e = in_ring ? sh.ring[p & 7][lane] : list[p];
+      if (!within_rn<DIM>(s, k, t.xp, e & kCwIndexMask)) {
+        if (in_ring) sh.ring[p & 7][lane] = kCwSkip;
+        else list[p] = kCwSkip;
+      }
+    }
+  }
+  nb = 0;
+}
+
 // P::entry(q, c, type of q) -> the list entry of a hit on q found in
-// neighbour cell c, or kCwSkip when the operator ignores it;
+// neighbour cell c, or kCwSkip when the operator ignores it (a skipped hit
+// is not an interaction of the operator);
 // P::process(list, stride, cnt) consumes cnt entries list[0], list[stride], ...
-// Returns the number of entries left in the list; sets `partial` when the
-// list was processed early.
-template <int DIM, class P>
+// skipping kCwSkip entries.  Returns the number of entries left in the list;
+// sets `partial` when the list was processed early.  FLUID_CELLS_ONLY: skip
+// neighbour cells without fluid (for operators that ignore wall neighbours).
+template <int DIM, bool FLUID_CELLS_ONLY, class P>
 __device__ __forceinline__ int cw_traverse(const State& s, const Geometry& g, const Consts& k,
                                            const BinScratch& b, CwShared& sh, int lane,
-                                           const CwTarget& t, P& proc, int& pairs,
-                                           bool& partial) {
-  int* const list = b.hits + t.i;  // dereferenced only by active lanes
-  const int stride = b.hit_stride;
+                                           const CwTarget& t, P& proc, bool& partial) {
+  int* const list = cw_list(b, t.i);  // dereferenced only by active lanes
   const int cap = b.hit_cap;
   int cnt = 0;
+  int nb = 0;  // deferred band candidates of this lane
   cw_offsets(g, k, sh, lane, t);
   for (int c = 0; c < g.n_diff; ++c) {
     const int nk = t.key + g.key_diff[c];
     if (nk < 1 || nk > g.key_max) continue;  // core.jl:98
+    if (FLUID_CELLS_ONLY && __ldg(&b.cell_fluid[nk]) == 0) continue;
     const int st = __ldg(&b.cell_start[nk]);
     const int en = __ldg(&b.cell_start[nk + 1]);
     if (st == en) continue;
     const float4 off = sh.offs[c];
     for (int base = st; base < en; base += 32) {
       const int m = min(32, en - base);
+      // a chunk adds at most m entries per lane: make room first
+      if (__any_sync(0xffffffffu, cnt > cap - m)) {
+        cw_resolve<DIM>(s, k, sh, lane, t, list, cnt, nb);
+        if (t.active) cw_flush_tail(sh, lane, list, cnt);
+        proc.process(list, kCwRow, cnt);
+        cnt = 0;
+        partial = true;
+      }
       __syncwarp();
       if (lane < m) sh.buf[lane] = __ldg(&s.pl[base + lane]);
       __syncwarp();
-      for (int u = 0; u < m; ++u) {
-        const float4 pq = sh.buf[u];
-        if (t.active) {
-          const int q = base + u;
-          const float dx = (t.pi4.x - pq.x) - off.x;
-          const float dy = (t.pi4.y - pq.y) - off.y;
-          float ss = dx * dx + dy * dy;
-          if (DIM == 3) {
-            const float dz = (t.pi4.z - pq.z) - off.z;
-            ss = ss + dz * dz;
+      if (t.active) {
+        for (int u0 = 0; u0 < m; u0 += 4) {
+          // four candidates' FP32 distances first (independent work), then
+          // their hits in candidate order
+          float ss4[4];
+          int tq4[4];
+#pragma unroll
+          for (int j = 0; j < 4; ++j) {
+            const float4 pq = sh.buf[min(u0 + j, 31)];
+            const float dx = (t.pi4.x - pq.x) - off.x;
+            const float dy = (t.pi4.y - pq.y) - off.y;
+            float ss = dx * dx + dy * dy;
+            if (DIM == 3) {
+              const float dz = (t.pi4.z - pq.z) - off.z;
+              ss = ss + dz * dz;
+            }
+            ss4[j] = ss;
+            tq4[j] = __float_as_int(pq.w);
           }
-          if (!(ss > k.s_hi) && q != t.i && (ss < k.s_lo || within_rn<DIM>(s, k, t.xp, q))) {
-            ++pairs;
-            const int e = proc.entry(q, c, __float_as_int(pq.w));
-            if (e != kCwSkip) {
-              list[(size_t)cnt * stride] = e;
-              ++cnt;
+#pragma unroll
+          for (int j = 0; j < 4; ++j) {
+            const int q = base + u0 + j;
+            if (u0 + j < m && !(ss4[j] > k.s_hi) && q != t.i) {
+              int e = proc.entry(q, c, tq4[j]);
+              if (e != kCwSkip && !(ss4[j] < k.s_lo)) {
+                // in the band: defer the FP64 test, or take it now when this
+                // lane's deferral slots are full
+                if (nb < kCwBand) {
+                  sh.band[nb][lane] = (short)cnt;
+                  ++nb;
+                } else if (!cw_band_test<DIM>(s, k, t.xp, q)) {
+                  e = kCwSkip;
+                }
+              }
+              if (e != kCwSkip) {
+                sh.ring[cnt & 7][lane] = e;
+                ++cnt;
+                if ((cnt & 7) == 0) cw_flush8(sh, lane, list + (cnt - 8));
+              }
             }
           }
-        }
-        if (__any_sync(0xffffffffu, cnt == cap)) {
-          proc.process(list, stride, cnt);
-          cnt = 0;
-          partial = true;
         }
       }
     }
   }
+  cw_resolve<DIM>(s, k, sh, lane, t, list, cnt, nb);
+  if (t.active) cw_flush_tail(sh, lane, list, cnt);
   __syncwarp();
-  proc.process(list, stride, cnt);
+  proc.process(list, kCwRow, cnt);
   return cnt;
 }
 
@@ -144,9 +227,10 @@ __device__ __forceinline__ void cw_warp_add(unsigned long long* dst, int v) {
 
 // Pair and per-category hit counters (c0: the operator's main hits; for the
 // force c0 = fluid neighbours, c1 = wall neighbours, c2 = viscosity active).
+// Pair interactions = every processed entry.
 template <int OP>
-__device__ __forceinline__ void cw_count(const BinScratch& b, int pairs, int c0, int c1, int c2) {
-  cw_warp_add(b.d_pairs, pairs);
+__device__ __forceinline__ void cw_count(const BinScratch& b, int c0, int c1, int c2) {
+  cw_warp_add(b.d_pairs, c0 + c1);
   if (OP == SPH_OP_FORCE) {
     cw_warp_add(b.d_cat + kCatForceFluid, c0);
     cw_warp_add(b.d_cat + kCatForceWall, c1);
@@ -164,19 +248,16 @@ __device__ __forceinline__ void cw_count(const BinScratch& b, int pairs, int c0,
 template <int DIM, int OP, class P>
 __device__ __forceinline__ void cw_pass(const State& s, const Geometry& g, const Consts& k,
                                         const BinScratch& b, CwShared& sh, int lane, int item,
-                                        const CwTarget& t, P& proc, int& pairs, int list_mode) {
+                                        const CwTarget& t, P& proc, int list_mode) {
   if (list_mode == 2 && __ldg(&b.item_partial[item]) == 0) {
     cw_offsets(g, k, sh, lane, t);
-    if (t.active) {
-      const int cnt = __ldg(&b.hit_count[t.i]);
-      pairs += cnt;
-      proc.process(b.hits + t.i, b.hit_stride, cnt);
-    }
+    if (t.active) proc.process(cw_list(b, t.i), kCwRow, __ldg(&b.hit_count[t.i]));
     __syncwarp();
     return;
   }
   bool partial = false;
-  const int left = cw_traverse<DIM>(s, g, k, b, sh, lane, t, proc, pairs, partial);
+  const int left = cw_traverse<DIM, OP == SPH_OP_WALL_PRESSURE>(s, g, k, b, sh, lane, t, proc,
+                                                                partial);
   if (list_mode == 1) {
     if (t.active) b.hit_count[t.i] = left;
     if (lane == 0) b.item_partial[item] = partial ? 1 : 0;

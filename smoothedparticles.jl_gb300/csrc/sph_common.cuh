@@ -66,6 +66,8 @@ struct Consts {
   // FP32 squared distance lies below s_lo is inside the support, above s_hi
   // outside; in between the FP64 test decides.
   float hf, s_lo, s_hi;
+  // the largest double s with sqrt_rn(s) <= h: r > h  <=>  fl64(r^2 sum) > s_max
+  double s_max;
   // FP32 copies for the mixed-precision pair arithmetic
   float inv_hf, cwf, crf, massf, eta2f, alpha_c0f, h_smoothf, rho0f;
   float gf[3];
@@ -98,14 +100,14 @@ struct BinScratch {
   int2* items;      // (first target, count)
   int* item_off;    // key_max + 3: exclusive prefix of items per cell
   int max_items;    // capacity of `items`
-  // hit lists: target i's hits are hits[t * hit_stride + i], t < hit_count[i]
+  // hit lists (layout in sph_cellwarp.cuh: cw_list), t < hit_count[i]
   // (entry = neighbour index | neighbour-cell number << 27), written by the
   // density passes and read back by the force pass of the same binning
   int* hits;
   int* hit_count;
   int* item_partial;  // 1 when an item's list overflowed hit_cap
   int hit_cap;
-  int hit_stride;
+  int* cell_fluid;    // key_max + 3: fluid particles per cell
 };
 
 // Upper bound of the work-list length for n particles (every cell with
@@ -166,7 +168,9 @@ __device__ __forceinline__ long long find_key_point(const Geometry& g, const Con
 // The reference's distance test, r = sqrt((d1*d1 + d2*d2) + d3*d3) and
 // r > h (core.jl:8-10, :105; algebra.jl:49-60), with round-to-nearest
 // intrinsics so that no compiler contraction can change a rounding: the
-// FP64 band test gives the same answer in every translation unit.
+// FP64 band test gives the same answer in every translation unit.  Because
+// the correctly rounded square root is monotone, sqrt_rn(s) > h exactly when
+// s > s_max, so no square root is taken.
 template <int DIM>
 __device__ __forceinline__ bool within_rn(const State& s, const Consts& k, const double* xp, int q) {
   const double d0 = __dsub_rn(xp[0], __ldg(&s.x[0][q]));
@@ -176,7 +180,7 @@ __device__ __forceinline__ bool within_rn(const State& s, const Consts& k, const
     const double d2 = __dsub_rn(xp[2], __ldg(&s.x[2][q]));
     ss = __dadd_rn(ss, __dmul_rn(d2, d2));
   }
-  return !(__dsqrt_rn(ss) > k.h);
+  return !(ss > k.s_max);
 }
 
 __device__ __forceinline__ unsigned lanemask_lt() {

@@ -80,64 +80,83 @@ struct Proc32 {
     }
   }
 
-  // <= 32 hits summed in FP32, folded into the FP64 accumulators
+  // <= 32 hits summed in FP32, folded into the FP64 accumulators; the loads
+  // of four hits are issued before their arithmetic
   __device__ __forceinline__ void process_batch(const int* list, int stride, int cnt) {
     float f0 = 0.f, f1 = 0.f, f2 = 0.f, f3 = 0.f, f4 = 0.f, f5 = 0.f;
-    for (int t = 0; t < cnt; ++t) {
-      const int e = __ldg(&list[(size_t)t * stride]);
-      const int q = e & kCwIndexMask;
-      const float4 off = offs[(unsigned)e >> kCwCellBits];
-      const float4 pq = __ldg(&s.pl[q]);
-      const float hx = (pi4.x - pq.x) - off.x;
-      const float hy = (pi4.y - pq.y) - off.y;
-      const float hz = DIM == 3 ? (pi4.z - pq.z) - off.z : 0.f;
-      float ss = hx * hx + hy * hy;
-      if (DIM == 3) ss = ss + hz * hz;
-      const float r = fsqrt(ss);
-      const float kt = kt32(k, r);
-      const bool fluid = __float_as_int(pq.w) == kFluid;
-      if (OP != SPH_OP_FORCE || fluid) ++c0; else ++c1;
-      if (OP == SPH_OP_DENSITY || OP == SPH_OP_DENSITY_REF) {
-        // the shape t^4 (1 + 4x) only; m * C_w is applied in FP64 per batch
-        const float t2 = kt * kt;
-        f0 += (t2 * t2) * (5.f - 4.f * kt);
-      } else if (OP == SPH_OP_WALL_PRESSURE) {
-        const float w = kw32(k, r, kt);
-        float gd = k.gf[0] * hx + k.gf[1] * hy;
-        if (DIM == 3) gd += k.gf[2] * hz;
-        const float rq = __ldg(&s.rhof[q]);
-        const float Pq = __ldg(&s.vr[q]).w * rq * rq;
-        f0 += Pq * w;
-        f1 += (rq * gd) * w;
-        f2 += w;
-      } else if (fluid) {
-        const float4 vq = __ldg(&s.vr[q]);
-        const float rq = __ldg(&s.rhof[q]);
-        const float ker = k.massf * krdw32(k, kt);
-        const float dvx = vp.x - vq.x, dvy = vp.y - vq.y, dvz = vp.z - vq.z;
-        float vdx = dvx * hx + dvy * hy;
-        if (DIM == 3) vdx += dvz * hz;
-        const float inv_rb = __fdividef(2.f, rhop + rq);
-        float pi = 0.f;
-        if (vdx < 0.f) {
-          const float mu = __fdividef(k.h_smoothf * vdx, ss + k.eta2f);
-          pi = (-k.alpha_c0f * mu) * inv_rb;
-          ++c2;
+    for (int t0 = 0; t0 < cnt; t0 += 4) {
+      int e4[4];
+      float4 p4[4], v4[4];
+      float r4[4];
+#pragma unroll
+      for (int j = 0; j < 4; ++j)
+        e4[j] = t0 + j < cnt ? __ldg(&list[(size_t)(t0 + j) * stride]) : kCwSkip;
+#pragma unroll
+      for (int j = 0; j < 4; ++j) {
+        const int q = e4[j] == kCwSkip ? 0 : e4[j] & kCwIndexMask;
+        p4[j] = __ldg(&s.pl[q]);
+        if (OP == SPH_OP_FORCE || OP == SPH_OP_WALL_PRESSURE) {
+          v4[j] = __ldg(&s.vr[q]);
+          r4[j] = __ldg(&s.rhof[q]);
         }
-        const float cf = -ker * ((vp.w + vq.w) + pi);
-        f0 += cf * hx;
-        f1 += cf * hy;
-        f2 += cf * hz;
-        const float wx = k.massf * kw32(k, r, kt) * inv_rb;
-        f3 -= wx * dvx;
-        f4 -= wx * dvy;
-        f5 -= wx * dvz;
-      } else {
-        const float prq = __ldg(&s.vr[q]).w;
-        const float cf = -(k.massf * krdw32(k, kt)) * (vp.w + prq);
-        f0 += cf * hx;
-        f1 += cf * hy;
-        f2 += cf * hz;
+      }
+#pragma unroll
+      for (int j = 0; j < 4; ++j) {
+        if (t0 + j >= cnt) break;
+        const int e = e4[j];
+        if (e == kCwSkip) continue;  // a band candidate beyond the support
+        const float4 off = offs[(unsigned)e >> kCwCellBits];
+        const float4 pq = p4[j];
+        const float hx = (pi4.x - pq.x) - off.x;
+        const float hy = (pi4.y - pq.y) - off.y;
+        const float hz = DIM == 3 ? (pi4.z - pq.z) - off.z : 0.f;
+        float ss = hx * hx + hy * hy;
+        if (DIM == 3) ss = ss + hz * hz;
+        const float r = fsqrt(ss);
+        const float kt = kt32(k, r);
+        const bool fluid = __float_as_int(pq.w) == kFluid;
+        if (OP != SPH_OP_FORCE || fluid) ++c0; else ++c1;
+        if (OP == SPH_OP_DENSITY || OP == SPH_OP_DENSITY_REF) {
+          // the shape t^4 (1 + 4x) only; m * C_w is applied in FP64 per batch
+          const float t2 = kt * kt;
+          f0 += (t2 * t2) * (5.f - 4.f * kt);
+        } else if (OP == SPH_OP_WALL_PRESSURE) {
+          const float w = kw32(k, r, kt);
+          float gd = k.gf[0] * hx + k.gf[1] * hy;
+          if (DIM == 3) gd += k.gf[2] * hz;
+          const float rq = r4[j];
+          const float Pq = v4[j].w * rq * rq;
+          f0 += Pq * w;
+          f1 += (rq * gd) * w;
+          f2 += w;
+        } else if (fluid) {
+          const float4 vq = v4[j];
+          const float rq = r4[j];
+          const float ker = k.massf * krdw32(k, kt);
+          const float dvx = vp.x - vq.x, dvy = vp.y - vq.y, dvz = vp.z - vq.z;
+          float vdx = dvx * hx + dvy * hy;
+          if (DIM == 3) vdx += dvz * hz;
+          const float inv_rb = __fdividef(2.f, rhop + rq);
+          float pi = 0.f;
+          if (vdx < 0.f) {
+            const float mu = __fdividef(k.h_smoothf * vdx, ss + k.eta2f);
+            pi = (-k.alpha_c0f * mu) * inv_rb;
+            ++c2;
+          }
+          const float cf = -ker * ((vp.w + vq.w) + pi);
+          f0 += cf * hx;
+          f1 += cf * hy;
+          f2 += cf * hz;
+          const float wx = k.massf * kw32(k, r, kt) * inv_rb;
+          f3 -= wx * dvx;
+          f4 -= wx * dvy;
+          f5 -= wx * dvz;
+        } else {
+          const float cf = -(k.massf * krdw32(k, kt)) * (vp.w + v4[j].w);
+          f0 += cf * hx;
+          f1 += cf * hy;
+          f2 += cf * hz;
+        }
       }
     }
     if (OP == SPH_OP_DENSITY || OP == SPH_OP_DENSITY_REF) {
@@ -198,8 +217,7 @@ __global__ void __launch_bounds__(kCwThreads) pair32_kernel(State s, Geometry g,
       p.rhop = s.rhof[i];
     }
   }
-  int pairs = 0;
-  cw_pass<DIM, OP>(s, g, k, b, shared[w], lane, item, t, p, pairs, list_mode);
+  cw_pass<DIM, OP>(s, g, k, b, shared[w], lane, item, t, p, list_mode);
 
   if (valid && !t.active) {
     if (reset) {
@@ -256,7 +274,7 @@ __global__ void __launch_bounds__(kCwThreads) pair32_kernel(State s, Geometry g,
       }
     }
   }
-  cw_count<OP>(b, pairs, p.c0, p.c1, p.c2);
+  cw_count<OP>(b, p.c0, p.c1, p.c2);
 }
 
 template <int DIM>

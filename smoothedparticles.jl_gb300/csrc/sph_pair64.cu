@@ -69,7 +69,9 @@ struct Proc64 {
 
   __device__ __forceinline__ void process(const int* list, int stride, int cnt) {
     for (int t = 0; t < cnt; ++t) {
-      const int q = __ldg(&list[(size_t)t * stride]) & kCwIndexMask;
+      const int e = __ldg(&list[(size_t)t * stride]);
+      if (e == kCwSkip) continue;  // a band candidate beyond the support
+      const int q = e & kCwIndexMask;
       double d[3];
       const double ss = dist2_64<DIM>(s, xp, q, d);
       const double r = sqrt(ss);
@@ -173,8 +175,7 @@ __global__ void __launch_bounds__(kCwThreads) pair64_kernel(State s, Geometry g,
       p.prp = s.Pr[i];
     }
   }
-  int pairs = 0;
-  cw_pass<DIM, OP>(s, g, k, b, shared[w], lane, item, t, p, pairs, list_mode);
+  cw_pass<DIM, OP>(s, g, k, b, shared[w], lane, item, t, p, list_mode);
 
   if (valid && !t.active) {
     // a folded reset_*! still zeroes the targets the operator skips
@@ -236,7 +237,7 @@ __global__ void __launch_bounds__(kCwThreads) pair64_kernel(State s, Geometry g,
       }
     }
   }
-  cw_count<OP>(b, pairs, p.c0, p.c1, p.c2);
+  cw_count<OP>(b, p.c0, p.c1, p.c2);
 }
 
 // sum(sys, func, x) (core.jl:240-260) / sum(sys, func, p) (core.jl:271-291):
