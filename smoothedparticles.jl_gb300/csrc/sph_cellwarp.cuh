@@ -143,7 +143,9 @@ __device__ __forceinline__ int cw_traverse(const State& s, const Geometry& g, co
     const int st = __ldg(&b.cell_start[nk]);
     const int en = __ldg(&b.cell_start[nk + 1]);
     if (st == en) continue;
+    // the target's position relative to this neighbour cell's origin
     const float4 off = sh.offs[c];
+    const float ax = t.pi4.x - off.x, ay = t.pi4.y - off.y, az = t.pi4.z - off.z;
     for (int base = st; base < en; base += 32) {
       const int m = min(32, en - base);
       // a chunk adds at most m entries per lane: make room first
@@ -166,11 +168,11 @@ __device__ __forceinline__ int cw_traverse(const State& s, const Geometry& g, co
 #pragma unroll
           for (int j = 0; j < 4; ++j) {
             const float4 pq = sh.buf[min(u0 + j, 31)];
-            const float dx = (t.pi4.x - pq.x) - off.x;
-            const float dy = (t.pi4.y - pq.y) - off.y;
+            const float dx = ax - pq.x;
+            const float dy = ay - pq.y;
             float ss = dx * dx + dy * dy;
             if (DIM == 3) {
-              const float dz = (t.pi4.z - pq.z) - off.z;
+              const float dz = az - pq.z;
               ss = ss + dz * dz;
             }
             ss4[j] = ss;

@@ -14,8 +14,9 @@
 //
 // Why the FP32 classification is exact: positions are stored relative to
 // their cell's origin, |xl| < 1.02 h; the neighbour-cell offset is an integer
-// multiple of fl32(h).  Each component of the FP32 separation then differs
-// from the true separation by at most 8 * 2^-24 h, so the FP32 squared
+// multiple of fl32(h).  The separation is formed as (xl_p - offset) - xl_q,
+// three roundings of magnitudes below 2.1 h, so each component differs from
+// the true separation by at most 8 * 2^-24 h, and the FP32 squared
 // distance of any candidate within 1.1 h differs from the true one by less
 // than 2^-18 h^2.  The band [h^2 (1 - 2^-14), h^2 (1 + 2^-14)] is 16x wider
 // than that, and outside the band the reference's test sqrt(fl64(s)) > h
@@ -113,10 +114,12 @@ struct Proc64 {
         ax = ax + cf * d[0];
         ay = ay + cf * d[1];
         if (DIM == 3) az = az + cf * d[2];
+        // XSPH: wx (v_q - v_p); v_q - v_p = -(v_p - v_q) exactly in IEEE
+        // arithmetic, so subtracting wx dv rounds identically
         const double wx = (k.mass * ker_w(k, r)) * inv_rb;
-        sx = sx + wx * (vq[0] - vp[0]);
-        sy = sy + wx * (vq[1] - vp[1]);
-        if (DIM == 3) sz = sz + wx * (vq[2] - vp[2]);
+        sx = sx - wx * dv0;
+        sy = sy - wx * dv1;
+        if (DIM == 3) sz = sz - wx * (vp[2] - vq[2]);
       } else {
         // wall neighbour: pressure term with the wall pressure
         const double ker = k.mass * ker_rdw(k, r);
