@@ -201,6 +201,46 @@ int sph_kernel_stats(sph_system* sys, int kernel, double* total_ms, int64_t* lau
 int sph_reset_kernel_stats(sph_system* sys);
 /* Kernels launched by this handle since creation. */
 int sph_launch_count(sph_system* sys, int64_t* launches);
+/* ---- tuning (no reference counterpart): warps per block of the pair passes
+ * (2, 4 or 8, i.e. 64/128/256 threads; default 4).  Results do not depend on
+ * it; the batched ensemble's autotuner picks it per size class. */
+int sph_set_tuning(sph_system* sys, int warps_per_block);
+int sph_get_tuning(const sph_system* sys, int* warps_per_block);
+
+/* ---- device memory accounting for admission by an HBM budget (no
+ * reference counterpart).  sph_memory_estimate: the device bytes a system
+ * with these parameters holds once it stores n particles (cell tables plus the
+ * particle arena; sum() query buffers excluded), computed on the host without
+ * any CUDA call.  sph_memory_usage: the bytes the system holds now.
+ * sph_query: *idle = 1 when all work queued on the system's stream has
+ * finished, 0 otherwise (never waits). */
+int sph_memory_estimate(const sph_params* params, int64_t n, uint64_t* bytes);
+int sph_memory_usage(const sph_system* sys, uint64_t* bytes);
+int sph_query(sph_system* sys, int* idle);
+
+/* ---- batched ensembles (no reference counterpart)
+ *
+ * A batch steps many independent systems (same device) together.  The first
+ * sph_batch_step of two or more steps captures every member's fused step
+ * (the sph_step sequence) into one CUDA graph, two steps per graph, each
+ * member an independent branch; every further pair of steps is one graph
+ * launch, and the branches overlap on the device.  An odd last step runs on
+ * the members' own streams.  Each member's results are bit-identical to
+ * stepping it alone.  The graph is captured again when a member's buffers or
+ * tuning changed; members must outlive the batch and must not be stepped by
+ * other calls while a batch step is in flight. */
+typedef struct sph_batch sph_batch;
+int sph_batch_create(sph_system* const* members, int count, sph_batch** out);
+int sph_batch_destroy(sph_batch* batch);
+const char* sph_batch_last_error(const sph_batch* batch);
+int sph_batch_step(sph_batch* batch, int nsteps);
+int sph_batch_synchronize(sph_batch* batch);
+/* kernels in one captured graph, graph launches so far, kernels executed */
+int sph_batch_stats(sph_batch* batch, int64_t* kernels_per_graph, int64_t* graph_launches,
+                    int64_t* kernels);
+/* the stream the graph is launched on (a cudaStream_t) */
+int sph_batch_stream(sph_batch* batch, void** stream);
+
 /* ---- allocation-free cell-list build (no counterpart in the reference)
  *
  * For callers that must not have the library allocate device memory: a host

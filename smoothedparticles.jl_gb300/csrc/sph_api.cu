@@ -43,6 +43,29 @@ struct sph_system {
   double total_ms[SPH_KERNEL_COUNT] = {};
   long long kernel_launches[SPH_KERNEL_COUNT] = {};
   long long total_launches = 0;
+  // bumped whenever device buffers are reallocated or the launch shape
+  // changes, so a batch knows its captured graph is stale
+  long long generation = 0;
+};
+
+// Many systems stepped together: each member's fused step is captured once
+// into a CUDA graph as an independent branch (two steps per graph, so every
+// member's ping-pong buffers end where they started) and the graph is
+// replayed; the branches overlap on the device.
+struct sph_batch {
+  std::vector<sph_system*> members;
+  std::vector<long long> generations;
+  int device = 0;
+  cudaStream_t origin = nullptr;
+  cudaEvent_t fork = nullptr;
+  cudaEvent_t after = nullptr;
+  std::vector<cudaEvent_t> joins;
+  cudaGraph_t graph = nullptr;
+  cudaGraphExec_t exec = nullptr;
+  long long kernels_per_graph = 0;
+  long long launches = 0;
+  long long graph_launches = 0;
+  std::string err;
 };
 
 namespace {
@@ -189,6 +212,7 @@ int ensure_capacity(sph_system* s, int n) {
   s->arena = p;
   carve(s, (char*)p, C);
   s->cap = (int)C;
+  ++s->generation;
   return SPH_OK;
 }
 
@@ -271,9 +295,9 @@ int sph_abi_version(void) { return SPHGPU_ABI_VERSION; }
 
 const char* sph_last_error(const sph_system* s) { return s ? s->err.c_str() : "null handle"; }
 
-int sph_create(const sph_params* p, int device, sph_system** out) {
-  if (!p || !out) return SPH_ERR_ARG;
-  *out = nullptr;
+// Validates the parameters and fills the host-side geometry and constants
+// (no CUDA call).
+static int setup_host(const sph_params* p, sph_system* s) {
   if (p->dim != 2 && p->dim != 3) return SPH_ERR_ARG;
   if (!(p->h > 0.0)) return SPH_ERR_ARG;  // structs.jl:59
   if (p->precision != SPH_PREC_FP64 && p->precision != SPH_PREC_MIXED) return SPH_ERR_ARG;
@@ -281,15 +305,7 @@ int sph_create(const sph_params* p, int device, sph_system** out) {
   for (int d = 0; d < 3; ++d)
     if (!(p->domain_min[d] <= p->domain_max[d])) return SPH_ERR_ARG;
   if (p->dim == 2 && (p->domain_min[2] > 0.0 || p->domain_max[2] < 0.0)) return SPH_ERR_ARG;
-  int ndev = 0;
-  if (cudaGetDeviceCount(&ndev) != cudaSuccess || device < 0 || device >= ndev) {
-    cudaGetLastError();
-    return SPH_ERR_CUDA;
-  }
-  sph_system* s = new sph_system();
   s->params = *p;
-  s->device = device;
-  DeviceGuard guard(device);
   // structs.jl:64-82
   const double H = p->h;
   long long key_max = 1;
@@ -298,10 +314,8 @@ int sph_create(const sph_params* p, int device, sph_system** out) {
     s->geo.key_lim[d] = (long long)std::floor(p->domain_max[d] / H) - s->geo.key_phase[d] + 1;
     key_max *= s->geo.key_lim[d];
   }
-  if (key_max <= 0 || key_max > 0x7fffffffLL - 8) {
-    delete s;
+  if (key_max <= 0 || key_max > 0x7fffffffLL - 8)
     return SPH_ERR_ARG;  // the cell table must be indexable with int32
-  }
   s->geo.key_max = (int)key_max;
   int nd = 0;
   const long long L0 = s->geo.key_lim[0], L1 = s->geo.key_lim[1];
@@ -317,6 +331,7 @@ int sph_create(const sph_params* p, int device, sph_system** out) {
   // derived constants: same expressions as the CPU restatement
   Consts& k = s->k;
   k.dim = p->dim;
+  k.warps = 4;
   k.h = H;
   k.inv_h = 1.0 / H;
   const double h2 = H * H;
@@ -362,7 +377,34 @@ int sph_create(const sph_params* p, int device, sph_system** out) {
   k.h_smoothf = (float)k.h_smooth;
   k.rho0f = (float)k.rho0;
   for (int d = 0; d < 3; ++d) k.gf[d] = (float)k.g[d];
+  return SPH_OK;
+}
 
+// Bytes of the cell tables (fixed per system) and of the particle arena for
+// capacity C.
+static size_t cells_bytes(const sph_system* s) {
+  const size_t nb = (size_t)s->geo.key_max + 3;
+  const size_t scan_ints = scan_tmp_ints((int)nb) + 64;
+  return align_up(4 * nb) * 4 + align_up(4 * scan_ints) + 2048;
+}
+
+int sph_create(const sph_params* p, int device, sph_system** out) {
+  if (!p || !out) return SPH_ERR_ARG;
+  *out = nullptr;
+  sph_system* s = new sph_system();
+  const int rc = setup_host(p, s);
+  if (rc) {
+    delete s;
+    return rc;
+  }
+  int ndev = 0;
+  if (cudaGetDeviceCount(&ndev) != cudaSuccess || device < 0 || device >= ndev) {
+    cudaGetLastError();
+    delete s;
+    return SPH_ERR_CUDA;
+  }
+  s->device = device;
+  DeviceGuard guard(device);
   if (cudaStreamCreateWithFlags(&s->stream, cudaStreamNonBlocking) != cudaSuccess) {
     cudaGetLastError();
     delete s;
@@ -370,7 +412,7 @@ int sph_create(const sph_params* p, int device, sph_system** out) {
   }
   const size_t nb = (size_t)s->geo.key_max + 3;
   const size_t scan_ints = scan_tmp_ints((int)nb) + 64;
-  size_t bytes = align_up(4 * nb) * 4 + align_up(4 * scan_ints) + 2048;
+  const size_t bytes = cells_bytes(s);
   void* cells = nullptr;
   if (cudaMalloc(&cells, bytes) != cudaSuccess) {
     cudaGetLastError();
@@ -615,19 +657,25 @@ int sph_sum_particle(sph_system* s, int func, int64_t nq, const int64_t* index, 
   return sum_common(s, func, nq, nullptr, index, out);
 }
 
+// one verlet_step!: every launch is asynchronous on the handle's stream (no
+// host synchronisation), so the sequence can be captured into a CUDA graph
+static int step_once(sph_system* s) {
+  int rc = binning(s, 1, kGatherStep);  // kick + drift + create_cell_list!
+  if (rc) return rc;
+  rc = pair_pass(s, SPH_OP_DENSITY, 1, 1, 1);  // reset_rho!, find_rho!(self), EOS
+  if (rc) return rc;
+  rc = pair_pass(s, SPH_OP_WALL_PRESSURE, 0, 0, 0);
+  if (rc) return rc;
+  rc = pair_pass(s, SPH_OP_FORCE, 0, 1, 0);  // reset_a!, internal_force!
+  if (rc) return rc;
+  return unary(s, SPH_OP_KICK);
+}
+
 int sph_step(sph_system* s, int nsteps) {
   if (!s || nsteps < 0) return SPH_ERR_ARG;
   DeviceGuard guard(s->device);
   for (int it = 0; it < nsteps; ++it) {
-    int rc = binning(s, 1, kGatherStep);  // kick + drift + create_cell_list!
-    if (rc) return rc;
-    rc = pair_pass(s, SPH_OP_DENSITY, 1, 1, 1);  // reset_rho!, find_rho!(self), EOS
-    if (rc) return rc;
-    rc = pair_pass(s, SPH_OP_WALL_PRESSURE, 0, 0, 0);
-    if (rc) return rc;
-    rc = pair_pass(s, SPH_OP_FORCE, 0, 1, 0);  // reset_a!, internal_force!
-    if (rc) return rc;
-    rc = unary(s, SPH_OP_KICK);
+    const int rc = step_once(s);
     if (rc) return rc;
   }
   return SPH_OK;
@@ -761,9 +809,235 @@ int sph_reset_kernel_stats(sph_system* s) {
   return SPH_OK;
 }
 
+int sph_set_tuning(sph_system* s, int warps_per_block) {
+  if (!s) return SPH_ERR_ARG;
+  if (warps_per_block != 2 && warps_per_block != 4 && warps_per_block != 8)
+    return fail(s, SPH_ERR_ARG, "warps per block must be 2, 4 or 8 (got %d)", warps_per_block);
+  if (s->k.warps != warps_per_block) ++s->generation;
+  s->k.warps = warps_per_block;
+  return SPH_OK;
+}
+
+int sph_get_tuning(const sph_system* s, int* warps_per_block) {
+  if (!s || !warps_per_block) return SPH_ERR_ARG;
+  *warps_per_block = s->k.warps;
+  return SPH_OK;
+}
+
+int sph_memory_estimate(const sph_params* p, int64_t n, uint64_t* bytes) {
+  if (!p || !bytes || n < 0 || n > 0x7fffffffLL - 64) return SPH_ERR_ARG;
+  sph_system tmp;
+  const int rc = setup_host(p, &tmp);
+  if (rc) return rc;
+  *bytes = (uint64_t)(cells_bytes(&tmp) + carve(&tmp, nullptr, (size_t)(n > 0 ? n : 1)));
+  return SPH_OK;
+}
+
+int sph_memory_usage(const sph_system* s, uint64_t* bytes) {
+  if (!s || !bytes) return SPH_ERR_ARG;
+  sph_system tmp;
+  tmp.params = s->params;
+  tmp.geo = s->geo;
+  size_t b = cells_bytes(s);
+  if (s->arena) b += carve(&tmp, nullptr, (size_t)s->cap);
+  b += s->query_bytes;
+  *bytes = (uint64_t)b;
+  return SPH_OK;
+}
+
+int sph_query(sph_system* s, int* idle) {
+  if (!s || !idle) return SPH_ERR_ARG;
+  DeviceGuard guard(s->device);
+  const cudaError_t e = cudaStreamQuery(s->stream);
+  if (e == cudaSuccess) {
+    *idle = 1;
+    return SPH_OK;
+  }
+  if (e == cudaErrorNotReady) {
+    *idle = 0;
+    return SPH_OK;
+  }
+  cudaGetLastError();
+  return fail(s, SPH_ERR_CUDA, "stream query failed: %s", cudaGetErrorString(e));
+}
+
 int sph_launch_count(sph_system* s, int64_t* launches) {
   if (!s || !launches) return SPH_ERR_ARG;
   *launches = s->total_launches;
+  return SPH_OK;
+}
+
+
+// ---------------------------------------------------------------- batches
+
+static int bfail(sph_batch* b, int code, const char* msg) {
+  if (b) b->err = msg;
+  return code;
+}
+
+static void batch_drop_graph(sph_batch* b) {
+  if (b->exec) cudaGraphExecDestroy(b->exec);
+  if (b->graph) cudaGraphDestroy(b->graph);
+  b->exec = nullptr;
+  b->graph = nullptr;
+}
+
+// Captures two fused steps of every member into one graph.
+static int batch_capture(sph_batch* b) {
+  batch_drop_graph(b);
+  std::vector<long long> before(b->members.size());
+  std::vector<bool> prof(b->members.size());
+  for (size_t j = 0; j < b->members.size(); ++j) {
+    before[j] = b->members[j]->total_launches;
+    prof[j] = b->members[j]->profiling;
+    b->members[j]->profiling = false;  // no event records inside the graph
+  }
+  cudaError_t e = cudaStreamBeginCapture(b->origin, cudaStreamCaptureModeThreadLocal);
+  if (e != cudaSuccess) return bfail(b, SPH_ERR_CUDA, "cudaStreamBeginCapture failed");
+  int rc = SPH_OK;
+  cudaEventRecord(b->fork, b->origin);
+  for (size_t j = 0; j < b->members.size() && !rc; ++j) {
+    sph_system* m = b->members[j];
+    cudaStreamWaitEvent(m->stream, b->fork, 0);
+    rc = step_once(m);
+    if (!rc) rc = step_once(m);
+    cudaEventRecord(b->joins[j], m->stream);
+    cudaStreamWaitEvent(b->origin, b->joins[j], 0);
+  }
+  cudaGraph_t g = nullptr;
+  e = cudaStreamEndCapture(b->origin, &g);
+  long long kernels = 0;
+  for (size_t j = 0; j < b->members.size(); ++j) {
+    kernels += b->members[j]->total_launches - before[j];
+    b->members[j]->total_launches = before[j];  // captured, not yet executed
+    b->members[j]->profiling = prof[j];
+    b->generations[j] = b->members[j]->generation;
+  }
+  if (rc) {
+    if (g) cudaGraphDestroy(g);
+    return bfail(b, rc, "a member's step failed during capture");
+  }
+  if (e != cudaSuccess || !g) return bfail(b, SPH_ERR_CUDA, "cudaStreamEndCapture failed");
+  b->graph = g;
+  if (cudaGraphInstantiate(&b->exec, g, 0) != cudaSuccess) {
+    cudaGetLastError();
+    batch_drop_graph(b);
+    return bfail(b, SPH_ERR_CUDA, "cudaGraphInstantiate failed");
+  }
+  b->kernels_per_graph = kernels;
+  return SPH_OK;
+}
+
+int sph_batch_create(sph_system* const* members, int count, sph_batch** out) {
+  if (!members || !out || count <= 0) return SPH_ERR_ARG;
+  *out = nullptr;
+  for (int j = 0; j < count; ++j) {
+    if (!members[j]) return SPH_ERR_ARG;
+    if (members[j]->device != members[0]->device) return SPH_ERR_ARG;
+    if (members[j]->n_host <= 0 || !members[j]->arena) return SPH_ERR_STATE;
+    for (int i = 0; i < j; ++i)
+      if (members[i] == members[j]) return SPH_ERR_ARG;
+  }
+  sph_batch* b = new sph_batch();
+  b->members.assign(members, members + count);
+  b->generations.assign(count, -1);
+  b->device = members[0]->device;
+  DeviceGuard guard(b->device);
+  bool ok = cudaStreamCreateWithFlags(&b->origin, cudaStreamNonBlocking) == cudaSuccess &&
+            cudaEventCreateWithFlags(&b->fork, cudaEventDisableTiming) == cudaSuccess &&
+            cudaEventCreateWithFlags(&b->after, cudaEventDisableTiming) == cudaSuccess;
+  b->joins.assign(count, nullptr);
+  for (int j = 0; j < count && ok; ++j)
+    ok = cudaEventCreateWithFlags(&b->joins[j], cudaEventDisableTiming) == cudaSuccess;
+  if (!ok) {
+    cudaGetLastError();
+    sph_batch_destroy(b);
+    return SPH_ERR_CUDA;
+  }
+  *out = b;
+  return SPH_OK;
+}
+
+int sph_batch_destroy(sph_batch* b) {
+  if (!b) return SPH_ERR_ARG;
+  DeviceGuard guard(b->device);
+  if (b->origin) cudaStreamSynchronize(b->origin);
+  batch_drop_graph(b);
+  for (auto e : b->joins)
+    if (e) cudaEventDestroy(e);
+  if (b->fork) cudaEventDestroy(b->fork);
+  if (b->after) cudaEventDestroy(b->after);
+  if (b->origin) cudaStreamDestroy(b->origin);
+  delete b;
+  return SPH_OK;
+}
+
+const char* sph_batch_last_error(const sph_batch* b) { return b ? b->err.c_str() : "null handle"; }
+
+int sph_batch_step(sph_batch* b, int nsteps) {
+  if (!b || nsteps < 0) return SPH_ERR_ARG;
+  DeviceGuard guard(b->device);
+  bool stale = !b->exec;
+  for (size_t j = 0; j < b->members.size(); ++j)
+    if (b->generations[j] != b->members[j]->generation) stale = true;
+  if (nsteps >= 2 && stale) {
+    // the members' own streams may still run earlier work: order after it
+    for (auto* m : b->members) {
+      cudaEventRecord(b->after, m->stream);
+      cudaStreamWaitEvent(b->origin, b->after, 0);
+    }
+    const int rc = batch_capture(b);
+    if (rc) return rc;
+  }
+  // the graph's branches start behind whatever each member queued before
+  for (auto* m : b->members) {
+    cudaEventRecord(b->after, m->stream);
+    cudaStreamWaitEvent(b->origin, b->after, 0);
+  }
+  for (int it = 0; it + 1 < nsteps; it += 2) {
+    if (cudaGraphLaunch(b->exec, b->origin) != cudaSuccess) {
+      cudaGetLastError();
+      return bfail(b, SPH_ERR_CUDA, "cudaGraphLaunch failed");
+    }
+    b->launches += b->kernels_per_graph;
+    ++b->graph_launches;
+  }
+  // members continue on their own streams behind the graph
+  cudaEventRecord(b->after, b->origin);
+  for (auto* m : b->members) cudaStreamWaitEvent(m->stream, b->after, 0);
+  if (nsteps & 1) {
+    for (auto* m : b->members) {
+      const long long l0 = m->total_launches;
+      const int rc = step_once(m);
+      if (rc) return bfail(b, rc, "a member's step failed");
+      b->launches += m->total_launches - l0;
+      m->total_launches = l0;
+    }
+  }
+  return SPH_OK;
+}
+
+int sph_batch_synchronize(sph_batch* b) {
+  if (!b) return SPH_ERR_ARG;
+  DeviceGuard guard(b->device);
+  for (auto* m : b->members)
+    if (cudaStreamSynchronize(m->stream) != cudaSuccess) return bfail(b, SPH_ERR_CUDA, "stream failed");
+  if (cudaStreamSynchronize(b->origin) != cudaSuccess) return bfail(b, SPH_ERR_CUDA, "stream failed");
+  return SPH_OK;
+}
+
+int sph_batch_stats(sph_batch* b, int64_t* kernels_per_graph, int64_t* graph_launches,
+                    int64_t* kernels) {
+  if (!b) return SPH_ERR_ARG;
+  if (kernels_per_graph) *kernels_per_graph = b->kernels_per_graph;
+  if (graph_launches) *graph_launches = b->graph_launches;
+  if (kernels) *kernels = b->launches;
+  return SPH_OK;
+}
+
+int sph_batch_stream(sph_batch* b, void** stream) {
+  if (!b || !stream) return SPH_ERR_ARG;
+  *stream = (void*)b->origin;
   return SPH_OK;
 }
 

@@ -26,8 +26,6 @@
 
 namespace sphgpu {
 
-constexpr int kCwWarps = 4;                 // warps per block
-constexpr int kCwThreads = 32 * kCwWarps;
 constexpr int kCwCellBits = 27;             // entry = index | neighbour cell << 27
 constexpr int kCwIndexMask = (1 << kCwCellBits) - 1;
 constexpr int kCwSkip = -1;

@@ -62,6 +62,7 @@ struct Consts {
   double dmin[3], dmax[3];
   int vaxis;
   int dim;
+  int warps;  // warps per block of the pair passes (2, 4 or 8; tunable)
   // FP32 candidate classification (see the pair kernels): a candidate whose
   // FP32 squared distance lies below s_lo is inside the support, above s_hi
   // outside; in between the FP64 test decides.

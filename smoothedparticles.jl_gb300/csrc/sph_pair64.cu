@@ -132,14 +132,14 @@ struct Proc64 {
   }
 };
 
-template <int DIM, int OP>
-__global__ void __launch_bounds__(kCwThreads) pair64_kernel(State s, Geometry g, Consts k,
+template <int DIM, int OP, int WARPS>
+__global__ void __launch_bounds__(32 * WARPS) pair64_kernel(State s, Geometry g, Consts k,
                                                             BinScratch b, int self, int reset,
                                                             int fuse_eos, int list_mode) {
-  __shared__ CwShared shared[kCwWarps];
+  __shared__ CwShared shared[WARPS];
   const int lane = threadIdx.x & 31;
   const int w = threadIdx.x >> 5;
-  const int item = blockIdx.x * kCwWarps + w;
+  const int item = blockIdx.x * WARPS + w;
   int first = 0, count = 0;
   if (!cw_item(b, g, item, first, count)) return;  // warp-uniform
   const int i = first + lane;
@@ -352,23 +352,32 @@ template <int DIM>
 cudaError_t launch_pair_dim(const LaunchCtx& c, const State& s, const Geometry& g,
                             const Consts& k, const BinScratch& b, int, int op, int self,
                             int reset, int fuse_eos, int list_mode) {
-  const int blocks = (b.max_items + kCwWarps - 1) / kCwWarps;
+  const int W = k.warps;
+  const int blocks = (b.max_items + W - 1) / W;
   const int kid = op == SPH_OP_FORCE           ? SPH_KERNEL_FORCE
                   : op == SPH_OP_WALL_PRESSURE ? SPH_KERNEL_WALL
                                                : SPH_KERNEL_DENSITY;
   mark(c, kid, 0);
   switch (op) {
     case SPH_OP_DENSITY:
-      pair64_kernel<DIM, SPH_OP_DENSITY><<<blocks, kCwThreads, 0, c.stream>>>(s, g, k, b, self, reset, fuse_eos, 1);
+      if (W == 2) pair64_kernel<DIM, SPH_OP_DENSITY, 2><<<blocks, 64, 0, c.stream>>>(s, g, k, b, self, reset, fuse_eos, 1);
+      else if (W == 8) pair64_kernel<DIM, SPH_OP_DENSITY, 8><<<blocks, 256, 0, c.stream>>>(s, g, k, b, self, reset, fuse_eos, 1);
+      else pair64_kernel<DIM, SPH_OP_DENSITY, 4><<<blocks, 128, 0, c.stream>>>(s, g, k, b, self, reset, fuse_eos, 1);
       break;
     case SPH_OP_DENSITY_REF:
-      pair64_kernel<DIM, SPH_OP_DENSITY_REF><<<blocks, kCwThreads, 0, c.stream>>>(s, g, k, b, self, reset, 0, 1);
+      if (W == 2) pair64_kernel<DIM, SPH_OP_DENSITY_REF, 2><<<blocks, 64, 0, c.stream>>>(s, g, k, b, self, reset, 0, 1);
+      else if (W == 8) pair64_kernel<DIM, SPH_OP_DENSITY_REF, 8><<<blocks, 256, 0, c.stream>>>(s, g, k, b, self, reset, 0, 1);
+      else pair64_kernel<DIM, SPH_OP_DENSITY_REF, 4><<<blocks, 128, 0, c.stream>>>(s, g, k, b, self, reset, 0, 1);
       break;
     case SPH_OP_WALL_PRESSURE:
-      pair64_kernel<DIM, SPH_OP_WALL_PRESSURE><<<blocks, kCwThreads, 0, c.stream>>>(s, g, k, b, 0, 0, 0, 0);
+      if (W == 2) pair64_kernel<DIM, SPH_OP_WALL_PRESSURE, 2><<<blocks, 64, 0, c.stream>>>(s, g, k, b, 0, 0, 0, 0);
+      else if (W == 8) pair64_kernel<DIM, SPH_OP_WALL_PRESSURE, 8><<<blocks, 256, 0, c.stream>>>(s, g, k, b, 0, 0, 0, 0);
+      else pair64_kernel<DIM, SPH_OP_WALL_PRESSURE, 4><<<blocks, 128, 0, c.stream>>>(s, g, k, b, 0, 0, 0, 0);
       break;
     default:
-      pair64_kernel<DIM, SPH_OP_FORCE><<<blocks, kCwThreads, 0, c.stream>>>(s, g, k, b, self, reset, 0, list_mode);
+      if (W == 2) pair64_kernel<DIM, SPH_OP_FORCE, 2><<<blocks, 64, 0, c.stream>>>(s, g, k, b, self, reset, 0, list_mode);
+      else if (W == 8) pair64_kernel<DIM, SPH_OP_FORCE, 8><<<blocks, 256, 0, c.stream>>>(s, g, k, b, self, reset, 0, list_mode);
+      else pair64_kernel<DIM, SPH_OP_FORCE, 4><<<blocks, 128, 0, c.stream>>>(s, g, k, b, self, reset, 0, list_mode);
       break;
   }
   mark(c, kid, 1);

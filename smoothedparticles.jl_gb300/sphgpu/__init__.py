@@ -24,7 +24,8 @@ __all__ = ["ParticleSystem", "ParticleField", "create_cell_list", "apply", "appl
            "apply_binary", "sum", "SphError", "Operator", "SumFunction", "FLUID", "WALL",
            "FP64", "MIXED", "find_rho", "find_rho0", "internal_force", "find_pressure",
            "reset_rho", "reset_rho0", "reset_a", "accelerate", "move", "hydrostatic",
-           "DENSITY", "KERNEL", "PRESSURE", "SHEPARD", "wall_pressure"]
+           "DENSITY", "KERNEL", "PRESSURE", "SHEPARD", "wall_pressure", "Batch", "pipe_peak",
+           "memory_estimate"]
 
 
 class SphError(RuntimeError):
@@ -253,12 +254,93 @@ class ParticleSystem:
         self._check(self._lib.sph_launch_count(self._h, C.byref(c)))
         return c.value
 
+    def memory_usage(self) -> int:
+        """Device bytes this system holds now."""
+        b = C.c_uint64()
+        self._check(self._lib.sph_memory_usage(self._h, C.byref(b)))
+        return b.value
+
+    def idle(self) -> bool:
+        """True when all queued work of this system has finished (never waits)."""
+        i = C.c_int()
+        self._check(self._lib.sph_query(self._h, C.byref(i)))
+        return bool(i.value)
+
+    def set_tuning(self, warps_per_block: int):
+        """Warps per block of the pair passes (2, 4 or 8); results do not change."""
+        self._check(self._lib.sph_set_tuning(self._h, int(warps_per_block)))
+
+    def tuning(self) -> int:
+        w = C.c_int()
+        self._check(self._lib.sph_get_tuning(self._h, C.byref(w)))
+        return w.value
+
     def pair_stats(self, reset: bool = False) -> dict:
         """Hits per category: density, wall (pressure pass), force_fluid,
         force_wall, force_av."""
         v = (C.c_uint64 * 8)()
         self._check(self._lib.sph_pair_stats(self._h, v, 1 if reset else 0))
         return dict(density=v[0], wall=v[1], force_fluid=v[2], force_wall=v[3], force_av=v[4])
+
+
+class Batch:
+    """Many independent systems stepped together: each pair of steps is one
+    CUDA-graph launch whose branches (one per member) overlap on the device.
+    Members keep their own state; results equal stepping each alone."""
+
+    def __init__(self, members):
+        self._lib = L.load()
+        self.members = list(members)
+        arr = (C.c_void_p * len(self.members))(*[m._h.value for m in self.members])
+        h = C.c_void_p()
+        rc = self._lib.sph_batch_create(arr, len(self.members), C.byref(h))
+        if rc != 0:
+            raise SphError(rc, "sph_batch_create failed (members must hold particles, one device)")
+        self._h = h
+
+    def _check(self, rc):
+        if rc != 0:
+            msg = self._lib.sph_batch_last_error(self._h)
+            raise SphError(rc, msg.decode() if msg else "")
+
+    def step(self, nsteps: int = 2):
+        self._check(self._lib.sph_batch_step(self._h, int(nsteps)))
+
+    def synchronize(self):
+        self._check(self._lib.sph_batch_synchronize(self._h))
+
+    def stream(self) -> int:
+        p = C.c_void_p()
+        self._check(self._lib.sph_batch_stream(self._h, C.byref(p)))
+        return p.value or 0
+
+    def stats(self) -> dict:
+        a, b_, c = C.c_int64(), C.c_int64(), C.c_int64()
+        self._check(self._lib.sph_batch_stats(self._h, C.byref(a), C.byref(b_), C.byref(c)))
+        return dict(kernels_per_graph=a.value, graph_launches=b_.value, kernels=c.value)
+
+    def close(self):
+        if getattr(self, "_h", None):
+            self._lib.sph_batch_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def memory_estimate(params: dict, n: int, precision: int = FP64) -> int:
+    """Device bytes a system with these parameters holds with n particles
+    (host-side arithmetic, no GPU needed)."""
+    lib = L.load()
+    p = L.make_params(L.sph_params, params, precision)
+    b = C.c_uint64()
+    rc = lib.sph_memory_estimate(C.byref(p), int(n), C.byref(b))
+    if rc != 0:
+        raise SphError(rc, "sph_memory_estimate: invalid parameters")
+    return b.value
 
 
 def pipe_peak(which: str, device: int = 0) -> float:

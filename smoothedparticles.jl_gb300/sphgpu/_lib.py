@@ -135,6 +135,18 @@ PROTOTYPES = {
     "sph_pair_stats": (C.c_int, [_P, C.POINTER(C.c_uint64), C.c_int]),
     "sph_pipe_peak": (C.c_int, [C.c_int, C.c_int, C.POINTER(C.c_double)]),
     "sph_cell_list_noalloc": (C.c_int, [C.POINTER(sph_params), _I64, _P, _P, _P, _P]),
+    "sph_set_tuning": (C.c_int, [_P, C.c_int]),
+    "sph_get_tuning": (C.c_int, [_P, C.POINTER(C.c_int)]),
+    "sph_batch_create": (C.c_int, [C.POINTER(_P), C.c_int, C.POINTER(_P)]),
+    "sph_batch_destroy": (C.c_int, [_P]),
+    "sph_batch_last_error": (C.c_char_p, [_P]),
+    "sph_batch_step": (C.c_int, [_P, C.c_int]),
+    "sph_batch_synchronize": (C.c_int, [_P]),
+    "sph_batch_stats": (C.c_int, [_P, C.POINTER(_I64), C.POINTER(_I64), C.POINTER(_I64)]),
+    "sph_batch_stream": (C.c_int, [_P, C.POINTER(_P)]),
+    "sph_memory_estimate": (C.c_int, [C.POINTER(sph_params), _I64, C.POINTER(C.c_uint64)]),
+    "sph_memory_usage": (C.c_int, [_P, C.POINTER(C.c_uint64)]),
+    "sph_query": (C.c_int, [_P, C.POINTER(C.c_int)]),
 }
 
 _lib = None

@@ -117,10 +117,13 @@ def boundary_layer(dim: int, dr: float, shape: Box, width: float, keep=None) -> 
     bb = Box(lo, hi)
     dxs = ball_offsets(dim, dr, width)
     I = _lattice_axis(bb.lo[0], bb.hi[0], dr)
+    J = _lattice_axis(bb.lo[1], bb.hi[1], dr)
+    K = _lattice_axis(bb.lo[2], bb.hi[2], dr) if dim == 3 else np.zeros(1, np.int64)
+    # blocks of consecutive i keep memory bounded; the order stays i outer
+    step = max(1, (1 << 21) // (J.size * K.size))
     out = []
-    # one i-slab at a time keeps memory bounded; the order stays i outer
-    for i in I:
-        x = _slab(dim, bb, dr, i)
+    for i0 in range(0, I.size, step):
+        x = _block(dim, I[i0:i0 + step], J, K, dr)
         cand = ~shape.inside(x)
         if keep is not None:
             cand &= keep(x)
@@ -132,17 +135,17 @@ def boundary_layer(dim: int, dr: float, shape: Box, width: float, keep=None) -> 
     return np.concatenate(out) if out else np.zeros((0, 3))
 
 
-def _slab(dim: int, bb: Box, dr: float, i: int) -> np.ndarray:
-    J = _lattice_axis(bb.lo[1], bb.hi[1], dr)
+def _block(dim: int, I: np.ndarray, J: np.ndarray, K: np.ndarray, dr: float) -> np.ndarray:
+    """Lattice points i*dr, j*dr(, k*dr) for i in I, j in J(, k in K), i outer."""
     if dim == 2:
-        x = np.zeros((J.size, 3))
-        x[:, 0] = float(i) * dr
-        x[:, 1] = J.astype(np.float64) * dr
+        gi, gj = np.meshgrid(I, J, indexing="ij")
+        x = np.zeros((gi.size, 3))
+        x[:, 0] = gi.ravel().astype(np.float64) * dr
+        x[:, 1] = gj.ravel().astype(np.float64) * dr
         return x
-    K = _lattice_axis(bb.lo[2], bb.hi[2], dr)
-    gj, gk = np.meshgrid(J, K, indexing="ij")
-    x = np.empty((gj.size, 3))
-    x[:, 0] = float(i) * dr
+    gi, gj, gk = np.meshgrid(I, J, K, indexing="ij")
+    x = np.empty((gi.size, 3))
+    x[:, 0] = gi.ravel().astype(np.float64) * dr
     x[:, 1] = gj.ravel().astype(np.float64) * dr
     x[:, 2] = gk.ravel().astype(np.float64) * dr
     return x

@@ -1,0 +1,79 @@
+"""Host-side checks of the ensemble generator and the autotuner's size classes."""
+import math
+
+from sphgpu.ensemble import ensemble_specs
+from sphgpu import autotune
+
+
+def test_specs_reproducible_and_in_range():
+    a = ensemble_specs(256, seed=11)
+    b = ensemble_specs(256, seed=11)
+    assert a == b
+    assert len(a) == 256
+    for dr, hc, al in a:
+        assert 0.004 <= dr <= 0.02
+        assert 1.0 <= hc <= 2.0
+        assert 0.01 <= al <= 0.1
+    counts = [hc / (dr * dr) for dr, hc, al in a]
+    assert min(counts) < 5000 and max(counts) > 40000
+
+
+def test_size_classes():
+    assert autotune.size_class(1) == 0
+    assert autotune.size_class(2048) == 11
+    assert autotune.size_class(4095) == 11
+    assert autotune.size_class(4096) == 12
+    assert set(autotune.CHOICES) == {2, 4, 8}
+
+
+class _FakeSystem:
+    def __init__(self, n):
+        self.n = n
+        self.w = 4
+
+    def set_tuning(self, w):
+        self.w = w
+
+
+def test_apply_table():
+    sy = [_FakeSystem(3000), _FakeSystem(50000), _FakeSystem(5000)]
+    autotune.apply(sy, {11: (2, {}), 15: (8, {})})
+    assert [g.w for g in sy] == [2, 8, 4]
+
+
+def test_memory_estimate_host_only(sph_lib):
+    import sphgpu
+    from sphgpu import geometry as G
+    c = G.dam_break(2, 0.02)
+    a = sphgpu.memory_estimate(c.params, 1000)
+    b = sphgpu.memory_estimate(c.params, 2000)
+    d = sphgpu.memory_estimate(c.params, 3000)
+    assert 0 < a < b < d
+    # linear in n up to the 256-byte alignment of each buffer
+    assert abs((d - b) - (b - a)) <= 256 * 64
+    c3 = G.dam_break(3, 0.05)
+    assert sphgpu.memory_estimate(c3.params, 1000) > a  # larger hit lists in 3D
+    bad = dict(c.params, h=-1.0)
+    try:
+        sphgpu.memory_estimate(bad, 10)
+    except sphgpu.SphError:
+        pass
+    else:
+        raise AssertionError("negative h accepted")
+
+
+def test_request_stream_seeded():
+    from sphgpu.serve import request_stream, spacing_for, summarize
+    a = request_stream(200, rate=2.0, seed=3)
+    b = request_stream(200, rate=2.0, seed=3)
+    assert [(r.dim, r.dr, r.steps, r.precision, r.arrival) for r in a] == \
+           [(r.dim, r.dr, r.steps, r.precision, r.arrival) for r in b]
+    arr = [r.arrival for r in a]
+    assert arr == sorted(arr) and arr[0] > 0
+    assert 60 < arr[-1] < 160  # 200 arrivals at 2/s
+    for r in a:
+        assert 200 <= r.steps <= 2000 and r.dim in (2, 3) and r.precision in (0, 1)
+        n = 2.0 / r.dr ** r.dim
+        assert 5e3 * 0.999 <= n <= 2e6 * 1.001
+    assert abs(spacing_for(2, 2.0 / 0.01 ** 2) - 0.01) < 1e-15
+    assert summarize([], 1.0)["requests"] == 0

@@ -1,0 +1,65 @@
+"""The served stream: requests admitted by HBM budget while others run, all
+stepped concurrently; each result equals the same request run alone (exact
+equality -- members never interact and run the launches of sph_step)."""
+import numpy as np
+import pytest
+
+import sphgpu
+from sphgpu.serve import Request, Server, summarize
+
+pytestmark = pytest.mark.gpu
+
+
+def alone(r, fields):
+    c = r.case()
+    g = sphgpu.ParticleSystem(c.params, r.precision)
+    g.upload(c.x, c.v, type=c.type)
+    g.init_state()
+    g.step(r.steps)
+    out = {f: g.get(f) for f in fields}
+    g.close()
+    return out
+
+
+def test_served_results_equal_alone(gpu):
+    F, M = sphgpu.FP64, sphgpu.MIXED
+    reqs = [Request(0, 2, 0.04, 24, F, 0.00), Request(1, 3, 0.08, 10, M, 0.02),
+            Request(2, 2, 0.03, 31, M, 0.05), Request(3, 3, 0.06, 12, F, 0.05),
+            Request(4, 2, 0.05, 7, F, 0.10, col_height=1.4, alpha=0.06),
+            Request(5, 2, 0.035, 20, M, 0.12, col_height=1.1)]
+    est = []
+    for r in reqs:
+        c = r.case()
+        est.append(sphgpu.memory_estimate(c.params, c.n, r.precision))
+    # room for the three largest together: later arrivals must wait for memory
+    budget = sum(sorted(est)[-3:])
+    srv = Server(budget, max_slots=4, chunk=4)
+    t = __import__("time").perf_counter()
+    done = srv.run(reqs)
+    makespan = __import__("time").perf_counter() - t
+    assert sorted(r.rid for r in done) == list(range(len(reqs)))
+    assert srv.peak_bytes <= budget
+    assert srv.peak_slots <= 4
+    for r in done:
+        assert r.bytes == est[r.rid]
+        assert r.admitted >= r.arrival and r.done >= r.admitted
+        ref = alone(r, srv.result_fields)
+        for f in srv.result_fields:
+            assert np.array_equal(r.result[f], ref[f]), f"request {r.rid}: field {f} differs"
+        assert r.pairs > 0
+    s = summarize(done, makespan)
+    assert s["requests"] == len(reqs) and s["p99_latency_s"] >= s["p50_latency_s"]
+
+
+def test_usage_matches_estimate(gpu):
+    r = Request(0, 3, 0.07, 2, sphgpu.MIXED, 0.0)
+    c = r.case()
+    g = sphgpu.ParticleSystem(c.params, r.precision)
+    g.upload(c.x, c.v, type=c.type)
+    assert g.memory_usage() == sphgpu.memory_estimate(c.params, c.n, r.precision)
+    g.init_state()
+    g.step(2)
+    assert g.memory_usage() == sphgpu.memory_estimate(c.params, c.n, r.precision)
+    g.synchronize()
+    assert g.idle()
+    g.close()
