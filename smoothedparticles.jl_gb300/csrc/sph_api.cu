@@ -28,7 +28,10 @@ struct sph_system {
   int cap = 0;              // particles the arena holds
   int n_host = 0;           // upper bound of the device-resident count
   bool cells_valid = false;
-  bool aux_fresh = false;  // FP32 neighbour copies current (mixed precision)
+  // FP32 neighbour records current (mixed precision): of the fluid particles
+  // (written by a fused density pass) and of the walls (wall-pressure pass)
+  bool aux_fluid = false;
+  bool aux_wall = false;
   bool lists_valid = false;  // hit lists of the last density pass match cells and positions
   std::string err;
   // launch accounting and optional per-kernel CUDA-event timing
@@ -166,8 +169,8 @@ size_t carve(sph_system* s, char* base, size_t C) {
     st->oid = (long long*)take(8 * C);
     st->pl = (float4*)take(16 * C);
   }
-  s->cur.vr = s->alt.vr = (float4*)take(16 * C);
-  s->cur.rhof = s->alt.rhof = (float*)take(4 * C);
+  s->cur.rec = s->alt.rec =
+      s->params.precision == SPH_PREC_MIXED ? (float4*)take(32 * C) : nullptr;
   BinScratch& b = s->b;
   b.keys = (int*)take(4 * C);
   b.slots = (int*)take(4 * C);
@@ -183,12 +186,26 @@ size_t carve(sph_system* s, char* base, size_t C) {
   b.max_items = max_work_items((int)C, s->geo.key_max);
   b.items = (int2*)take(8 * (size_t)b.max_items);
   b.item_partial = (int*)take(4 * (size_t)b.max_items);
-  // hits per target: ~256 in the 3D lattice interior (H = 4 dr), ~68 in 2D
-  // (H = 4.8 dr); the capacity leaves room for compression, and an overflow
-  // only sends that warp back to a full traversal
-  b.hit_cap = D == 3 ? 384 : 160;
-  b.hits = (int*)take(4 * (size_t)b.hit_cap * C);
-  b.hit_count = (int*)take(4 * C);
+  if (s->params.precision == SPH_PREC_MIXED) {
+    // hit masks: a full 3D item (32 targets, cells of ~64 particles) has 54
+    // chunks, ~1.7 per particle; 2D items ~0.4 per particle.  Items beyond
+    // the capacity traverse in the force pass too.
+    const long long cap = 2LL * (long long)C + 64;
+    b.ck_cap = (int)(cap < 0x3ffffffLL * 16 ? cap : 0x3ffffffLL * 16);
+    b.ck_mask = (unsigned*)take(4 * 32 * (size_t)b.ck_cap);
+    b.hit_cap = 0;
+    b.hits = nullptr;
+    b.hit_count = nullptr;
+  } else {
+    // hits per target: ~256 in the 3D lattice interior (H = 4 dr), ~68 in
+    // 2D (H = 4.8 dr); the capacity leaves room for compression, and an
+    // overflow only sends that warp back to a full traversal
+    b.hit_cap = D == 3 ? 384 : 160;
+    b.hits = (int*)take(4 * (size_t)b.hit_cap * C);
+    b.hit_count = (int*)take(4 * C);
+    b.ck_cap = 0;
+    b.ck_mask = nullptr;
+  }
   s->staging = take(72 * C + 64);
   return off;
 }
@@ -225,18 +242,26 @@ int read_count(sph_system* s, int* n) {
 
 int pair_pass(sph_system* s, int op, int self, int reset, int fuse_eos) {
   cudaError_t e;
-  if (s->params.precision == SPH_PREC_MIXED)
+  if (s->params.precision == SPH_PREC_MIXED) {
+    // the wall pressure reads fluid records, the force every record
+    const bool fresh = op == SPH_OP_FORCE           ? s->aux_fluid && s->aux_wall
+                       : op == SPH_OP_WALL_PRESSURE ? s->aux_fluid
+                                                    : true;
     e = launch_pair_mixed(ctx(s), s->cur, s->geo, s->k, s->b, s->n_host, op, self, reset, fuse_eos,
-                          s->aux_fresh ? 1 : 0, s->lists_valid ? 1 : 0);
-  else
+                          fresh ? 1 : 0, s->lists_valid ? 1 : 0);
+    if (!fresh && e == cudaSuccess) s->aux_fluid = s->aux_wall = true;  // rebuilt first
+  } else {
     e = launch_pair_fp64(ctx(s), s->cur, s->geo, s->k, s->b, s->n_host, op, self, reset, fuse_eos,
                          s->lists_valid ? 1 : 0);
+  }
   if (e == cudaErrorNotSupported)
     return fail(s, SPH_ERR_UNSUPPORTED, "pair operator %d is not provided in this precision", op);
   if (e != cudaSuccess) return fail(s, SPH_ERR_CUDA, "pair pass launch: %s", cudaGetErrorString(e));
-  // a fused density pass leaves the FP32 copies of the fluid current; a
-  // non-fused one changes rho without P, so the copies are stale
-  if (op == SPH_OP_DENSITY) s->aux_fresh = fuse_eos != 0;
+  // a fused density pass leaves the fluid records current; a non-fused one
+  // changes rho without P, so they are stale; the wall pressure writes the
+  // walls' records
+  if (op == SPH_OP_DENSITY) s->aux_fluid = fuse_eos != 0;
+  if (op == SPH_OP_WALL_PRESSURE) s->aux_wall = true;
   // the density passes keep every fluid target's hit list for the force pass
   if (op == SPH_OP_DENSITY || op == SPH_OP_DENSITY_REF) s->lists_valid = true;
   return SPH_OK;
@@ -248,7 +273,7 @@ int binning(sph_system* s, int step_mode, int gather_mode) {
   if (e != cudaSuccess) return fail(s, SPH_ERR_CUDA, "binning launch: %s", cudaGetErrorString(e));
   std::swap(s->cur, s->alt);
   s->cells_valid = true;
-  s->aux_fresh = false;
+  s->aux_fluid = s->aux_wall = false;
   s->lists_valid = false;
   return SPH_OK;
 }
@@ -260,7 +285,7 @@ int unary(sph_system* s, int op) {
     s->cells_valid = false;
     s->lists_valid = false;
   }
-  s->aux_fresh = false;
+  s->aux_fluid = s->aux_wall = false;
   return SPH_OK;
 }
 
@@ -385,7 +410,7 @@ static int setup_host(const sph_params* p, sph_system* s) {
 static size_t cells_bytes(const sph_system* s) {
   const size_t nb = (size_t)s->geo.key_max + 3;
   const size_t scan_ints = scan_tmp_ints((int)nb) + 64;
-  return align_up(4 * nb) * 4 + align_up(4 * scan_ints) + 2048;
+  return align_up(4 * nb) * 5 + align_up(4 * scan_ints) + 2048;
 }
 
 int sph_create(const sph_params* p, int device, sph_system** out) {
@@ -429,6 +454,8 @@ int sph_create(const sph_params* p, int device, sph_system** out) {
   s->b.item_off = (int*)c;
   c += align_up(4 * nb);
   s->b.cell_fluid = (int*)c;
+  c += align_up(4 * nb);
+  s->b.chunk_off = (int*)c;
   c += align_up(4 * nb);
   s->b.scan_tmp = (int*)c;
   c += align_up(4 * scan_ints);
@@ -519,7 +546,7 @@ int sph_upload(sph_system* s, int64_t n, const double* x, const double* v, const
   CK(cudaStreamSynchronize(s->stream));
   s->n_host = (int)n;
   s->cells_valid = false;
-  s->aux_fresh = false;
+  s->aux_fluid = s->aux_wall = false;
   s->lists_valid = false;
   return SPH_OK;
 }
@@ -576,7 +603,7 @@ int sph_set_field(sph_system* s, int field, const void* in) {
   CK(cudaStreamSynchronize(s->stream));
   if (field == SPH_FIELD_X) s->cells_valid = false;
   if (field == SPH_FIELD_X || field == SPH_FIELD_TYPE) s->lists_valid = false;
-  s->aux_fresh = false;
+  s->aux_fluid = s->aux_wall = false;
   return SPH_OK;
 }
 

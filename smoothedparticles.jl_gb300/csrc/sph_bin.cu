@@ -228,6 +228,9 @@ __global__ void __launch_bounds__(kThreads) bin_gather_kernel(State cur, State a
   alt.rid[dst] = rid;
   alt.cell[dst] = key;
   alt.pl[dst] = make_float4(xl[0], xl[1], xl[2], __int_as_float(t));
+  // mixed precision: the position half of the FP32 neighbour record, with the
+  // type in the sign bit (the pair passes fill in rho, v and P/rho^2)
+  if (alt.rec) alt.rec[2 * dst] = make_float4(xl[0], xl[1], xl[2], t == kFluid ? 1.f : -1.f);
   b.inv_rid[rid] = dst;
   if (t == kFluid) {  // fluid per cell, one atomic per cell and warp
     const unsigned peers = __match_any_sync(__activemask(), key);
@@ -256,6 +259,24 @@ __global__ void __launch_bounds__(kThreads) items_write_kernel(Geometry g, BinSc
   const int c = b.cell_start[k + 1] - st;
   int off = b.item_off[k];
   for (int t = 0; t < c; t += 32, ++off) b.items[off] = make_int2(st + t, min(32, c - t));
+}
+
+// ---- mask slots of the mixed-precision pair passes: every item of a cell
+// with fluid gets one slot per 32-candidate chunk of the cell's neighbour
+// cells (the chunk sequence of the pair traversal)
+__global__ void __launch_bounds__(kThreads) chunks_count_kernel(Geometry g, BinScratch b) {
+  const int k = blockIdx.x * kThreads + threadIdx.x;  // 0 .. key_max + 2
+  if (k > g.key_max + 2) return;
+  int v = 0;
+  if (k >= 1 && k <= g.key_max && b.cell_fluid[k] > 0) {
+    int nc = 0;
+    for (int j = 0; j < g.n_diff; ++j) {
+      const int nk = k + g.key_diff[j];
+      if (nk >= 1 && nk <= g.key_max) nc += (b.cell_start[nk + 1] - b.cell_start[nk] + 31) >> 5;
+    }
+    v = ((b.cell_start[k + 1] - b.cell_start[k] + 31) >> 5) * nc;
+  }
+  b.counts[k] = v;  // the item counts are no longer needed once items exist
 }
 
 // ---- generic exclusive scan (3 kernels)
@@ -372,6 +393,14 @@ cudaError_t launch_binning(const LaunchCtx& c, const State& cur, const State& al
   else
     bin_gather_kernel<3><<<blocks, kThreads, 0, c.stream>>>(cur, alt, g, k, b, gather_mode);
   mark(c, SPH_KERNEL_BIN_GATHER, 1);
+  if (b.ck_mask) {
+    // after the gather: it counts each cell's fluid particles
+    mark(c, SPH_KERNEL_BIN_SCAN, 0);
+    chunks_count_kernel<<<(nbuckets + kThreads - 1) / kThreads, kThreads, 0, c.stream>>>(g, b);
+    mark(c, SPH_KERNEL_BIN_SCAN, 1);
+    e = launch_scan(c, b.counts, b.chunk_off, nbuckets, b.scan_tmp);
+    if (e != cudaSuccess) return e;
+  }
   return cudaGetLastError();
 }
 

@@ -37,10 +37,11 @@ struct State {
   int* cell;
   long long* oid;
   float4* pl;
-  // FP32 neighbour data of the mixed-precision path, rebuilt every step after
-  // the binning (so not ping-ponged): (vx, vy, vz, P/rho^2) and rho
-  float4* vr;
-  float* rhof;
+  // FP32 neighbour records of the mixed-precision path, 32 bytes per
+  // particle, rebuilt every step after the binning (so not ping-ponged):
+  // rec[2i] = (cell-relative x, y, z, rho with the sign bit set for walls),
+  // rec[2i+1] = (vx, vy, vz, P/rho^2)
+  float4* rec;
 };
 
 // Cell-table geometry (structs.jl:66-82).  key_max and key_diff fit int32
@@ -101,14 +102,22 @@ struct BinScratch {
   int2* items;      // (first target, count)
   int* item_off;    // key_max + 3: exclusive prefix of items per cell
   int max_items;    // capacity of `items`
-  // hit lists (layout in sph_cellwarp.cuh: cw_list), t < hit_count[i]
-  // (entry = neighbour index | neighbour-cell number << 27), written by the
-  // density passes and read back by the force pass of the same binning
+  // FP64 passes: hit lists (layout in sph_cellwarp.cuh: cw_list), t <
+  // hit_count[i] (entry = neighbour index | neighbour-cell number << 27),
+  // written by the density passes and read back by the force pass of the
+  // same binning (null in mixed-precision systems)
   int* hits;
   int* hit_count;
   int* item_partial;  // 1 when an item's list overflowed hit_cap
   int hit_cap;
   int* cell_fluid;    // key_max + 3: fluid particles per cell
+  // mixed-precision passes: one 32-bit hit mask per lane and 32-candidate
+  // chunk of the neighbour sequence (sph_pair32.cu); item j of cell k owns
+  // the slots chunk_off[k] + j * n_k .. + n_k, n_k = the chunks of k's
+  // neighbour cells (null in FP64 systems)
+  unsigned* ck_mask;  // ck_cap * 32
+  int ck_cap;
+  int* chunk_off;     // key_max + 3: exclusive prefix of the cells' slots
 };
 
 // Upper bound of the work-list length for n particles (every cell with

@@ -1,19 +1,34 @@
 // sph_pair32.cu -- mixed-precision pair passes.
 //
-// Same traversal and the same candidate classification as the FP64 passes
-// (FP32 test on cell-relative positions, FP64 band test with round-to-nearest
-// intrinsics), so the set of pairs is identical to the FP64 path for the same
-// positions.  What changes is the arithmetic on a hit:
-//   * the separation is the FP32 cell-relative one the scan tested (x_p - x_q
-//     with both positions within one cell of their origins, accurate to
-//     ~2^-21 h), rebuilt from the hit's index and neighbour-cell number;
+// Same cells, the same neighbour sequence and the same candidate
+// classification as the FP64 passes (FP32 test on cell-relative positions,
+// FP64 band test with round-to-nearest intrinsics), so the set of pairs is
+// identical to the FP64 path for the same positions.  What changes is the
+// arithmetic on a hit:
+//   * the separation is the FP32 cell-relative one (x_p - x_q with both
+//     positions within one cell of their origins, accurate to ~2^-21 h);
 //   * kernel values, pressure, viscosity and XSPH terms are FP32, with the
 //     neighbour's (v, P/rho^2, rho) read from a 20-byte FP32 copy;
-//   * each queue batch (<= 32 hits) is summed in FP32 and folded into FP64
-//     accumulators, so FP64 adds are per batch, not per hit;
+//   * a lane's hits are summed in FP32 in batches of at most 32 and each
+//     batch is folded into FP64 accumulators;
 //   * positions, the self term, the EOS, the wall-pressure quotient and the
 //     time integration stay FP64.
-// Built with FMA contraction (the FP64 band test uses explicit intrinsics).
+//
+// Traversal (one warp per work item of <= 32 targets of one cell): every
+// neighbour cell is visited in chunks of 32 candidates, staged into shared
+// memory with coalesced loads.  Per chunk each lane
+//   A. classifies the 32 staged candidates into a hit mask and a band mask
+//      (FP32 distances from broadcast reads),
+//   B. resolves band candidates with the FP64 test, all lanes in lockstep,
+//   C. walks its hit mask in candidate order and accumulates from shared
+//      memory -- so each target's sums keep the reference's neighbour order.
+// The density pass stores the final hit masks (4 bytes per lane per chunk,
+// written coalesced) in slots counted during the binning; the force pass of
+// the same binning replays the chunk sequence, reads the masks, stages only
+// chunks with hits and skips steps A and B.  An item whose slots do not fit
+// the mask capacity traverses in both passes.
+// Built with FMA contraction (the FP64 band test uses explicit intrinsics;
+// any FP32 evaluation order stays within the classification band's margin).
 #include "sph_cellwarp.cuh"
 #include "sph_launch.h"
 #include "sphgpu.h"
@@ -22,6 +37,24 @@ namespace sphgpu {
 
 namespace {
 
+// Chunk table of the force pass's per-lane walk (3D items have ~54 chunks).
+constexpr int kMaxChunks = 128;
+
+template <int OP>
+struct MxShared {
+  static constexpr bool kRec = OP == SPH_OP_FORCE || OP == SPH_OP_WALL_PRESSURE;
+  static constexpr int kTab = OP == SPH_OP_FORCE ? kMaxChunks : 1;
+  // staged candidates: density passes stage positions (type bits in .w);
+  // force and wall pressure stage the 32-byte neighbour record
+  float4 c0[32];               // (x, y, z) cell-relative, .w = type / signed rho
+  float4 c1[kRec ? 32 : 1];    // (vx, vy, vz, P/rho^2)
+  float4 offs[27];             // offset of each neighbour cell from the target cell
+  int cb[kTab];                // first candidate of each chunk of the item
+  unsigned char cc[kTab];      // neighbour-cell number of each chunk
+};
+
+// coordinate of an empty staging slot: never within the support
+constexpr float kFar = 1.0e18f;
 
 // FP32 Wendland quintic pieces: t = 1 - r/h (0 outside the support)
 __device__ __forceinline__ float kt32(const Consts& k, float r) {
@@ -36,131 +69,59 @@ __device__ __forceinline__ float krdw32(const Consts& k, float t) { return k.crf
 
 __device__ __forceinline__ float fsqrt(float ss) { return ss > 0.f ? ss * rsqrtf(ss) : 0.f; }
 
+// The FP32 neighbour record of particle i: (cell-relative x, y, z, rho with
+// the sign bit set for walls) and (vx, vy, vz, P/rho^2).
+__device__ __forceinline__ void put_rec(const State& s, int i, const float4& pl, bool fluid,
+                                        float rho, float vx, float vy, float vz, float pr) {
+  const float rr = fabsf(rho);
+  s.rec[2 * i] = make_float4(pl.x, pl.y, pl.z, fluid ? rr : -rr);
+  s.rec[2 * i + 1] = make_float4(vx, vy, vz, pr);
+}
+
+// one 256-bit load of a record (32-byte aligned: the array is 256-byte
+// aligned and records are 32 bytes)
+__device__ __forceinline__ void ld_rec(const float4* p, float4& a, float4& b) {
+  asm("ld.global.nc.v8.f32 {%0, %1, %2, %3, %4, %5, %6, %7}, [%8];"
+      : "=f"(a.x), "=f"(a.y), "=f"(a.z), "=f"(a.w), "=f"(b.x), "=f"(b.y), "=f"(b.z), "=f"(b.w)
+      : "l"(p));
+}
+
 template <int DIM>
 __global__ void __launch_bounds__(256) aux_refresh_kernel(State s, BinScratch b) {
   const int n = *b.d_n;
   const int i = blockIdx.x * 256 + threadIdx.x;
   if (i >= n) return;
-  s.vr[i] = make_float4((float)s.v[0][i], (float)s.v[1][i], DIM == 3 ? (float)s.v[2][i] : 0.f,
-                        (float)s.Pr[i]);
-  s.rhof[i] = (float)s.rho[i];
+  put_rec(s, i, s.pl[i], s.type[i] == kFluid, (float)s.rho[i], (float)s.v[0][i],
+          (float)s.v[1][i], DIM == 3 ? (float)s.v[2][i] : 0.f, (float)s.Pr[i]);
 }
 
-// The operator bodies on a hit in FP32 (list entry = q | neighbour cell << 27;
-// the separation is rebuilt from q's cell-relative position and the offset of
-// its cell, exactly as the traversal computed it).
+// A lane's accumulators and the operator bodies on a hit, in FP32.
 template <int DIM, int OP>
-struct Proc32 {
-  const State& s;
+struct Acc32 {
   const Consts& k;
-  float4 pi4;
+  float4 pi4;  // own cell-relative position
   float4 vp;   // own (vx, vy, vz, P/rho^2)
   float rhop;
+  float f0, f1, f2, f3, f4, f5;  // the current FP32 batch
+  int nh;                        // hits in the current batch
   double acc, ax, ay, az, sx, sy, sz, wp, wg, ws;
   int c0, c1, c2;
 
-  __device__ Proc32(const State& s_, const Consts& k_) : s(s_), k(k_) {
+  __device__ explicit Acc32(const Consts& k_) : k(k_) {
     acc = ax = ay = az = sx = sy = sz = wp = wg = ws = 0.0;
     vp = make_float4(0.f, 0.f, 0.f, 0.f);
     pi4 = vp;
     rhop = 0.f;
+    f0 = f1 = f2 = f3 = f4 = f5 = 0.f;
+    nh = 0;
     c0 = c1 = c2 = 0;
   }
 
-  __device__ __forceinline__ int entry(int q, int c, int tq) const {
-    if (OP == SPH_OP_WALL_PRESSURE && tq != kFluid) return kCwSkip;
-    return q | (c << kCwCellBits);
-  }
-
-  const float4* offs;  // the warp's neighbour-cell offsets (shared memory)
-
-  __device__ __forceinline__ void process(const int* list, int stride, int cnt) {
-    for (int t0 = 0; t0 < cnt; t0 += 32) {
-      process_batch(list + (size_t)t0 * stride, stride, min(32, cnt - t0));
-    }
-  }
-
-  // <= 32 hits summed in FP32, folded into the FP64 accumulators; the loads
-  // of four hits are issued before their arithmetic
-  __device__ __forceinline__ void process_batch(const int* list, int stride, int cnt) {
-    float f0 = 0.f, f1 = 0.f, f2 = 0.f, f3 = 0.f, f4 = 0.f, f5 = 0.f;
-    for (int t0 = 0; t0 < cnt; t0 += 4) {
-      int e4[4];
-      float4 p4[4], v4[4];
-      float r4[4];
-#pragma unroll
-      for (int j = 0; j < 4; ++j)
-        e4[j] = t0 + j < cnt ? __ldg(&list[(size_t)(t0 + j) * stride]) : kCwSkip;
-#pragma unroll
-      for (int j = 0; j < 4; ++j) {
-        const int q = e4[j] == kCwSkip ? 0 : e4[j] & kCwIndexMask;
-        p4[j] = __ldg(&s.pl[q]);
-        if (OP == SPH_OP_FORCE || OP == SPH_OP_WALL_PRESSURE) {
-          v4[j] = __ldg(&s.vr[q]);
-          r4[j] = __ldg(&s.rhof[q]);
-        }
-      }
-#pragma unroll
-      for (int j = 0; j < 4; ++j) {
-        if (t0 + j >= cnt) break;
-        const int e = e4[j];
-        if (e == kCwSkip) continue;  // a band candidate beyond the support
-        const float4 off = offs[(unsigned)e >> kCwCellBits];
-        const float4 pq = p4[j];
-        const float hx = (pi4.x - pq.x) - off.x;
-        const float hy = (pi4.y - pq.y) - off.y;
-        const float hz = DIM == 3 ? (pi4.z - pq.z) - off.z : 0.f;
-        float ss = hx * hx + hy * hy;
-        if (DIM == 3) ss = ss + hz * hz;
-        const float r = fsqrt(ss);
-        const float kt = kt32(k, r);
-        const bool fluid = __float_as_int(pq.w) == kFluid;
-        if (OP != SPH_OP_FORCE || fluid) ++c0; else ++c1;
-        if (OP == SPH_OP_DENSITY || OP == SPH_OP_DENSITY_REF) {
-          // the shape t^4 (1 + 4x) only; m * C_w is applied in FP64 per batch
-          const float t2 = kt * kt;
-          f0 += (t2 * t2) * (5.f - 4.f * kt);
-        } else if (OP == SPH_OP_WALL_PRESSURE) {
-          const float w = kw32(k, r, kt);
-          float gd = k.gf[0] * hx + k.gf[1] * hy;
-          if (DIM == 3) gd += k.gf[2] * hz;
-          const float rq = r4[j];
-          const float Pq = v4[j].w * rq * rq;
-          f0 += Pq * w;
-          f1 += (rq * gd) * w;
-          f2 += w;
-        } else if (fluid) {
-          const float4 vq = v4[j];
-          const float rq = r4[j];
-          const float ker = k.massf * krdw32(k, kt);
-          const float dvx = vp.x - vq.x, dvy = vp.y - vq.y, dvz = vp.z - vq.z;
-          float vdx = dvx * hx + dvy * hy;
-          if (DIM == 3) vdx += dvz * hz;
-          const float inv_rb = __fdividef(2.f, rhop + rq);
-          float pi = 0.f;
-          if (vdx < 0.f) {
-            const float mu = __fdividef(k.h_smoothf * vdx, ss + k.eta2f);
-            pi = (-k.alpha_c0f * mu) * inv_rb;
-            ++c2;
-          }
-          const float cf = -ker * ((vp.w + vq.w) + pi);
-          f0 += cf * hx;
-          f1 += cf * hy;
-          f2 += cf * hz;
-          const float wx = k.massf * kw32(k, r, kt) * inv_rb;
-          f3 -= wx * dvx;
-          f4 -= wx * dvy;
-          f5 -= wx * dvz;
-        } else {
-          const float cf = -(k.massf * krdw32(k, kt)) * (vp.w + v4[j].w);
-          f0 += cf * hx;
-          f1 += cf * hy;
-          f2 += cf * hz;
-        }
-      }
-    }
+  // the batch into the FP64 accumulators
+  __device__ __forceinline__ void fold() {
+    if (nh == 0) return;
     if (OP == SPH_OP_DENSITY || OP == SPH_OP_DENSITY_REF) {
-      acc += (k.mass * k.cw) * (double)f0;
+      acc += (k.mass * k.cw) * (double)f0;  // m * C_w applied in FP64
     } else if (OP == SPH_OP_WALL_PRESSURE) {
       wp += (double)f0;
       wg += (double)f1;
@@ -173,14 +134,295 @@ struct Proc32 {
       sy += (double)f4;
       sz += (double)f5;
     }
+    f0 = f1 = f2 = f3 = f4 = f5 = 0.f;
+    nh = 0;
+  }
+
+  // a hit on the neighbour with position / record (pq, vq) in a cell at
+  // offset `off` from the target's cell
+  __device__ __forceinline__ void hit(const float4& pq, const float4& vq, const float4& off) {
+    const float hx = (pi4.x - pq.x) - off.x;
+    const float hy = (pi4.y - pq.y) - off.y;
+    const float hz = DIM == 3 ? (pi4.z - pq.z) - off.z : 0.f;
+    float ss = hx * hx + hy * hy;
+    if (DIM == 3) ss = ss + hz * hz;
+    const float r = fsqrt(ss);
+    const float kt = kt32(k, r);
+    ++nh;
+    if (OP == SPH_OP_DENSITY || OP == SPH_OP_DENSITY_REF) {
+      ++c0;
+      // the shape t^4 (1 + 4x) only; m * C_w is applied per batch
+      const float t2 = kt * kt;
+      f0 += (t2 * t2) * (5.f - 4.f * kt);
+    } else if (OP == SPH_OP_WALL_PRESSURE) {
+      ++c0;
+      // Adami, Hu & Adams (2012) wall pressure, g . (x_w - x_f)
+      const float w = kw32(k, r, kt);
+      float gd = k.gf[0] * hx + k.gf[1] * hy;
+      if (DIM == 3) gd += k.gf[2] * hz;
+      const float rq = fabsf(pq.w);
+      const float Pq = vq.w * rq * rq;
+      f0 += Pq * w;
+      f1 += (rq * gd) * w;
+      f2 += w;
+    } else if (!signbit(pq.w)) {
+      ++c0;
+      // pressure (collapse_symplectic.jl:114-118) + Monaghan viscosity + XSPH
+      const float rq = pq.w;
+      const float ker = k.massf * krdw32(k, kt);
+      const float dvx = vp.x - vq.x, dvy = vp.y - vq.y, dvz = vp.z - vq.z;
+      float vdx = dvx * hx + dvy * hy;
+      if (DIM == 3) vdx += dvz * hz;
+      const float inv_rb = __fdividef(2.f, rhop + rq);
+      float pi = 0.f;
+      if (vdx < 0.f) {
+        const float mu = __fdividef(k.h_smoothf * vdx, ss + k.eta2f);
+        pi = (-k.alpha_c0f * mu) * inv_rb;
+        ++c2;
+      }
+      const float cf = -ker * ((vp.w + vq.w) + pi);
+      f0 += cf * hx;
+      f1 += cf * hy;
+      f2 += cf * hz;
+      const float wx = k.massf * kw32(k, r, kt) * inv_rb;
+      f3 -= wx * dvx;
+      f4 -= wx * dvy;
+      f5 -= wx * dvz;
+    } else {
+      ++c1;
+      // wall neighbour: pressure term with the wall pressure
+      const float cf = -(k.massf * krdw32(k, kt)) * (vp.w + vq.w);
+      f0 += cf * hx;
+      f1 += cf * hy;
+      f2 += cf * hz;
+    }
   }
 };
+
+// Stages candidates [base, base + m) of one neighbour cell; empty slots get a
+// far-away position and the type of no operator's neighbour.
+template <int OP>
+__device__ __forceinline__ void mx_stage(const State& s, MxShared<OP>& sh, int lane, int base,
+                                         int m) {
+  __syncwarp();
+  if (MxShared<OP>::kRec) {
+    if (lane < m) {
+      ld_rec(s.rec + 2 * (base + lane), sh.c0[lane], sh.c1[lane]);
+    } else {
+      sh.c0[lane] = make_float4(kFar, kFar, kFar, -1.f);
+    }
+  } else {
+    sh.c0[lane] = lane < m ? __ldg(&s.pl[base + lane])
+                           : make_float4(kFar, kFar, kFar, __int_as_float(-1));
+  }
+  __syncwarp();
+}
+
+// Step A: hit mask (inside or in the band) and band mask of the 32 staged
+// candidates for a target at (ax, ay, az) relative to their cell.  The wall
+// pressure takes fluid neighbours only.
+template <int DIM, int OP>
+__device__ __forceinline__ void mx_classify(const MxShared<OP>& sh, const Consts& k, float ax,
+                                            float ay, float az, unsigned& hit, unsigned& band) {
+  unsigned h = 0u, bd = 0u;
+#pragma unroll
+  for (int u = 0; u < 32; ++u) {
+    const float4 pq = sh.c0[u];
+    const float dx = ax - pq.x;
+    const float dy = ay - pq.y;
+    float ss = dx * dx + dy * dy;
+    if (DIM == 3) {
+      const float dz = az - pq.z;
+      ss = ss + dz * dz;
+    }
+    bool in = !(ss > k.s_hi);
+    if (OP == SPH_OP_WALL_PRESSURE) in = in && !signbit(pq.w);
+    if (in) h |= 1u << u;
+    if (!(ss < k.s_lo)) bd |= 1u << u;
+  }
+  hit = h;
+  band = bd & h;
+}
+
+// Step B: the reference's FP64 test for every band candidate, the lanes
+// taking their band candidates together (on the benchmark lattices many
+// candidates lie exactly at r = h).
+template <int DIM>
+__device__ __forceinline__ void mx_resolve(const State& s, const Consts& k, const CwTarget& t,
+                                           int base, unsigned& hit, unsigned band) {
+  while (__any_sync(0xffffffffu, band != 0u)) {
+    if (band) {
+      const int u = __ffs(band) - 1;
+      band &= band - 1u;
+      if (!within_rn<DIM>(s, k, t.xp, base + u)) hit &= ~(1u << u);
+    }
+  }
+}
+
+// Force pass over stored masks: the chunk table of the item (first candidate
+// and neighbour-cell number of every chunk, in traversal order).  False when
+// it does not match the slots the binning counted or does not fit.
+__device__ __forceinline__ bool mx_chunk_table(const Geometry& g, const BinScratch& b,
+                                               MxShared<SPH_OP_FORCE>& sh, int lane,
+                                               const CwTarget& t, int nc) {
+  int st = 0, nch = 0;
+  if (lane < g.n_diff) {
+    const int nk = t.key + g.key_diff[lane];
+    if (nk >= 1 && nk <= g.key_max) {
+      st = __ldg(&b.cell_start[nk]);
+      nch = (__ldg(&b.cell_start[nk + 1]) - st + 31) >> 5;
+    }
+  }
+  int incl = nch;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const int v = __shfl_up_sync(0xffffffffu, incl, o);
+    if (lane >= o) incl += v;
+  }
+  const int total = __shfl_sync(0xffffffffu, incl, 31);
+  if (total != nc || total > kMaxChunks) return false;
+  for (int j = 0, f = incl - nch; j < nch; ++j, ++f) {
+    sh.cb[f] = st + 32 * j;
+    sh.cc[f] = (unsigned char)lane;
+  }
+  __syncwarp();
+  return true;
+}
+
+// Force pass over stored masks: every lane walks its own hits (chunk by
+// chunk, bit by bit: the traversal order) and loads each neighbour's record
+// directly, so lanes never wait for one another within a chunk.  Two hits per
+// step keep two record loads in flight.
+__device__ __forceinline__ int mx_next(const unsigned* mrow, const MxShared<SPH_OP_FORCE>& sh,
+                                       int nc, int& gi, unsigned& cm, int& cell) {
+  while (cm == 0u && gi + 1 < nc) {
+    ++gi;
+    cm = __ldg(mrow + (size_t)gi * 32);
+  }
+  if (cm == 0u) return -1;
+  const int u = __ffs(cm) - 1;
+  cm &= cm - 1u;
+  cell = sh.cc[gi];
+  return sh.cb[gi] + u;
+}
+
+template <int DIM>
+__device__ __forceinline__ void mx_walk(const State& s, const BinScratch& b,
+                                        const MxShared<SPH_OP_FORCE>& sh, int lane,
+                                        const CwTarget& t, Acc32<DIM, SPH_OP_FORCE>& a, int ck,
+                                        int nc) {
+  const unsigned* mrow = b.ck_mask + (size_t)ck * 32 + lane;
+  int gi = t.active ? -1 : nc;
+  unsigned cm = 0u;
+  int qa = -1, qb = -1, ca = 0, cb = 0;
+  for (;;) {
+    // take two hits per step until every lane is done or a lane with hits
+    // left would overflow its FP32 batch; then fold every lane's batch
+    unsigned w;
+    for (;;) {
+      if (qa < 0) qa = mx_next(mrow, sh, nc, gi, cm, ca);
+      if (qb < 0) qb = mx_next(mrow, sh, nc, gi, cm, cb);
+      const bool work = qa >= 0;
+      const bool full = a.nh > 30;
+      w = __reduce_or_sync(0xffffffffu, (work ? 1u : 0u) | ((work && full) ? 2u : 0u));
+      if (w != 1u) break;
+      if (work) {
+        float4 pa, va, pb, vb;
+        ld_rec(s.rec + 2 * qa, pa, va);
+        if (qb >= 0) ld_rec(s.rec + 2 * qb, pb, vb);
+        a.hit(pa, va, sh.offs[ca]);
+        if (qb >= 0) a.hit(pb, vb, sh.offs[cb]);
+        qa = qb = -1;
+      }
+    }
+    if (w == 0u) return;
+    a.fold();
+  }
+}
+
+// list_mode: 0 traverse; 1 traverse and store the hit masks (density
+// passes); 2 read the masks stored by the density pass of this binning.
+template <int DIM, int OP>
+__device__ __forceinline__ void mx_pass(const State& s, const Geometry& g, const Consts& k,
+                                        const BinScratch& b, MxShared<OP>& sh, int lane, int item,
+                                        const CwTarget& t, Acc32<DIM, OP>& a, int list_mode) {
+  // this item's mask slots: the binning counted every cell's chunks
+  int ck = -1, nc = 0;
+  if (list_mode != 0 && b.ck_mask) {
+    const int i0 = __ldg(&b.item_off[t.key]);
+    const int ni = __ldg(&b.item_off[t.key + 1]) - i0;
+    const int co = __ldg(&b.chunk_off[t.key]);
+    nc = ni > 0 ? (__ldg(&b.chunk_off[t.key + 1]) - co) / ni : 0;
+    const long long start = (long long)co + (long long)(item - i0) * nc;
+    if (start + nc <= (long long)b.ck_cap) ck = (int)start;
+  }
+  // slots beyond the counted nc (types changed since the binning) are
+  // neither read nor written
+  const bool read = list_mode == 2 && ck >= 0;
+  const bool store = list_mode == 1 && ck >= 0;
+  if (lane < g.n_diff) {
+    const int nk = t.key + g.key_diff[lane];
+    sh.offs[lane] = (nk >= 1 && nk <= g.key_max) ? cw_offset(g, k, t, nk)
+                                                 : make_float4(0.f, 0.f, 0.f, 0.f);
+  }
+  __syncwarp();
+  if constexpr (OP == SPH_OP_FORCE) {
+    if (read && mx_chunk_table(g, b, sh, lane, t, nc)) {
+      mx_walk<DIM>(s, b, sh, lane, t, a, ck, nc);
+      a.fold();
+      return;
+    }
+  }
+  int gi = 0;  // chunk number in the item's neighbour sequence
+  for (int c = 0; c < g.n_diff; ++c) {
+    const int nk = t.key + g.key_diff[c];
+    if (nk < 1 || nk > g.key_max) continue;  // core.jl:98
+    if (OP == SPH_OP_WALL_PRESSURE && __ldg(&b.cell_fluid[nk]) == 0) continue;
+    const int st = __ldg(&b.cell_start[nk]);
+    const int en = __ldg(&b.cell_start[nk + 1]);
+    const float4 off = sh.offs[c];
+    const float ax = t.pi4.x - off.x, ay = t.pi4.y - off.y, az = t.pi4.z - off.z;
+    for (int base = st; base < en; base += 32) {
+      const int m = min(32, en - base);
+      unsigned mask;
+      if (read && gi < nc) {
+        mask = t.active ? __ldg(&b.ck_mask[((size_t)ck + gi) * 32 + lane]) : 0u;
+        ++gi;
+        if (!__any_sync(0xffffffffu, mask != 0u)) continue;
+        mx_stage<OP>(s, sh, lane, base, m);
+      } else {
+        mx_stage<OP>(s, sh, lane, base, m);
+        unsigned band;
+        mx_classify<DIM, OP>(sh, k, ax, ay, az, mask, band);
+        const int self_u = t.i - base;  // core.jl:105: p == q is skipped
+        if (self_u >= 0 && self_u < 32) {
+          mask &= ~(1u << self_u);
+          band &= ~(1u << self_u);
+        }
+        if (!t.active) mask = band = 0u;
+        if (__any_sync(0xffffffffu, band != 0u)) mx_resolve<DIM>(s, k, t, base, mask, band);
+        if (store && gi < nc) b.ck_mask[((size_t)ck + gi) * 32 + lane] = mask;
+        ++gi;
+      }
+      // keep every lane's FP32 batch at <= 32 hits (one decision per warp)
+      if (__any_sync(0xffffffffu, a.nh + __popc(mask) > 32)) a.fold();
+      while (mask) {
+        const int u = __ffs(mask) - 1;
+        mask &= mask - 1u;
+        float4 vq = make_float4(0.f, 0.f, 0.f, 0.f);
+        if constexpr (MxShared<OP>::kRec) vq = sh.c1[u];
+        a.hit(sh.c0[u], vq, off);
+      }
+    }
+  }
+  a.fold();
+}
 
 template <int DIM, int OP, int WARPS>
 __global__ void __launch_bounds__(32 * WARPS) pair32_kernel(State s, Geometry g, Consts k,
                                                             BinScratch b, int self, int reset,
                                                             int fuse_eos, int list_mode) {
-  __shared__ CwShared shared[WARPS];
+  __shared__ MxShared<OP> shared[WARPS];
   const int lane = threadIdx.x & 31;
   const int w = threadIdx.x >> 5;
   const int item = blockIdx.x * WARPS + w;
@@ -199,9 +441,8 @@ __global__ void __launch_bounds__(32 * WARPS) pair32_kernel(State s, Geometry g,
   t.xp[0] = valid ? s.x[0][i] : 0.0;
   t.xp[1] = valid ? s.x[1][i] : 0.0;
   t.xp[2] = (DIM == 3 && valid) ? s.x[2][i] : 0.0;
-  Proc32<DIM, OP> p(s, k);
+  Acc32<DIM, OP> p(k);
   p.pi4 = t.pi4;
-  p.offs = shared[w].offs;
   if (t.active) {
     if (OP == SPH_OP_DENSITY) {
       if (!reset) p.acc = s.rho[i];
@@ -213,12 +454,13 @@ __global__ void __launch_bounds__(32 * WARPS) pair32_kernel(State s, Geometry g,
         p.sx = s.xs[0][i]; p.sy = s.xs[1][i];
         if (DIM == 3) { p.az = s.a[2][i]; p.sz = s.xs[2][i]; }
       }
-      p.vp = s.vr[i];
-      p.rhop = s.rhof[i];
+      float4 r0;
+      ld_rec(s.rec + 2 * i, r0, p.vp);
+      p.rhop = fabsf(r0.w);
     }
   }
-  cw_pass<DIM, OP>(s, g, k, b, shared[w], lane, item, t, p, list_mode);
-
+  if (__any_sync(0xffffffffu, t.active))
+    mx_pass<DIM, OP>(s, g, k, b, shared[w], lane, item, t, p, list_mode);
   if (valid && !t.active) {
     if (reset) {
       if (OP == SPH_OP_DENSITY) {
@@ -247,9 +489,8 @@ __global__ void __launch_bounds__(32 * WARPS) pair32_kernel(State s, Geometry g,
           s.P[i] = P;
           s.Pr[i] = Pr;
         }
-        s.vr[i] = make_float4((float)s.v[0][i], (float)s.v[1][i],
-                              DIM == 3 ? (float)s.v[2][i] : 0.f, (float)Pr);
-        s.rhof[i] = (float)acc;
+        put_rec(s, i, t.pi4, true, (float)acc, (float)s.v[0][i], (float)s.v[1][i],
+                DIM == 3 ? (float)s.v[2][i] : 0.f, (float)Pr);
       } else {
         s.rho_ref[i] = acc;
       }
@@ -259,9 +500,8 @@ __global__ void __launch_bounds__(32 * WARPS) pair32_kernel(State s, Geometry g,
       s.P[i] = P;
       s.Pr[i] = Pr;
       s.rho[i] = k.rho0;
-      s.vr[i] = make_float4((float)s.v[0][i], (float)s.v[1][i], DIM == 3 ? (float)s.v[2][i] : 0.f,
-                            (float)Pr);
-      s.rhof[i] = (float)k.rho0;
+      put_rec(s, i, t.pi4, false, (float)k.rho0, (float)s.v[0][i], (float)s.v[1][i],
+              DIM == 3 ? (float)s.v[2][i] : 0.f, (float)Pr);
     } else {
       // the self term of the force adds exact zeros
       s.a[0][i] = p.ax;
