@@ -174,12 +174,11 @@ struct Acc32 {
       float vdx = dvx * hx + dvy * hy;
       if (DIM == 3) vdx += dvz * hz;
       const float inv_rb = __fdividef(2.f, rhop + rq);
-      float pi = 0.f;
-      if (vdx < 0.f) {
-        const float mu = __fdividef(k.h_smoothf * vdx, ss + k.eta2f);
-        pi = (-k.alpha_c0f * mu) * inv_rb;
-        ++c2;
-      }
+      // Monaghan viscosity only for approaching pairs (v.x < 0); evaluated
+      // without a branch: mu = 0 otherwise
+      const float mu = __fdividef(k.h_smoothf * fminf(vdx, 0.f), ss + k.eta2f);
+      const float pi = (-k.alpha_c0f * mu) * inv_rb;
+      c2 += vdx < 0.f ? 1 : 0;
       const float cf = -ker * ((vp.w + vq.w) + pi);
       f0 += cf * hx;
       f1 += cf * hy;
@@ -293,17 +292,24 @@ __device__ __forceinline__ bool mx_chunk_table(const Geometry& g, const BinScrat
 // chunk, bit by bit: the traversal order) and loads each neighbour's record
 // directly, so lanes never wait for one another within a chunk.  Two hits per
 // step keep two record loads in flight.
+struct MxCursor {
+  int gi;       // current chunk
+  unsigned cm;  // its bits not yet taken
+  unsigned nm;  // mask of chunk gi + 1 (loaded ahead)
+};
+
 __device__ __forceinline__ int mx_next(const unsigned* mrow, const MxShared<SPH_OP_FORCE>& sh,
-                                       int nc, int& gi, unsigned& cm, int& cell) {
-  while (cm == 0u && gi + 1 < nc) {
-    ++gi;
-    cm = __ldg(mrow + (size_t)gi * 32);
+                                       int nc, MxCursor& c, int& cell) {
+  while (c.cm == 0u && c.gi + 1 < nc) {
+    ++c.gi;
+    c.cm = c.nm;
+    if (c.gi + 1 < nc) c.nm = __ldg(mrow + (size_t)(c.gi + 1) * 32);
   }
-  if (cm == 0u) return -1;
-  const int u = __ffs(cm) - 1;
-  cm &= cm - 1u;
-  cell = sh.cc[gi];
-  return sh.cb[gi] + u;
+  if (c.cm == 0u) return -1;
+  const int u = __ffs(c.cm) - 1;
+  c.cm &= c.cm - 1u;
+  cell = sh.cc[c.gi];
+  return sh.cb[c.gi] + u;
 }
 
 template <int DIM>
@@ -312,16 +318,18 @@ __device__ __forceinline__ void mx_walk(const State& s, const BinScratch& b,
                                         const CwTarget& t, Acc32<DIM, SPH_OP_FORCE>& a, int ck,
                                         int nc) {
   const unsigned* mrow = b.ck_mask + (size_t)ck * 32 + lane;
-  int gi = t.active ? -1 : nc;
-  unsigned cm = 0u;
+  MxCursor cur;
+  cur.gi = t.active ? -1 : nc;
+  cur.cm = 0u;
+  cur.nm = t.active && nc > 0 ? __ldg(mrow) : 0u;
   int qa = -1, qb = -1, ca = 0, cb = 0;
   for (;;) {
     // take two hits per step until every lane is done or a lane with hits
     // left would overflow its FP32 batch; then fold every lane's batch
     unsigned w;
     for (;;) {
-      if (qa < 0) qa = mx_next(mrow, sh, nc, gi, cm, ca);
-      if (qb < 0) qb = mx_next(mrow, sh, nc, gi, cm, cb);
+      if (qa < 0) qa = mx_next(mrow, sh, nc, cur, ca);
+      if (qb < 0) qb = mx_next(mrow, sh, nc, cur, cb);
       const bool work = qa >= 0;
       const bool full = a.nh > 30;
       w = __reduce_or_sync(0xffffffffu, (work ? 1u : 0u) | ((work && full) ? 2u : 0u));
