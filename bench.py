@@ -62,7 +62,7 @@ def parse():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     # batched ensemble of 2D dam breaks (mixed precision, one CUDA graph)
     ap.add_argument("--ens-members", type=int, default=256)
-    ap.add_argument("--ens-steps", type=int, default=20)
+    ap.add_argument("--ens-steps", type=int, default=1000)
     ap.add_argument("--ens-seed", type=int, default=2024)
     # served stream of solve requests (continuous batching, HBM budget)
     ap.add_argument("--serve-requests", type=int, default=24)
@@ -262,6 +262,56 @@ def kernel_table(kst, cats):
     return rows
 
 
+def hbm_peak_gbs():
+    """The measured copy bandwidth of the GB300s (driver-written)."""
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            return float(json.load(f)["hbm_gbs"]), "measured (MEASURED_PEAKS.json hbm_gbs)"
+    except (OSError, KeyError, ValueError):
+        return 6800.0, "fallback 6.8 TB/s"
+
+
+def binning_roofline(kst, case, mixed: bool):
+    """Algorithmic HBM bytes of the step-mode binning kernels over their
+    CUDA-event times.  Per particle (d = dimension, fluid moves, walls do not):
+      bin_keys    fluid: read x, v, a, xsph (32 d) + type 4, write x, v (16 d)
+                  + key 4 + slot 4; wall: read x (8 d) + type 4, write key + slot 8
+      bin_scatter read key, slot, rid 12, write 2 indices 8
+      bin_rank    read 2 indices 8, write 2 indices 8
+      bin_gather  read perm, key, rid 12 + x, v (16 d) + type 4 + rho_ref 8 + oid 8;
+                  write x, v (16 d) + rho_ref 8 + type 4 + oid 8 + rid 4 + key 4
+                  + cell-relative position 16 + inverse index 4 (+ 16 mixed record)
+    Cell tables (scans, item list) are excluded: 4-12 B per cell."""
+    d, n, nf = case.dim, case.n, case.n_fluid
+    nw = n - nf
+    by = {
+        "bin_keys": nf * (32 * d + 4 + 16 * d + 8) + nw * (8 * d + 4 + 8),
+        "bin_scatter": n * 20,
+        "bin_rank": n * 16,
+        "bin_gather": n * (12 + 16 * d + 20 + 16 * d + 48 + (16 if mixed else 0)),
+    }
+    peak, src = hbm_peak_gbs()
+    out = {"peak_gbs": peak, "peak_source": src}
+    tb, tt = 0, 0.0
+    for k, b in by.items():
+        if k not in kst:
+            continue
+        ms = kst[k]["ms_avg"]
+        gbs = b / (ms * 1e-3) / 1e9
+        out[k] = {"bytes_per_launch": b, "ms_avg": ms, "achieved_gbs": round(gbs, 1),
+                  "frac": round(gbs / peak, 3)}
+        tb += b
+        tt += ms
+    if tt > 0:
+        all_ms = sum(kst[k]["ms_avg"] * kst[k]["launches"] for k in kst if k.startswith("bin_"))
+        steps = max(kst["bin_keys"]["launches"], 1)
+        out["particle_kernels"] = {"bytes_per_step": tb, "ms": round(tt, 4),
+                                   "achieved_gbs": round(tb / (tt * 1e-3) / 1e9, 1),
+                                   "frac": round(tb / (tt * 1e-3) / 1e9 / peak, 3)}
+        out["binning_ms_per_step"] = round(all_ms / steps, 4)
+    return out
+
+
 def field_errors(ref, got):
     """Per-field error of `got` against `ref` (dicts of reference-ordered arrays)."""
     out = {}
@@ -284,7 +334,7 @@ def run_ensemble(args, torch, dev):
     together in mixed precision, two steps per CUDA-graph launch."""
     import sphgpu
     from sphgpu import autotune
-    from sphgpu.ensemble import ensemble_cases
+    from sphgpu.ensemble import count_quantiles, ensemble_cases
     t0 = time.perf_counter()
     cases = ensemble_cases(args.ens_members, seed=args.ens_seed)
     t_geo = time.perf_counter() - t0
@@ -330,10 +380,9 @@ def run_ensemble(args, torch, dev):
     for g in mem:
         g.close()
     return {
-        "workload": (f"{len(cases)} independent 2D dam breaks (seeded): fluid count U[2k, 60k] "
-                     "via dr in [0.004, 0.02], column height U[1, 2], alpha U[0.01, 0.1]; mixed "
-                     "precision"),
-        "particles_total": int(sum(n)), "particles_min": int(min(n)), "particles_max": int(max(n)),
+        "workload": (f"{len(cases)} independent 2D dam breaks (seed {args.ens_seed}): dr U[0.004, "
+                     "0.02], column height U[1, 2], alpha U[0.01, 0.1]; mixed precision"),
+        "particles_total": int(sum(n)), "particles_per_member": count_quantiles(n),
         "steps_timed": S, "ms_per_step": ms / S,
         "value": pairs / (ms * 1e-3), "unit": UNIT,
         "member_steps_per_s": len(cases) * S / (ms * 1e-3),
@@ -346,7 +395,7 @@ def run_ensemble(args, torch, dev):
                               "ms_per_step": {str(w): round(t, 4) for w, t in v[1].items()}}
                      for k, v in sorted(table.items())},
         "autotune_s": t_tune, "setup_lattices_s": t_geo, "clocks": clk.summary(),
-        "l2": "no flush: 1.5 GB resident state > 129 MB L2",
+        "l2": "no flush: resident state of all members > 129 MB L2",
     }
 
 
@@ -454,6 +503,7 @@ def run_ours(args):
              "dtype": "fp32 pair arithmetic, fp64 positions/integration/accumulators",
              "error_vs_fp64_after_steps": field_errors(final64, final_mx),
              "kernels": kernel_table(rmx["kernels"], rmx["cats"]),
+             "binning_hbm": None,
              "gpu_launches": rmx["launches"], "clocks": rmx["clocks"]}
     # one step from an identical FP64 state (reference density included): the
     # per-step error of the mixed arithmetic
@@ -474,6 +524,7 @@ def run_ours(args):
 
     # ---- roofline of the dominant kernel of the FP64 step (the force pass)
     kt = kernel_table(r64["kernels"], r64["cats"])
+    mixed["binning_hbm"] = binning_roofline(mixed["kernels"], case, True)
     dom = max((k for k in kt if "tflops" in kt[k]), key=lambda k: kt[k]["ms_total"])
     dfma = sphgpu.pipe_peak("dfma", dev)
     ffma = sphgpu.pipe_peak("ffma", dev)
@@ -509,6 +560,7 @@ def run_ours(args):
                        "replicas": world},
             "steps_per_s": 1e3 * args.steps / ms_max,
             "roofline": roofline, "kernels": kt, "mixed": mixed,
+            "binning_hbm": binning_roofline(kt, case, False),
             "ensemble": ensemble, "served": served,
             "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": r64["launches"],
             "clocks": r64["clocks"],
@@ -520,9 +572,10 @@ def run_ours(args):
 
 
 # DRAM bytes (read + write) per launch of the FP64 force kernel from the ncu
-# capture summarised in profiles/pair64_force_3d_dr0.02.md (28,297,984 B for
-# 517,040 particles), scaled by particle count to the 5,746,633-particle case.
-NCU_TRAFFIC: dict = {"force": int(28297984 * 5746633 / 517040)}
+# capture summarised in profiles/pair64_force_3d_dr0.0125.md (1,217,046,016 +
+# 700,111,360 B for the 1,699,240-particle dam break at dr = 0.0125), scaled by
+# particle count to the 5,746,633-particle case.
+NCU_TRAFFIC: dict = {"force": int((1217046016 + 700111360) * 5746633 / 1699240)}
 
 
 def main():

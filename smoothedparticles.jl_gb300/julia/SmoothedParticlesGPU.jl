@@ -17,7 +17,8 @@ import SmoothedParticles: create_cell_list!, apply!, apply_unary!, apply_binary!
 
 export GPUParticleSystem, DensitySum, ReferenceDensitySum, InternalForce, WallPressure,
        FindPressure, ResetRho, ResetRho0, ResetA, Accelerate, Move, Hydrostatic,
-       upload!, download, step!, init_state!
+       upload!, download, step!, init_state!, set_tuning!, memory_estimate, memory_usage,
+       isidle, GPUBatch
 
 const libsphgpu = get(ENV, "SPHGPU_LIB", joinpath(@__DIR__, "..", "libsphgpu.so"))
 
@@ -148,5 +149,59 @@ step!(sys::GPUParticleSystem, nsteps::Integer = 1) =
 
 init_state!(sys::GPUParticleSystem) =
     check(sys, ccall((:sph_init_state, libsphgpu), Cint, (Ptr{Cvoid},), sys.handle))
+
+"Warps per block of the pair passes (2, 4 or 8); results do not depend on it."
+set_tuning!(sys::GPUParticleSystem, warps::Integer) =
+    check(sys, ccall((:sph_set_tuning, libsphgpu), Cint, (Ptr{Cvoid}, Cint), sys.handle, warps))
+
+"Device bytes a system with parameters p holds with n particles (no GPU call)."
+function memory_estimate(p::SphParams, n::Integer)
+    b = Ref{UInt64}(0)
+    rc = ccall((:sph_memory_estimate, libsphgpu), Cint, (Ref{SphParams}, Int64, Ref{UInt64}),
+               p, n, b)
+    rc == 0 || error("sph_memory_estimate failed ($rc)")
+    return Int(b[])
+end
+
+function memory_usage(sys::GPUParticleSystem)
+    b = Ref{UInt64}(0)
+    check(sys, ccall((:sph_memory_usage, libsphgpu), Cint, (Ptr{Cvoid}, Ref{UInt64}),
+                     sys.handle, b))
+    return Int(b[])
+end
+
+"True when all work queued on the system's stream has finished (never waits)."
+function isidle(sys::GPUParticleSystem)
+    i = Ref{Cint}(0)
+    check(sys, ccall((:sph_query, libsphgpu), Cint, (Ptr{Cvoid}, Ref{Cint}), sys.handle, i))
+    return i[] == 1
+end
+
+"""
+Many independent systems stepped together: every pair of steps is one CUDA-graph
+launch in which each member is an independent branch.  Members must outlive the
+batch; their results equal stepping each alone.
+"""
+mutable struct GPUBatch
+    handle::Ptr{Cvoid}
+    members::Vector{GPUParticleSystem}
+    function GPUBatch(members::Vector{GPUParticleSystem})
+        hs = [m.handle for m in members]
+        h = Ref{Ptr{Cvoid}}(C_NULL)
+        rc = ccall((:sph_batch_create, libsphgpu), Cint, (Ptr{Ptr{Cvoid}}, Cint, Ref{Ptr{Cvoid}}),
+                   hs, length(hs), h)
+        rc == 0 || error("sph_batch_create failed ($rc)")
+        b = new(h[], members)
+        finalizer(x -> ccall((:sph_batch_destroy, libsphgpu), Cint, (Ptr{Cvoid},), x.handle), b)
+        return b
+    end
+end
+
+function step!(b::GPUBatch, nsteps::Integer = 2)
+    rc = ccall((:sph_batch_step, libsphgpu), Cint, (Ptr{Cvoid}, Cint), b.handle, nsteps)
+    rc == 0 || error(unsafe_string(ccall((:sph_batch_last_error, libsphgpu), Cstring,
+                                         (Ptr{Cvoid},), b.handle)))
+    return nothing
+end
 
 end # module

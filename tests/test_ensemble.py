@@ -16,6 +16,9 @@ def test_specs_reproducible_and_in_range():
         assert 0.01 <= al <= 0.1
     counts = [hc / (dr * dr) for dr, hc, al in a]
     assert min(counts) < 5000 and max(counts) > 40000
+    from sphgpu.ensemble import count_quantiles
+    q = count_quantiles(counts)
+    assert q["min"] <= q["p25"] <= q["p50"] <= q["p75"] <= q["max"]
 
 
 def test_size_classes():
