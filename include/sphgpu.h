@@ -207,6 +207,33 @@ int sph_launch_count(sph_system* sys, int64_t* launches);
 int sph_set_tuning(sph_system* sys, int warps_per_block);
 int sph_get_tuning(const sph_system* sys, int* warps_per_block);
 
+/* ---- device-side particle generation: covering(grid, shape) of
+ * src/grids.jl:52-66 / :128-144 (square / cubic grid, points i*dr in the
+ * reference's loop order, i outer) for a Box / Rectangle (src/geometry.jl:15-43)
+ * or a BoundaryLayer (src/geometry.jl:198-234) with an optional Specification
+ * x[keep_axis] < keep_max (src/geometry.jl:179-196).  2D shapes have
+ * lo[2] = hi[2] = 0. */
+#define SPH_SHAPE_BOX 1
+#define SPH_SHAPE_LAYER 2
+typedef struct sph_shape {
+  int32_t kind;        /* SPH_SHAPE_BOX or SPH_SHAPE_LAYER                      */
+  int32_t type;        /* SPH_FLUID / SPH_WALL of the generated particles       */
+  double dr;           /* grid spacing                                           */
+  double lo[3], hi[3]; /* the box (BOX: the filled shape; LAYER: the enclosed box) */
+  double width;        /* LAYER: width of the layer                              */
+  int32_t keep_axis;   /* LAYER: keep points with x[keep_axis] < keep_max; -1: all */
+  int32_t reserved;
+  double keep_max;
+} sph_shape;
+/* Replaces the particle set by the particles of shapes[0..count) in order (as
+ * generate_particles! once per shape, src/grids.jl:253-258), generated on the
+ * device: v = 0, rho = rho_ref = 0.  Same result as sph_upload of the same
+ * points; *n_out = the particle count. */
+int sph_generate(sph_system* sys, const sph_shape* shapes, int count, int64_t* n_out);
+/* The particle count sph_generate would produce for a system of dimension dim,
+ * computed on `device` without a system (for admission before allocation). */
+int sph_shape_count(int device, int dim, const sph_shape* shapes, int count, int64_t* n_out);
+
 /* ---- device memory accounting for admission by an HBM budget (no
  * reference counterpart).  sph_memory_estimate: the device bytes a system
  * with these parameters holds once it stores n particles (cell tables plus the

@@ -1,7 +1,9 @@
 // sph_api.cu -- the C ABI (include/sphgpu.h): handle, device memory, stream,
 // argument checking and the order of kernel launches for each call.
+#include <algorithm>
 #include <cmath>
 #include <cstdarg>
+#include <cstdint>
 #include <cstdio>
 #include <cstring>
 #include <string>
@@ -548,6 +550,133 @@ int sph_upload(sph_system* s, int64_t n, const double* x, const double* v, const
   s->cells_valid = false;
   s->aux_fluid = s->aux_wall = false;
   s->lists_valid = false;
+  return SPH_OK;
+}
+
+// Counts (and, when `write`, generates into x / type at the running offset)
+// the particles of every shape on `stream`; temporaries are allocated here.
+static int shapes_run(int dim, const sph_shape* shapes, int count, cudaStream_t stream,
+                      const LaunchCtx* c, double* x, int* type, long long* total_out,
+                      std::string* err) {
+  std::vector<LatticeShape> ls(count);
+  std::vector<std::vector<double>> offs(count);
+  long long maxp = 0, maxo = 0;
+  for (int i = 0; i < count; ++i) {
+    if (lattice_prepare(shapes[i], dim, ls[i], offs[i]) != SPH_OK) {
+      if (err) *err = "invalid shape " + std::to_string(i);
+      return SPH_ERR_ARG;
+    }
+    const long long np = lattice_points(ls[i]);
+    if (np > 0x7fffffffLL - 4096) {
+      if (err) *err = "shape " + std::to_string(i) + ": bounding box holds more than 2^31 points";
+      return SPH_ERR_ARG;
+    }
+    maxp = std::max(maxp, np);
+    maxo = std::max(maxo, (long long)offs[i].size());
+  }
+  const size_t scan_ints = scan_tmp_ints((int)(maxp + 1)) + 64;
+  const size_t bytes = 8 * (size_t)(maxp + 1) + 4 * scan_ints + 8 * (size_t)(maxo + 3) + 1024;
+  void* tmp = nullptr;
+  if (cudaMalloc(&tmp, bytes) != cudaSuccess) {
+    cudaGetLastError();
+    if (err) *err = "cannot allocate the generation scratch";
+    return SPH_ERR_NOMEM;
+  }
+  char* p = (char*)tmp;
+  int* flags = (int*)p;
+  int* pos = flags + (maxp + 1);
+  int* stmp = pos + (maxp + 1);
+  double* doffs = (double*)(((uintptr_t)(stmp + scan_ints) + 255) & ~(uintptr_t)255);
+  LaunchCtx lc = c ? *c : LaunchCtx{stream, nullptr, nullptr};
+  long long total = 0;
+  int rc = SPH_OK;
+  for (int i = 0; i < count && rc == SPH_OK; ++i) {
+    const long long np = lattice_points(ls[i]);
+    if (!offs[i].empty() &&
+        cudaMemcpyAsync(doffs, offs[i].data(), 8 * offs[i].size(), cudaMemcpyHostToDevice,
+                        stream) != cudaSuccess) {
+      rc = SPH_ERR_CUDA;
+      break;
+    }
+    // flags[np] = 0 so that pos[np] is the shape's count
+    if (cudaMemsetAsync(flags + np, 0, sizeof(int), stream) != cudaSuccess ||
+        launch_lattice_flags(lc, ls[i], doffs, flags) != cudaSuccess ||
+        launch_scan(lc, flags, pos, (int)(np + 1), stmp) != cudaSuccess) {
+      rc = SPH_ERR_CUDA;
+      break;
+    }
+    int cnt = 0;
+    if (cudaMemcpyAsync(&cnt, pos + np, sizeof(int), cudaMemcpyDeviceToHost, stream) !=
+            cudaSuccess ||
+        cudaStreamSynchronize(stream) != cudaSuccess) {
+      rc = SPH_ERR_CUDA;
+      break;
+    }
+    if (x && launch_lattice_write(lc, ls[i], flags, pos, x, type, (int)total) != cudaSuccess) {
+      rc = SPH_ERR_CUDA;
+      break;
+    }
+    total += cnt;
+  }
+  if (rc == SPH_OK && cudaStreamSynchronize(stream) != cudaSuccess) rc = SPH_ERR_CUDA;
+  if (rc != SPH_OK) {
+    cudaGetLastError();
+    if (err) *err = "particle generation failed";
+  }
+  cudaFree(tmp);
+  *total_out = total;
+  return rc;
+}
+
+int sph_shape_count(int device, int dim, const sph_shape* shapes, int count, int64_t* n_out) {
+  if (!n_out || count < 0 || (count > 0 && !shapes) || (dim != 2 && dim != 3)) return SPH_ERR_ARG;
+  int ndev = 0;
+  if (cudaGetDeviceCount(&ndev) != cudaSuccess || device < 0 || device >= ndev) {
+    cudaGetLastError();
+    return SPH_ERR_CUDA;
+  }
+  DeviceGuard guard(device);
+  cudaStream_t st = nullptr;
+  if (cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking) != cudaSuccess) {
+    cudaGetLastError();
+    return SPH_ERR_CUDA;
+  }
+  long long total = 0;
+  const int rc = shapes_run(dim, shapes, count, st, nullptr, nullptr, nullptr, &total, nullptr);
+  cudaStreamDestroy(st);
+  if (rc == SPH_OK) *n_out = total;
+  return rc;
+}
+
+int sph_generate(sph_system* s, const sph_shape* shapes, int count, int64_t* n_out) {
+  if (!s || count < 0 || (count > 0 && !shapes)) return SPH_ERR_ARG;
+  DeviceGuard guard(s->device);
+  long long total = 0;
+  std::string err;
+  int rc = shapes_run(s->params.dim, shapes, count, s->stream, nullptr, nullptr, nullptr, &total,
+                      &err);
+  if (rc) return fail(s, rc, "%s", err.c_str());
+  // the pair passes pack a particle index into 27 bits of a list entry
+  if (total >= (1LL << 27))
+    return fail(s, SPH_ERR_ARG, "%lld particles exceed the limit 2^27 - 1", total);
+  rc = ensure_capacity(s, (int)total);
+  if (rc) return rc;
+  const size_t N = (size_t)total;
+  double* dx = (double*)s->staging;
+  int* dtype = (int*)((char*)s->staging + 64 * N);
+  long long again = 0;
+  const LaunchCtx c = ctx(s);
+  rc = shapes_run(s->params.dim, shapes, count, s->stream, &c, dx, dtype, &again, &err);
+  if (rc) return fail(s, rc, "%s", err.c_str());
+  cudaError_t e = launch_upload(ctx(s), s->cur, s->k, s->b, (int)total, dx, nullptr, nullptr,
+                                nullptr, dtype);
+  if (e != cudaSuccess) return fail(s, SPH_ERR_CUDA, "generate: %s", cudaGetErrorString(e));
+  CK(cudaStreamSynchronize(s->stream));
+  s->n_host = (int)total;
+  s->cells_valid = false;
+  s->aux_fluid = s->aux_wall = false;
+  s->lists_valid = false;
+  if (n_out) *n_out = total;
   return SPH_OK;
 }
 

@@ -2,7 +2,10 @@
 // family); the C ABI in sph_api.cu strings them together.
 #pragma once
 
+#include <vector>
+
 #include "sph_common.cuh"
+#include "sphgpu.h"
 
 namespace sphgpu {
 
@@ -63,6 +66,24 @@ cudaError_t launch_debug_pairs(const LaunchCtx& c, const State& s, const Geometr
                                const Consts& k, const BinScratch& b, int cap, int pass,
                                int* counts, const long long* offsets, long long* pairs,
                                long long cap_pairs);
+
+// ---- device-side particle generation (sph_lattice.cu)
+struct LatticeShape {
+  int kind, type, dim, keep_axis;
+  double dr, lo[3], hi[3], keep_max;
+  long long i0[3], n[3];  // first lattice index and count per axis (n[2] = 1 in 2D)
+  int n_off;              // ball offsets of a boundary layer
+};
+// Validates a shape and fills the kernels' description plus the layer's ball
+// offsets (x, y, z triples), computed on the host.
+int lattice_prepare(const sph_shape& in, int dim, LatticeShape& out, std::vector<double>& offs);
+long long lattice_points(const LatticeShape& s);
+// flags[idx] = 1 for the lattice points of the shape (idx in loop order)
+cudaError_t launch_lattice_flags(const LaunchCtx& c, const LatticeShape& s, const double* offs,
+                                 int* flags);
+// point idx with flags[idx] goes to row base + pos[idx] of x (n x 3) and type
+cudaError_t launch_lattice_write(const LaunchCtx& c, const LatticeShape& s, const int* flags,
+                                 const int* pos, double* x, int* type, int base);
 
 // ---- unary operators and field transfer (sph_unary.cu)
 cudaError_t launch_unary(const LaunchCtx& c, const State& s, const Consts& k,

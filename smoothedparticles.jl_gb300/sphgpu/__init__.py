@@ -25,7 +25,7 @@ __all__ = ["ParticleSystem", "ParticleField", "create_cell_list", "apply", "appl
            "FP64", "MIXED", "find_rho", "find_rho0", "internal_force", "find_pressure",
            "reset_rho", "reset_rho0", "reset_a", "accelerate", "move", "hydrostatic",
            "DENSITY", "KERNEL", "PRESSURE", "SHEPARD", "wall_pressure", "Batch", "pipe_peak",
-           "memory_estimate"]
+           "memory_estimate", "shape_count"]
 
 
 class SphError(RuntimeError):
@@ -142,6 +142,15 @@ class ParticleSystem:
         self._keep = (x, v, rho, rr, t)
         self._check(self._lib.sph_upload(self._h, n, _ptr(x), _ptr(v), _ptr(rho), _ptr(rr), _ptr(t)))
         self._keep = None
+
+    def generate(self, shapes) -> int:
+        """generate_particles! on the device (grids.jl:253-258): replaces the
+        particle set by the lattice points of ``shapes`` (dicts as produced by
+        ``geometry.dam_break_shapes``), in order; returns the particle count."""
+        arr = L.make_shapes(shapes)
+        n = C.c_int64()
+        self._check(self._lib.sph_generate(self._h, arr, len(shapes), C.byref(n)))
+        return n.value
 
     @property
     def n(self) -> int:
@@ -329,6 +338,17 @@ class Batch:
             self.close()
         except Exception:
             pass
+
+
+def shape_count(dim: int, shapes, device: int = 0) -> int:
+    """Particles the device generator makes from ``shapes`` (no system needed)."""
+    lib = L.load()
+    arr = L.make_shapes(shapes)
+    n = C.c_int64()
+    rc = lib.sph_shape_count(int(device), int(dim), arr, len(shapes), C.byref(n))
+    if rc != 0:
+        raise SphError(rc, "sph_shape_count failed (invalid shape or no CUDA device)")
+    return n.value
 
 
 def memory_estimate(params: dict, n: int, precision: int = FP64) -> int:

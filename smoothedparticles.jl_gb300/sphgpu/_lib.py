@@ -83,6 +83,42 @@ class sph_params(C.Structure):
     ]
 
 
+SPH_SHAPE_BOX = 1
+SPH_SHAPE_LAYER = 2
+
+
+class sph_shape(C.Structure):
+    _fields_ = [
+        ("kind", C.c_int32),
+        ("type", C.c_int32),
+        ("dr", C.c_double),
+        ("lo", C.c_double * 3),
+        ("hi", C.c_double * 3),
+        ("width", C.c_double),
+        ("keep_axis", C.c_int32),
+        ("reserved", C.c_int32),
+        ("keep_max", C.c_double),
+    ]
+
+
+def make_shapes(shapes) -> "C.Array":
+    """An array of sph_shape from dicts (kind 'box' or 'layer')."""
+    arr = (sph_shape * max(1, len(shapes)))()
+    for i, d in enumerate(shapes):
+        s = arr[i]
+        s.kind = SPH_SHAPE_BOX if d["kind"] == "box" else SPH_SHAPE_LAYER
+        s.type = int(d["type"])
+        s.dr = float(d["dr"])
+        for k in range(3):
+            s.lo[k] = float(d["lo"][k])
+            s.hi[k] = float(d["hi"][k])
+        s.width = float(d.get("width", 0.0))
+        s.keep_axis = int(d.get("keep_axis", -1))
+        s.reserved = 0
+        s.keep_max = float(d.get("keep_max", 0.0))
+    return arr
+
+
 def make_params(cls, p: dict, precision: int = 0):
     """Fills a params structure (``sph_params`` or the oracle's twin) from a dict."""
     s = cls()
@@ -147,6 +183,9 @@ PROTOTYPES = {
     "sph_memory_estimate": (C.c_int, [C.POINTER(sph_params), _I64, C.POINTER(C.c_uint64)]),
     "sph_memory_usage": (C.c_int, [_P, C.POINTER(C.c_uint64)]),
     "sph_query": (C.c_int, [_P, C.POINTER(C.c_int)]),
+    "sph_generate": (C.c_int, [_P, C.POINTER(sph_shape), C.c_int, C.POINTER(_I64)]),
+    "sph_shape_count": (C.c_int, [C.c_int, C.c_int, C.POINTER(sph_shape), C.c_int,
+                                  C.POINTER(_I64)]),
 }
 
 _lib = None

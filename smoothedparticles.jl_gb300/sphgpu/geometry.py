@@ -171,6 +171,46 @@ class Case:
         return int((self.type == FLUID).sum())
 
 
+@dataclass
+class Shapes:
+    """The shapes of a case as the device generator takes them (no particles)."""
+    name: str
+    dim: int
+    dr: float
+    shapes: list             # dicts: kind, type, dr, lo, hi, width, keep_axis, keep_max
+    params: dict = field(default_factory=dict)
+
+
+def _dam_break_setup(dim, dr, col_width, col_height, box_width, box_height, depth, h_factor,
+                     wall_layers, lid, alpha, eps_xsph, g, rho0):
+    if h_factor is None:
+        h_factor = 2.4 if dim == 2 else 2.0
+    width = wall_layers * dr
+    if dim == 2:
+        fluid_shape = rectangle(0.0, 0.0, col_width, col_height)
+        box = rectangle(0.0, 0.0, box_width, box_height)
+        vaxis = 1
+    else:
+        fluid_shape = box3(0.0, 0.0, 0.0, col_width, depth, col_height)
+        box = box3(0.0, 0.0, 0.0, box_width, depth, box_height)
+        vaxis = 2
+    h = h_factor * dr
+    H = 2.0 * h
+    dmin = [box.lo[d] - width for d in range(3)]
+    dmax = [box.hi[d] + width for d in range(3)]
+    if dim == 2:
+        dmin[2] = dmax[2] = 0.0
+    c0 = 10.0 * math.sqrt((2.0 * g) * col_height)
+    gravity = [0.0, 0.0, 0.0]
+    gravity[vaxis] = -g
+    mass = rho0 * (dr * dr) if dim == 2 else rho0 * ((dr * dr) * dr)
+    params = dict(dim=dim, h=H, domain_min=dmin, domain_max=dmax, mass=mass, rho0=rho0,
+                  c0=c0, h_smooth=h, alpha=alpha, eps_xsph=eps_xsph, gravity=gravity,
+                  dt=(0.1 * h) / c0, col_height=col_height,
+                  vertical_axis=vaxis)
+    return fluid_shape, box, width, vaxis, params
+
+
 def dam_break(dim: int, dr: float, *, col_width: float = 1.0, col_height: float = 2.0,
               box_width: float = 4.0, box_height: float = 3.0, depth: float = 1.0,
               h_factor: float | None = None, wall_layers: int = 3, lid: bool = False,
@@ -187,38 +227,33 @@ def dam_break(dim: int, dr: float, *, col_width: float = 1.0, col_height: float 
     The domain is ``box + walls``, whose bounding box is the box grown by the
     wall width (collapse_dry.jl:94).
     """
-    if h_factor is None:
-        h_factor = 2.4 if dim == 2 else 2.0
-    width = wall_layers * dr
-    if dim == 2:
-        fluid_shape = rectangle(0.0, 0.0, col_width, col_height)
-        box = rectangle(0.0, 0.0, box_width, box_height)
-        vaxis = 1
-    else:
-        fluid_shape = box3(0.0, 0.0, 0.0, col_width, depth, col_height)
-        box = box3(0.0, 0.0, 0.0, box_width, depth, box_height)
-        vaxis = 2
+    fluid_shape, box, width, vaxis, params = _dam_break_setup(
+        dim, dr, col_width, col_height, box_width, box_height, depth, h_factor, wall_layers,
+        lid, alpha, eps_xsph, g, rho0)
     xf = fill_box(dim, dr, fluid_shape)
     keep = None if lid else (lambda x, a=vaxis, top=box_height: x[:, a] < top)
     xw = boundary_layer(dim, dr, box, width, keep)
     x = np.concatenate([xf, xw])
     typ = np.concatenate([np.full(xf.shape[0], FLUID, np.int32), np.full(xw.shape[0], WALL, np.int32)])
-    h = h_factor * dr
-    H = 2.0 * h
-    dmin = [box.lo[d] - width for d in range(3)]
-    dmax = [box.hi[d] + width for d in range(3)]
-    if dim == 2:
-        dmin[2] = dmax[2] = 0.0
-    c0 = 10.0 * math.sqrt((2.0 * g) * col_height)
-    gravity = [0.0, 0.0, 0.0]
-    gravity[vaxis] = -g
-    mass = rho0 * (dr * dr) if dim == 2 else rho0 * ((dr * dr) * dr)
-    params = dict(dim=dim, h=H, domain_min=dmin, domain_max=dmax, mass=mass, rho0=rho0,
-                  c0=c0, h_smooth=h, alpha=alpha, eps_xsph=eps_xsph, gravity=gravity,
-                  dt=(0.1 * h) / c0, col_height=col_height,
-                  vertical_axis=vaxis)
     return Case(name or f"dam_break_{dim}d_dr{dr:g}", dim, dr, x, typ,
                 np.zeros_like(x), params)
+
+
+def dam_break_shapes(dim: int, dr: float, *, col_width: float = 1.0, col_height: float = 2.0,
+                     box_width: float = 4.0, box_height: float = 3.0, depth: float = 1.0,
+                     h_factor: float | None = None, wall_layers: int = 3, lid: bool = False,
+                     alpha: float = 0.02, eps_xsph: float = 0.5, g: float = 9.81,
+                     rho0: float = 1000.0, name: str | None = None) -> Shapes:
+    """The same dam break as ``dam_break`` for the device generator
+    (``ParticleSystem.generate``): the fluid box and the wall layer, whose
+    particles the GPU produces in the same order and bit for bit."""
+    fluid_shape, box, width, vaxis, params = _dam_break_setup(
+        dim, dr, col_width, col_height, box_width, box_height, depth, h_factor, wall_layers,
+        lid, alpha, eps_xsph, g, rho0)
+    shapes = [dict(kind="box", type=FLUID, dr=dr, lo=fluid_shape.lo, hi=fluid_shape.hi),
+              dict(kind="layer", type=WALL, dr=dr, lo=box.lo, hi=box.hi, width=width,
+                   keep_axis=-1 if lid else vaxis, keep_max=box_height)]
+    return Shapes(name or f"dam_break_{dim}d_dr{dr:g}", dim, dr, shapes, params)
 
 
 def collision_2d(dr: float = 0.02, c0: float = 20.0) -> Case:

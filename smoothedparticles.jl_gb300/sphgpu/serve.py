@@ -12,11 +12,12 @@ the GPU.  Requests are admitted in arrival order while
 * a slot is free (``max_slots``),
 
 so a request that arrives while others run starts as soon as memory and a slot
-free up, not when the running ones finish as a group.  Lattices are generated
-on host worker threads from arrival on, so setup overlaps the GPU work.  A
-finished request's fields are copied to the host, its device memory is
-released and its completion latency (arrival to results on the host) is
-recorded.
+free up, not when the running ones finish as a group.  Particles are generated
+on the device (``ParticleSystem.generate``; the exact count for the admission
+test comes from ``shape_count``), or, with ``device_lattice=False``, on host
+worker threads from arrival on.  A finished request's fields are copied to the
+host, its device memory is released and its completion latency (arrival to
+results on the host) is recorded.
 
 Members never interact, and each runs the same launches as ``sph_step``
 alone, so every result is bit-identical to running the request by itself.
@@ -58,8 +59,14 @@ class Request:
         return self.done - self.arrival
 
     def case(self):
+        """The request's particles generated on the host."""
         return G.dam_break(self.dim, self.dr, col_height=self.col_height, alpha=self.alpha,
                            name=f"request{self.rid}")
+
+    def shapes(self):
+        """The request's shapes for the device generator (same particles)."""
+        return G.dam_break_shapes(self.dim, self.dr, col_height=self.col_height,
+                                  alpha=self.alpha, name=f"request{self.rid}")
 
 
 def spacing_for(dim: int, particles: float) -> float:
@@ -105,7 +112,8 @@ class Server:
     """
 
     def __init__(self, budget_bytes: int, max_slots: int = 64, chunk: int = 10, depth: int = 2,
-                 device: int = 0, workers: int = 4, result_fields=RESULT_FIELDS):
+                 device: int = 0, workers: int = 4, result_fields=RESULT_FIELDS,
+                 device_lattice: bool = True):
         if chunk < 2 or chunk % 2:
             raise ValueError("chunk must be even and >= 2")
         self.budget = int(budget_bytes)
@@ -115,6 +123,7 @@ class Server:
         self.device = device
         self.workers = workers
         self.result_fields = tuple(result_fields)
+        self.device_lattice = device_lattice
         self.peak_bytes = 0
         self.peak_slots = 0
 
@@ -137,12 +146,19 @@ class Server:
         try:
             while waiting or active:
                 now = clock() - t0
-                # lattices of arrived requests are generated in the background
+                # arrived requests: shapes and exact particle counts (device
+                # generator) or whole lattices on host threads
                 for r in waiting:
                     if r.arrival > now:
                         break
                     if r.rid not in futures:
-                        futures[r.rid] = pool.submit(r.case)
+                        if self.device_lattice:
+                            sh = r.shapes()
+                            fut = cf.Future()
+                            fut.set_result((sh, sphgpu.shape_count(r.dim, sh.shapes, dev)))
+                            futures[r.rid] = fut
+                        else:
+                            futures[r.rid] = pool.submit(r.case)
                 # retire finished members: results to the host, memory released
                 still = []
                 for a in active:
@@ -165,7 +181,11 @@ class Server:
                     if fut is None or not fut.done():
                         break
                     case = fut.result()
-                    need = sphgpu.memory_estimate(case.params, case.n, r.precision)
+                    if self.device_lattice:
+                        case, n_case = case
+                    else:
+                        n_case = case.n
+                    need = sphgpu.memory_estimate(case.params, n_case, r.precision)
                     if need > self.budget:
                         raise RuntimeError(f"request {r.rid} needs {need} B, more than the "
                                            f"whole budget {self.budget} B")
@@ -174,10 +194,13 @@ class Server:
                     waiting.pop(0)
                     del futures[r.rid]
                     g = sphgpu.ParticleSystem(case.params, r.precision, device=dev)
-                    g.upload(case.x, case.v, type=case.type)
+                    if self.device_lattice:
+                        g.generate(case.shapes)
+                    else:
+                        g.upload(case.x, case.v, type=case.type)
                     g.init_state()
                     g.pair_count(reset=True)
-                    r.n, r.bytes = case.n, need
+                    r.n, r.bytes = n_case, need
                     r.admitted = clock() - t0
                     used += need
                     b = sphgpu.Batch([g])

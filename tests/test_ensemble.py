@@ -80,3 +80,13 @@ def test_request_stream_seeded():
         assert 5e3 * 0.999 <= n <= 2e6 * 1.001
     assert abs(spacing_for(2, 2.0 / 0.01 ** 2) - 0.01) < 1e-15
     assert summarize([], 1.0)["requests"] == 0
+
+
+def test_dam_break_shapes_params_match_host_case():
+    from sphgpu import geometry as G
+    for dim, dr, kw in ((2, 0.02, {}), (3, 0.05, dict(lid=True)), (2, 0.01, dict(col_height=1.5))):
+        host = G.dam_break(dim, dr, **kw)
+        dev = G.dam_break_shapes(dim, dr, **kw)
+        assert dev.params == host.params
+        assert [s["type"] for s in dev.shapes] == [G.FLUID, G.WALL]
+        assert dev.shapes[1]["keep_axis"] == (-1 if kw.get("lid") else dim - 1)

@@ -21,7 +21,8 @@ def alone(r, fields):
     return out
 
 
-def test_served_results_equal_alone(gpu):
+@pytest.mark.parametrize("device_lattice", [True, False])
+def test_served_results_equal_alone(gpu, device_lattice):
     F, M = sphgpu.FP64, sphgpu.MIXED
     reqs = [Request(0, 2, 0.04, 24, F, 0.00), Request(1, 3, 0.08, 10, M, 0.02),
             Request(2, 2, 0.03, 31, M, 0.05), Request(3, 3, 0.06, 12, F, 0.05),
@@ -33,7 +34,7 @@ def test_served_results_equal_alone(gpu):
         est.append(sphgpu.memory_estimate(c.params, c.n, r.precision))
     # room for the three largest together: later arrivals must wait for memory
     budget = sum(sorted(est)[-3:])
-    srv = Server(budget, max_slots=4, chunk=4)
+    srv = Server(budget, max_slots=4, chunk=4, device_lattice=device_lattice)
     t = __import__("time").perf_counter()
     done = srv.run(reqs)
     makespan = __import__("time").perf_counter() - t
