@@ -207,6 +207,50 @@ int sph_launch_count(sph_system* sys, int64_t* launches);
 int sph_set_tuning(sph_system* sys, int warps_per_block);
 int sph_get_tuning(const sph_system* sys, int* warps_per_block);
 
+/* ---- assemble_matrix / assemble_vector (src/core.jl:164-225) on the device
+ * and the conjugate-gradient solve of the implicit example
+ * (examples/collapse_dry_implicit.jl:218-233).  The matrix has one entry per
+ * pair within the support, the diagonal (q = p, r = 0) included, rows and
+ * columns in reference particle order, as CSR with each row's columns
+ * ascending.  Built-in functions:
+ *   SPH_MAT_KERNEL      A_pq = W(r_pq)
+ *   SPH_MAT_PROJECTION  the ISPH projection matrix of
+ *                       collapse_dry_implicit.jl:151-160 with this library's
+ *                       kernel: A_pq = 2 h^2 (m / rho0) rDW(r_pq) for q != p,
+ *                       A_pp = h^2 L_p (+ param * max(lambda_p, 0) for fluid p,
+ *                       param = C_free), L_p and lambda_p the div_L_lambda!
+ *                       sums (collapse_dry_implicit.jl:140-145); h = support
+ *   SPH_VEC_PROJECTION  b_p = -h^2 div_p / dt (collapse_dry_implicit.jl:162-164)
+ * sph_cg: unpreconditioned CG from x = 0 until ||r|| <= reltol ||b|| or
+ * maxiter iterations (maxiter < 0: n), host arrays in reference order. */
+#define SPH_MAT_KERNEL 1
+#define SPH_MAT_PROJECTION 2
+#define SPH_VEC_PROJECTION 1
+typedef struct sph_csr sph_csr;
+int sph_assemble_matrix(sph_system* sys, int func, double param, sph_csr** out);
+int sph_assemble_vector(sph_system* sys, int func, double* out);
+int sph_csr_info(const sph_csr* a, int64_t* n, int64_t* nnz);
+int sph_csr_download(sph_csr* a, int64_t* row_ptr, int32_t* col, double* val);
+int sph_csr_destroy(sph_csr* a);
+int sph_cg(sph_csr* a, const double* b, double* x, double reltol, int32_t maxiter,
+           int32_t* iters, double* resid);
+
+/* ---- ParaView export: new_pvd_file / save_frame! / save_pvd_file
+ * (src/IO.jl:15-75).  sph_vtk_open creates `dir` (mkpath) and a frame series;
+ * sph_vtk_save_frame gathers the positions plus the fields in `fields` (bit
+ * 1 << SPH_FIELD_*) on the system's stream, in reference particle order, and
+ * returns: the copy to pinned host memory runs on a separate stream and a host
+ * thread writes <dir>/frame<k>.vtp (VTK XML PolyData, raw appended binary,
+ * one vertex cell per particle); at most two frames are in flight (a third
+ * call waits for a slot).  *frame (optional) = k.  sph_vtk_close waits for
+ * every frame and writes <dir>/result.pvd with the frames' `time` values.
+ * No reference counterpart for sph_vtk_frames (frames on disk so far). */
+typedef struct sph_vtk sph_vtk;
+int sph_vtk_open(sph_system* sys, const char* dir, sph_vtk** out);
+int sph_vtk_save_frame(sph_vtk* vtk, unsigned fields, double time, int32_t* frame);
+int sph_vtk_frames(sph_vtk* vtk, int32_t* written);
+int sph_vtk_close(sph_vtk* vtk);
+
 /* ---- device-side particle generation: covering(grid, shape) of
  * src/grids.jl:52-66 / :128-144 (square / cubic grid, points i*dr in the
  * reference's loop order, i outer) for a Box / Rectangle (src/geometry.jl:15-43)

@@ -20,6 +20,8 @@ ORC_FLUID, ORC_WALL = 0, 1
 OP_DENSITY, OP_DENSITY_REF, OP_FORCE, OP_WALL_PRESSURE = 1, 2, 3, 4
 OP_RESET_RHO, OP_RESET_RHO_REF, OP_RESET_A, OP_EOS, OP_KICK, OP_DRIFT, OP_HYDROSTATIC = range(10, 17)
 SUM_DENSITY, SUM_KERNEL, SUM_PRESSURE, SUM_SHEPARD = 1, 2, 3, 4
+MAT_KERNEL, MAT_PROJECTION = 1, 2
+VEC_PROJECTION = 1
 
 
 class orc_params(C.Structure):
@@ -73,6 +75,8 @@ def load():
         "orc_sum_particle": (None, [P, C.c_int, I64, DP, DP]),
         "orc_keys": (None, [P, DP]),
         "orc_pairs": (I64, [P, DP, I64]),
+        "orc_assemble_matrix": (I64, [P, C.c_int, C.c_double, DP, DP, DP, I64]),
+        "orc_assemble_vector": (None, [P, C.c_int, DP]),
         "orc_init": (I64, [P]),
         "orc_step": (I64, [P, C.c_int]),
         "orc_pair_passes_sample": (I64, [P, I64, I64]),
@@ -193,6 +197,20 @@ class OracleSystem:
         x = np.ascontiguousarray(x, np.float64).reshape(-1, 3)
         out = np.empty(x.shape[0])
         self._lib.orc_sum_point(self._h, func, x.shape[0], _p(x), _p(out))
+        return out
+
+    def assemble_matrix(self, func: int, param: float = 0.0):
+        """(I, J, V) of assemble_matrix in the reference's push order."""
+        n = self._lib.orc_assemble_matrix(self._h, func, float(param), None, None, None, 0)
+        I = np.empty(n, np.int64)
+        J = np.empty(n, np.int64)
+        V = np.empty(n, np.float64)
+        self._lib.orc_assemble_matrix(self._h, func, float(param), _p(I), _p(J), _p(V), n)
+        return I, J, V
+
+    def assemble_vector(self, func: int) -> np.ndarray:
+        out = np.empty(self.n, np.float64)
+        self._lib.orc_assemble_vector(self._h, func, _p(out))
         return out
 
     def sum_particles(self, func: int, idx) -> np.ndarray:

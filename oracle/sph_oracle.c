@@ -535,6 +535,88 @@ int64_t orc_pairs(const orc_system* s, int64_t* pairs, int64_t cap) {
   return cnt;
 }
 
+/* ------------------------------------------------- matrix/vector assembly */
+/* div_L_lambda! of collapse_dry_implicit.jl:140-145 for particle p (after
+ * initialize!: div = L = 0, lambda = 1), neighbours q != p in the
+ * reference order; rDkernel is this library's rDW. */
+static void div_L_lambda(const orc_system* s, int64_t p, double* div, double* L, double* lam) {
+  const double m = s->p.mass, rho = s->p.rho0;
+  const double dim = (double)orc_dim(s);
+  const int64_t key = orc_find_key(s, s->x[p]);
+  double dv = 0.0, l = 0.0, la = 1.0;
+  for (int c = 0; c < s->n_diff; ++c) {
+    const int64_t nk = key + s->key_diff[c];
+    if (!(1 <= nk && nk <= s->key_max)) continue;
+    for (int64_t e = s->cstart[nk]; e < s->cstart[nk + 1]; ++e) {
+      const int64_t q = s->entries[e];
+      double d[3];
+      const double r = sqrt(dist2(s->x[p], s->x[q], d));
+      if (r > s->p.h || p == q) continue;
+      const double rDk = ker_rdw(s, r);
+      const double* vp = s->v[p];
+      const double* vq = s->v[q];
+      /* SmoothedParticles.dot(p.x - q.x, p.v - q.v), algebra.jl:49-51 */
+      const double dot = (d[0] * (vp[0] - vq[0]) + d[1] * (vp[1] - vq[1])) + d[2] * (vp[2] - vq[2]);
+      dv = dv + ((-dot) * m) * rDk;
+      l = l + ((-2.0 * m) / rho) * rDk;
+      la = la + (((m / rho) * rDk) * (r * r)) / dim;
+    }
+  }
+  *div = dv;
+  *L = l;
+  *lam = la;
+}
+
+int64_t orc_assemble_matrix(const orc_system* s, int func, double param, int64_t* I, int64_t* J,
+                            double* V, int64_t cap) {
+  const double H = s->p.h, m = s->p.mass, rho = s->p.rho0;
+  const double h2 = H * H;
+  int64_t cnt = 0;
+  for (int64_t p = 0; p < s->n; ++p) {
+    double diag = 0.0;
+    if (func == ORC_MAT_PROJECTION) {
+      double div, L, lam;
+      div_L_lambda(s, p, &div, &L, &lam);
+      /* projection_matrix(p, p, 0) */
+      diag = s->type[p] == ORC_FLUID ? h2 * L + param * (lam > 0.0 ? lam : 0.0) : h2 * L;
+    }
+    const int64_t key = orc_find_key(s, s->x[p]);
+    for (int c = 0; c < s->n_diff; ++c) {
+      const int64_t nk = key + s->key_diff[c];
+      if (!(1 <= nk && nk <= s->key_max)) continue;
+      for (int64_t e = s->cstart[nk]; e < s->cstart[nk + 1]; ++e) {
+        const int64_t q = s->entries[e];
+        double d[3];
+        const double r = sqrt(dist2(s->x[p], s->x[q], d));
+        if (r > H) continue; /* core.jl:210-213: p == q is kept */
+        double v;
+        if (func == ORC_MAT_KERNEL)
+          v = ker_w(s, r);
+        else
+          v = p == q ? diag : (((2.0 * h2) * m) / rho) * ker_rdw(s, r);
+        if (cnt < cap) {
+          I[cnt] = p;
+          J[cnt] = q;
+          V[cnt] = v;
+        }
+        ++cnt;
+      }
+    }
+  }
+  return cnt;
+}
+
+void orc_assemble_vector(const orc_system* s, int func, double* out) {
+  const double h2 = s->p.h * s->p.h;
+#pragma omp parallel for schedule(static)
+  for (int64_t p = 0; p < s->n; ++p) {
+    double div, L, lam;
+    div_L_lambda(s, p, &div, &L, &lam);
+    /* projection_vector: -h^2 p.div / dt */
+    out[p] = func == ORC_VEC_PROJECTION ? ((-h2) * div) / s->p.dt : 0.0;
+  }
+}
+
 /* ------------------------------------------------------ step and initial */
 /* collapse_symplectic.jl:186-191 (+ the hydrostatic reference density) */
 int64_t orc_init(orc_system* s) {

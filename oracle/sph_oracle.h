@@ -129,6 +129,20 @@ void orc_keys(const orc_system* s, int64_t* keys);
  * cap pairs and returns the total count. */
 int64_t orc_pairs(const orc_system* s, int64_t* pairs, int64_t cap);
 
+/* core.jl:196-225 assemble_matrix / core.jl:175-183 assemble_vector with the
+ * built-in functions (the GPU's SPH_MAT_* / SPH_VEC_*).  The matrix entries
+ * (I, J, V) are pushed in the reference's loop order: row p, its key_diff
+ * cells, each cell's entries, p itself included (r = 0).  Returns the entry
+ * count (writes at most cap). */
+enum {
+  ORC_MAT_KERNEL = 1,     /* W(r)                                              */
+  ORC_MAT_PROJECTION = 2  /* collapse_dry_implicit.jl:151-160 (param = C_free) */
+};
+enum { ORC_VEC_PROJECTION = 1 /* collapse_dry_implicit.jl:162-164, div by div_L_lambda! */ };
+int64_t orc_assemble_matrix(const orc_system* s, int func, double param, int64_t* I, int64_t* J,
+                            double* V, int64_t cap);
+void orc_assemble_vector(const orc_system* s, int func, double* out);
+
 /* Initialisation of the dam-break state (collapse_symplectic.jl:186-191 plus
  * the hydrostatic reference density) and the kick-drift-kick step
  * (collapse_symplectic.jl:170-180).  Both return fluid-target pair counts. */

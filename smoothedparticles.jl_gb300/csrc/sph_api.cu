@@ -10,48 +10,10 @@
 #include <vector>
 
 #include "sph_launch.h"
+#include "sph_system.h"
 #include "sphgpu.h"
 
 using namespace sphgpu;
-
-struct sph_system {
-  sph_params params{};
-  int device = 0;
-  Geometry geo{};
-  Consts k{};
-  cudaStream_t stream = nullptr;
-  State cur{}, alt{};
-  BinScratch b{};
-  void* arena = nullptr;    // per-particle arrays (both SoA sets + scratch + staging)
-  void* cells = nullptr;    // cell tables and counters
-  void* staging = nullptr;  // host-transfer staging inside the arena
-  double* query = nullptr;  // sum() query buffer
-  size_t query_bytes = 0;
-  int cap = 0;              // particles the arena holds
-  int n_host = 0;           // upper bound of the device-resident count
-  bool cells_valid = false;
-  // FP32 neighbour records current (mixed precision): of the fluid particles
-  // (written by a fused density pass) and of the walls (wall-pressure pass)
-  bool aux_fluid = false;
-  bool aux_wall = false;
-  bool lists_valid = false;  // hit lists of the last density pass match cells and positions
-  std::string err;
-  // launch accounting and optional per-kernel CUDA-event timing
-  bool profiling = false;
-  struct Pending {
-    int kid;
-    cudaEvent_t start, stop;
-  };
-  std::vector<Pending> pending;
-  std::vector<cudaEvent_t> pool;
-  cudaEvent_t open_start = nullptr;
-  double total_ms[SPH_KERNEL_COUNT] = {};
-  long long kernel_launches[SPH_KERNEL_COUNT] = {};
-  long long total_launches = 0;
-  // bumped whenever device buffers are reallocated or the launch shape
-  // changes, so a batch knows its captured graph is stale
-  long long generation = 0;
-};
 
 // Many systems stepped together: each member's fused step is captured once
 // into a CUDA graph as an independent branch (two steps per graph, so every
@@ -301,20 +263,14 @@ size_t field_bytes(int f, size_t n) {
   return 8 * n;
 }
 
-struct DeviceGuard {
-  int prev = -1;
-  explicit DeviceGuard(int dev) {
-    cudaGetDevice(&prev);
-    if (prev != dev) cudaSetDevice(dev);
-  }
-  ~DeviceGuard() {
-    int cur = -1;
-    cudaGetDevice(&cur);
-    if (prev >= 0 && cur != prev) cudaSetDevice(prev);
-  }
-};
+
 
 }  // namespace
+
+namespace sphgpu {
+LaunchCtx system_ctx(sph_system* s) { return ctx(s); }
+int system_fail(sph_system* s, int code, const char* msg) { return fail(s, code, "%s", msg); }
+}  // namespace sphgpu
 
 extern "C" {
 

@@ -25,7 +25,8 @@ __all__ = ["ParticleSystem", "ParticleField", "create_cell_list", "apply", "appl
            "FP64", "MIXED", "find_rho", "find_rho0", "internal_force", "find_pressure",
            "reset_rho", "reset_rho0", "reset_a", "accelerate", "move", "hydrostatic",
            "DENSITY", "KERNEL", "PRESSURE", "SHEPARD", "wall_pressure", "Batch", "pipe_peak",
-           "memory_estimate", "shape_count"]
+           "memory_estimate", "shape_count", "assemble_matrix", "assemble_vector", "CsrMatrix",
+           "MAT_KERNEL", "MAT_PROJECTION", "VEC_PROJECTION"]
 
 
 class SphError(RuntimeError):
@@ -338,6 +339,78 @@ class Batch:
             self.close()
         except Exception:
             pass
+
+
+MAT_KERNEL = L.SPH_MAT_KERNEL
+MAT_PROJECTION = L.SPH_MAT_PROJECTION
+VEC_PROJECTION = L.SPH_VEC_PROJECTION
+
+
+class CsrMatrix:
+    """A device-resident sparse matrix from ``assemble_matrix`` (CSR, rows
+    and columns in reference particle order, columns ascending per row)."""
+
+    def __init__(self, handle):
+        self._lib = L.load()
+        self._h = handle
+        n, nnz = C.c_int64(), C.c_int64()
+        self._lib.sph_csr_info(self._h, C.byref(n), C.byref(nnz))
+        self.n, self.nnz = n.value, nnz.value
+
+    def arrays(self):
+        """(row_ptr int64[n+1], col int32[nnz], val float64[nnz]) on the host."""
+        rp = np.empty(self.n + 1, np.int64)
+        col = np.empty(self.nnz, np.int32)
+        val = np.empty(self.nnz, np.float64)
+        rc = self._lib.sph_csr_download(self._h, _ptr(rp), _ptr(col), _ptr(val))
+        if rc != 0:
+            raise SphError(rc, "sph_csr_download failed")
+        return rp, col, val
+
+    def to_scipy(self):
+        import scipy.sparse as sp
+        rp, col, val = self.arrays()
+        return sp.csr_matrix((val, col, rp), shape=(self.n, self.n))
+
+    def cg(self, b, reltol: float = float(np.sqrt(np.finfo(np.float64).eps)), maxiter: int = -1):
+        """cg(A, b) of IterativeSolvers (x0 = 0, ||r|| <= reltol ||b||) on the
+        device; returns (x, iterations, final residual norm)."""
+        b = np.ascontiguousarray(b, dtype=np.float64).reshape(self.n)
+        x = np.empty(self.n, np.float64)
+        it, res = C.c_int32(), C.c_double()
+        rc = self._lib.sph_cg(self._h, _ptr(b), _ptr(x), float(reltol), int(maxiter),
+                              C.byref(it), C.byref(res))
+        if rc != 0:
+            raise SphError(rc, "sph_cg failed")
+        return x, it.value, res.value
+
+    def close(self):
+        if getattr(self, "_h", None):
+            self._lib.sph_csr_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def assemble_matrix(system: "ParticleSystem", func: int, param: float = 0.0) -> CsrMatrix:
+    """assemble_matrix(sys, func) (core.jl:196-225) with a built-in function:
+    MAT_KERNEL (W) or MAT_PROJECTION (the ISPH projection matrix; param =
+    C_free).  Needs a current cell list."""
+    h = C.c_void_p()
+    system._check(system._lib.sph_assemble_matrix(system._h, int(func), float(param), C.byref(h)))
+    return CsrMatrix(h)
+
+
+def assemble_vector(system: "ParticleSystem", func: int) -> np.ndarray:
+    """assemble_vector(sys, func) (core.jl:175-183) with a built-in function
+    (VEC_PROJECTION), in reference particle order."""
+    out = np.empty(system.n, np.float64)
+    system._check(system._lib.sph_assemble_vector(system._h, int(func), _ptr(out)))
+    return out
 
 
 def shape_count(dim: int, shapes, device: int = 0) -> int:

@@ -83,6 +83,10 @@ class sph_params(C.Structure):
     ]
 
 
+SPH_MAT_KERNEL = 1
+SPH_MAT_PROJECTION = 2
+SPH_VEC_PROJECTION = 1
+
 SPH_SHAPE_BOX = 1
 SPH_SHAPE_LAYER = 2
 
@@ -183,6 +187,16 @@ PROTOTYPES = {
     "sph_memory_estimate": (C.c_int, [C.POINTER(sph_params), _I64, C.POINTER(C.c_uint64)]),
     "sph_memory_usage": (C.c_int, [_P, C.POINTER(C.c_uint64)]),
     "sph_query": (C.c_int, [_P, C.POINTER(C.c_int)]),
+    "sph_assemble_matrix": (C.c_int, [_P, C.c_int, C.c_double, C.POINTER(_P)]),
+    "sph_assemble_vector": (C.c_int, [_P, C.c_int, _P]),
+    "sph_csr_info": (C.c_int, [_P, C.POINTER(_I64), C.POINTER(_I64)]),
+    "sph_csr_download": (C.c_int, [_P, _P, _P, _P]),
+    "sph_csr_destroy": (C.c_int, [_P]),
+    "sph_cg": (C.c_int, [_P, _P, _P, C.c_double, _I32, C.POINTER(_I32), C.POINTER(C.c_double)]),
+    "sph_vtk_open": (C.c_int, [_P, C.c_char_p, C.POINTER(_P)]),
+    "sph_vtk_save_frame": (C.c_int, [_P, C.c_uint, C.c_double, C.POINTER(_I32)]),
+    "sph_vtk_frames": (C.c_int, [_P, C.POINTER(_I32)]),
+    "sph_vtk_close": (C.c_int, [_P]),
     "sph_generate": (C.c_int, [_P, C.POINTER(sph_shape), C.c_int, C.POINTER(_I64)]),
     "sph_shape_count": (C.c_int, [C.c_int, C.c_int, C.POINTER(sph_shape), C.c_int,
                                   C.POINTER(_I64)]),
