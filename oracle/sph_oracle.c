@@ -34,6 +34,7 @@ struct orc_system {
   int n_diff;
   /* derived constants, computed once */
   double inv_h, cw, cr, B, hdt, eta2, alpha_c0, gmag;
+  double mcw, mcr, ca; /* m C_w, m C_r, -(alpha c0) h_smooth */
   /* particles in the reference's order (0-based index = position in
    * sys.particles minus one) */
   int64_t n, cap;
@@ -104,6 +105,9 @@ orc_system* orc_create(const orc_params* p) {
   s->hdt = 0.5 * p->dt;
   s->eta2 = 0.01 * (p->h_smooth * p->h_smooth);
   s->alpha_c0 = p->alpha * p->c0;
+  s->mcw = p->mass * s->cw;
+  s->mcr = p->mass * s->cr;
+  s->ca = -(s->alpha_c0 * p->h_smooth);
   s->gmag = fabs(p->gravity[p->vertical_axis]);
   s->cstart = (int64_t*)calloc((size_t)(s->key_max + 2), sizeof(int64_t));
   return s;
@@ -300,7 +304,6 @@ static inline double dist2(const double* xp, const double* xq, double d[3]) {
  *                / sum_f W over fluid neighbours (Adami, Hu & Adams 2012) */
 static int64_t binary_one(orc_system* s, int op, int64_t p) {
   const double H = s->p.h;
-  const double m = s->p.mass;
   const int64_t key = orc_find_key(s, s->x[p]); /* core.jl:95 */
   const int tp = s->type[p];
   const int active = op == ORC_OP_WALL_PRESSURE ? tp == ORC_WALL : tp == ORC_FLUID;
@@ -326,42 +329,50 @@ static int64_t binary_one(orc_system* s, int op, int64_t p) {
       /* pairs the operator acts on: every neighbour, except that the wall
        * pressure only sums fluid neighbours */
       if (op != ORC_OP_WALL_PRESSURE || tq == ORC_FLUID) ++pairs;
+      /* The kernel pieces on a hit (kernels.jl:108-195 are @fastmath; this
+       * is the one evaluation order both implementations use): x = r (1/h),
+       * t = 1 - x (0 beyond the support), W = (C_w t^4)(1 + 4x),
+       * rDW = C_r t^3, with the particle mass folded into the constants and
+       * the sums formed with fused multiply-adds. */
+      const double x = r * s->inv_h;
+      const double t = x > 1.0 ? 0.0 : 1.0 - x;
+      const double t2 = t * t;
       if (op == ORC_OP_DENSITY || op == ORC_OP_DENSITY_REF) {
-        acc = acc + m * ker_w(s, r);
+        acc = fma(s->mcw * (t2 * t2), fma(4.0, x, 1.0), acc); /* + m W */
       } else if (op == ORC_OP_WALL_PRESSURE) {
         if (tq == ORC_FLUID) {
-          const double w = ker_w(s, r);
-          const double gd = (g[0] * d[0] + g[1] * d[1]) + g[2] * d[2];
-          wp = wp + s->P[q] * w;
-          wg = wg + (s->rho[q] * gd) * w;
+          const double w = (s->cw * (t2 * t2)) * fma(4.0, x, 1.0);
+          const double gd = fma(g[2], d[2], fma(g[1], d[1], g[0] * d[0]));
+          wp = fma(s->P[q], w, wp);
+          wg = fma(s->rho[q] * gd, w, wg);
           ws = ws + w;
         }
       } else if (tq == ORC_FLUID) {
-        const double ker = m * ker_rdw(s, r);
+        const double ker = s->mcr * (t2 * t); /* m rDW */
         const double dv0 = vp[0] - s->v[q][0], dv1 = vp[1] - s->v[q][1], dv2 = vp[2] - s->v[q][2];
-        const double vdx = (dv0 * d[0] + dv1 * d[1]) + dv2 * d[2];
+        const double vdx = fma(dv2, d[2], fma(dv1, d[1], dv0 * d[0]));
         const double inv_rb = 2.0 / (rhop + s->rho[q]);
         double pi = 0.0;
         if (vdx < 0.0) {
+          /* Monaghan: -alpha c0 mu / rho_bar, mu = h v.x / (r^2 + eta^2) */
           const double r2 = (d[0] * d[0] + d[1] * d[1]) + d[2] * d[2];
-          const double mu = (s->p.h_smooth * vdx) / (r2 + s->eta2);
-          pi = (-s->alpha_c0 * mu) * inv_rb;
+          pi = ((s->ca * vdx) / (r2 + s->eta2)) * inv_rb;
         }
         const double cf = -ker * ((prp + s->Pr[q]) + pi);
-        ax = ax + cf * d[0];
-        ay = ay + cf * d[1];
-        az = az + cf * d[2];
-        const double wx = (m * ker_w(s, r)) * inv_rb;
-        sx = sx + wx * (s->v[q][0] - vp[0]);
-        sy = sy + wx * (s->v[q][1] - vp[1]);
-        sz = sz + wx * (s->v[q][2] - vp[2]);
+        ax = fma(cf, d[0], ax);
+        ay = fma(cf, d[1], ay);
+        az = fma(cf, d[2], az);
+        const double wx = ((s->mcw * (t2 * t2)) * fma(4.0, x, 1.0)) * inv_rb; /* m W / rho_bar */
+        sx = fma(-wx, dv0, sx); /* + wx (v_q - v_p) */
+        sy = fma(-wx, dv1, sy);
+        sz = fma(-wx, dv2, sz);
       } else {
         /* wall neighbour: pressure term only */
-        const double ker = m * ker_rdw(s, r);
+        const double ker = s->mcr * (t2 * t);
         const double cf = -ker * (prp + s->Pr[q]);
-        ax = ax + cf * d[0];
-        ay = ay + cf * d[1];
-        az = az + cf * d[2];
+        ax = fma(cf, d[0], ax);
+        ay = fma(cf, d[1], ay);
+        az = fma(cf, d[2], az);
       }
     }
   }

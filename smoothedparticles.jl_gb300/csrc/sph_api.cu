@@ -332,6 +332,9 @@ static int setup_host(const sph_params* p, sph_system* s) {
   k.dt = p->dt;
   k.eta2 = 0.01 * (p->h_smooth * p->h_smooth);
   k.alpha_c0 = p->alpha * p->c0;
+  k.mcw = p->mass * k.cw;
+  k.mcr = p->mass * k.cr;
+  k.ca = -(k.alpha_c0 * p->h_smooth);
   k.h_smooth = p->h_smooth;
   k.eps_xsph = p->eps_xsph;
   k.gmag = std::fabs(p->gravity[p->vertical_axis]);

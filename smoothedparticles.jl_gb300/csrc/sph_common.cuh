@@ -70,6 +70,8 @@ struct Consts {
   float hf, s_lo, s_hi;
   // the largest double s with sqrt_rn(s) <= h: r > h  <=>  fl64(r^2 sum) > s_max
   double s_max;
+  // folded constants of the FP64 pair arithmetic: m C_w, m C_r, -(alpha c0) h_smooth
+  double mcw, mcr, ca;
   // FP32 copies for the mixed-precision pair arithmetic
   float inv_hf, cwf, crf, massf, eta2f, alpha_c0f, h_smoothf, rho0f;
   float gf[3];
@@ -142,6 +144,29 @@ __device__ __forceinline__ void decode_key(const Geometry& g, int key, int& cx, 
   const int t = k0 / l0;
   cy = t % l1;
   cz = t / l1;
+}
+
+// x > 1 for x >= +0 (x = r / h), as an integer comparison of the bit patterns
+// (IEEE order equals integer order for non-negative doubles): no FP64 slot
+__device__ __forceinline__ bool gt1(double x) {
+  return __double_as_longlong(x) > 0x3FF0000000000000LL;
+}
+
+// v < 0.0 exactly (false for -0 and NaN), on the integer pipe
+__device__ __forceinline__ bool lt0(double v) {
+  const long long b = __double_as_longlong(v);
+  const long long m = b & 0x7FFFFFFFFFFFFFFFLL;
+  return b < 0 && m != 0 && m <= 0x7FF0000000000000LL;
+}
+
+// 2.0 / y, correctly rounded: 2 RN(1/y) with the factor 2 applied to the
+// exponent field, which is exact while RN(1/y) and its double are normal;
+// otherwise the division itself
+__device__ __forceinline__ double two_over(double y) {
+  const double r = __drcp_rn(y);
+  const long long b = __double_as_longlong(r);
+  const long long e = (b >> 52) & 0x7FF;
+  return (e >= 1 && e <= 0x7FD) ? __longlong_as_double(b + (1LL << 52)) : __ddiv_rn(2.0, y);
 }
 
 // kernels.jl:108-115 / :156-163 in the evaluation order written in the oracle

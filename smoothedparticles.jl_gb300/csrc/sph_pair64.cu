@@ -69,8 +69,8 @@ struct Proc64 {
   }
 
   __device__ __forceinline__ void process(const int* list, int stride, int cnt) {
-    for (int t = 0; t < cnt; ++t) {
-      const int e = __ldg(&list[(size_t)t * stride]);
+    for (int j = 0; j < cnt; ++j) {
+      const int e = __ldg(&list[(size_t)j * stride]);
       if (e == kCwSkip) continue;  // a band candidate beyond the support
       const int q = e & kCwIndexMask;
       double d[3];
@@ -78,55 +78,56 @@ struct Proc64 {
       const double r = sqrt(ss);
       const bool fluid = OP != SPH_OP_FORCE || __ldg(&s.type[q]) == kFluid;
       if (fluid) ++c0; else ++c1;
+      // kernel pieces in the oracle's order: x = r (1/h), t = 1 - x (0 beyond
+      // the support); W = (C_w t^4)(1 + 4x), rDW = C_r t^3; mass folded into
+      // the constants; sums with fused multiply-adds
+      const double x = r * k.inv_h;
+      const double t = gt1(x) ? 0.0 : 1.0 - x;
+      const double t2 = t * t;
       if (OP == SPH_OP_DENSITY || OP == SPH_OP_DENSITY_REF) {
-        acc = acc + k.mass * ker_w(k, r);
+        acc = __fma_rn(k.mcw * (t2 * t2), __fma_rn(4.0, x, 1.0), acc);
       } else if (OP == SPH_OP_WALL_PRESSURE) {
         // Adami, Hu & Adams (2012) wall pressure, g . (x_w - x_f)
-        const double w = ker_w(k, r);
-        double gd = k.g[0] * d[0] + k.g[1] * d[1];
-        if (DIM == 3) gd = gd + k.g[2] * d[2];
-        wp = wp + __ldg(&s.P[q]) * w;
-        wg = wg + (__ldg(&s.rho[q]) * gd) * w;
+        const double w = (k.cw * (t2 * t2)) * __fma_rn(4.0, x, 1.0);
+        double gd = __fma_rn(k.g[1], d[1], k.g[0] * d[0]);
+        if (DIM == 3) gd = __fma_rn(k.g[2], d[2], gd);
+        wp = __fma_rn(__ldg(&s.P[q]), w, wp);
+        wg = __fma_rn(__ldg(&s.rho[q]) * gd, w, wg);
         ws = ws + w;
       } else if (fluid) {
         // pressure (collapse_symplectic.jl:114-118) + Monaghan viscosity + XSPH
-        const double ker = k.mass * ker_rdw(k, r);
+        const double ker = k.mcr * (t2 * t);
         double vq[3];
         vq[0] = __ldg(&s.v[0][q]);
         vq[1] = __ldg(&s.v[1][q]);
         vq[2] = DIM == 3 ? __ldg(&s.v[2][q]) : 0.0;
         const double dv0 = vp[0] - vq[0];
         const double dv1 = vp[1] - vq[1];
-        double vdx = dv0 * d[0] + dv1 * d[1];
-        if (DIM == 3) {
-          const double dv2 = vp[2] - vq[2];
-          vdx = vdx + dv2 * d[2];
-        }
+        const double dv2 = DIM == 3 ? vp[2] - vq[2] : 0.0;
+        double vdx = __fma_rn(dv1, d[1], dv0 * d[0]);
+        if (DIM == 3) vdx = __fma_rn(dv2, d[2], vdx);
         const double rhoq = __ldg(&s.rho[q]);
-        const double inv_rb = 2.0 / (rhop + rhoq);
+        const double inv_rb = two_over(rhop + rhoq);
         double pi = 0.0;
-        if (vdx < 0.0) {
-          const double mu = (k.h_smooth * vdx) / (ss + k.eta2);
-          pi = (-k.alpha_c0 * mu) * inv_rb;
+        if (lt0(vdx)) {
+          pi = ((k.ca * vdx) / (ss + k.eta2)) * inv_rb;
           ++c2;
         }
         const double cf = -ker * ((prp + __ldg(&s.Pr[q])) + pi);
-        ax = ax + cf * d[0];
-        ay = ay + cf * d[1];
-        if (DIM == 3) az = az + cf * d[2];
-        // XSPH: wx (v_q - v_p); v_q - v_p = -(v_p - v_q) exactly in IEEE
-        // arithmetic, so subtracting wx dv rounds identically
-        const double wx = (k.mass * ker_w(k, r)) * inv_rb;
-        sx = sx - wx * dv0;
-        sy = sy - wx * dv1;
-        if (DIM == 3) sz = sz - wx * (vp[2] - vq[2]);
+        ax = __fma_rn(cf, d[0], ax);
+        ay = __fma_rn(cf, d[1], ay);
+        if (DIM == 3) az = __fma_rn(cf, d[2], az);
+        const double wx = ((k.mcw * (t2 * t2)) * __fma_rn(4.0, x, 1.0)) * inv_rb;
+        sx = __fma_rn(-wx, dv0, sx);
+        sy = __fma_rn(-wx, dv1, sy);
+        if (DIM == 3) sz = __fma_rn(-wx, dv2, sz);
       } else {
         // wall neighbour: pressure term with the wall pressure
-        const double ker = k.mass * ker_rdw(k, r);
+        const double ker = k.mcr * (t2 * t);
         const double cf = -ker * (prp + __ldg(&s.Pr[q]));
-        ax = ax + cf * d[0];
-        ay = ay + cf * d[1];
-        if (DIM == 3) az = az + cf * d[2];
+        ax = __fma_rn(cf, d[0], ax);
+        ay = __fma_rn(cf, d[1], ay);
+        if (DIM == 3) az = __fma_rn(cf, d[2], az);
       }
     }
   }
