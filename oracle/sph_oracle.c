@@ -354,9 +354,9 @@ static int64_t binary_one(orc_system* s, int op, int64_t p) {
         const double inv_rb = 2.0 / (rhop + s->rho[q]);
         double pi = 0.0;
         if (vdx < 0.0) {
-          /* Monaghan: -alpha c0 mu / rho_bar, mu = h v.x / (r^2 + eta^2) */
-          const double r2 = (d[0] * d[0] + d[1] * d[1]) + d[2] * d[2];
-          pi = ((s->ca * vdx) / (r2 + s->eta2)) * inv_rb;
+          /* Monaghan: -alpha c0 mu / rho_bar, mu = h v.x / (r^2 + eta^2),
+           * r^2 as r r, the quotient as a product with the reciprocal */
+          pi = ((s->ca * vdx) * (1.0 / (r * r + s->eta2))) * inv_rb;
         }
         const double cf = -ker * ((prp + s->Pr[q]) + pi);
         ax = fma(cf, d[0], ax);

@@ -160,6 +160,7 @@ size_t carve(sph_system* s, char* base, size_t C) {
     b.hit_cap = 0;
     b.hits = nullptr;
     b.hit_count = nullptr;
+    b.hitr = nullptr;
   } else {
     // hits per target: ~256 in the 3D lattice interior (H = 4 dr), ~68 in
     // 2D (H = 4.8 dr); the capacity leaves room for compression, and an
@@ -167,6 +168,8 @@ size_t carve(sph_system* s, char* base, size_t C) {
     b.hit_cap = D == 3 ? 384 : 160;
     b.hits = (int*)take(4 * (size_t)b.hit_cap * C);
     b.hit_count = (int*)take(4 * C);
+    // the density pass's distance of every entry, read by the force pass
+    b.hitr = (double*)take(8 * (size_t)b.hit_cap * C);
     b.ck_cap = 0;
     b.ck_mask = nullptr;
   }

@@ -1,4 +1,5 @@
-// sph_cellwarp.cuh -- the traversal shared by the FP64 and mixed pair passes.
+// sph_cellwarp.cuh -- the traversal of the FP64 pair passes (the mixed passes
+// in sph_pair32.cu stage candidates the same way but keep hit masks).
 //
 // One warp per work item: up to 32 targets of ONE cell (the work list is built
 // with the binning).  All lanes share the cell, so they share the neighbour
@@ -17,8 +18,10 @@
 // list in order, so each target's sums are formed in exactly the reference's
 // order, and the lanes' lists have nearly equal lengths (the FP64 work runs
 // with full warps).  The force pass of the same binning reads the lists back
-// instead of traversing again.  A list that would exceed hit_cap is processed
-// early and its item is marked partial (the force pass then traverses it).
+// instead of traversing again, together with each entry's distance, which
+// the density pass stores beside the list.  A list that would exceed hit_cap
+// is processed early and its item is marked partial (the force pass then
+// traverses it).
 #pragma once
 
 #include "sph_common.cuh"
@@ -122,15 +125,20 @@ __device__ __forceinline__ void cw_resolve(const State& s, const Consts& k, CwSh
 // neighbour cell c, or kCwSkip when the operator ignores it (a skipped hit
 // is not an interaction of the operator);
 // P::process(list, stride, cnt) consumes cnt entries list[0], list[stride], ...
-// skipping kCwSkip entries.  Returns the number of entries left in the list;
-// sets `partial` when the list was processed early.  FLUID_CELLS_ONLY: skip
+// skipping kCwSkip entries; P::rmem / P::rmode: the entries' distances beside
+// the list (rmode 1: process stores them, 2: process reads them, 0: neither).
+// Returns the number of entries left in the list; sets `partial` when the
+// list was processed early; `keep`: the pass keeps its lists (and distances).  FLUID_CELLS_ONLY: skip
 // neighbour cells without fluid (for operators that ignore wall neighbours).
 template <int DIM, bool FLUID_CELLS_ONLY, class P>
 __device__ __forceinline__ int cw_traverse(const State& s, const Geometry& g, const Consts& k,
                                            const BinScratch& b, CwShared& sh, int lane,
-                                           const CwTarget& t, P& proc, bool& partial) {
+                                           const CwTarget& t, P& proc, bool& partial, bool keep) {
   int* const list = cw_list(b, t.i);  // dereferenced only by active lanes
   const int cap = b.hit_cap;
+  // a keeping pass records each entry's distance for the force pass
+  proc.rmode = keep && b.hitr ? 1 : 0;
+  proc.rmem = b.hitr ? b.hitr + (size_t)t.i * cap : nullptr;
   int cnt = 0;
   int nb = 0;  // deferred band candidates of this lane
   cw_offsets(g, k, sh, lane, t);
@@ -251,13 +259,16 @@ __device__ __forceinline__ void cw_pass(const State& s, const Geometry& g, const
                                         const CwTarget& t, P& proc, int list_mode) {
   if (list_mode == 2 && __ldg(&b.item_partial[item]) == 0) {
     cw_offsets(g, k, sh, lane, t);
+    // the density pass stored each entry's distance next to the list
+    proc.rmode = b.hitr ? 2 : 0;
+    proc.rmem = b.hitr ? b.hitr + (size_t)t.i * b.hit_cap : nullptr;
     if (t.active) proc.process(cw_list(b, t.i), kCwRow, __ldg(&b.hit_count[t.i]));
     __syncwarp();
     return;
   }
   bool partial = false;
   const int left = cw_traverse<DIM, OP == SPH_OP_WALL_PRESSURE>(s, g, k, b, sh, lane, t, proc,
-                                                                partial);
+                                                                partial, list_mode == 1);
   if (list_mode == 1) {
     if (t.active) b.hit_count[t.i] = left;
     if (lane == 0) b.item_partial[item] = partial ? 1 : 0;

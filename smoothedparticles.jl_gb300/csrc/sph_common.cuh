@@ -110,6 +110,7 @@ struct BinScratch {
   // same binning (null in mixed-precision systems)
   int* hits;
   int* hit_count;
+  double* hitr;       // the distance of every hit list entry (same layout as hits)
   int* item_partial;  // 1 when an item's list overflowed hit_cap
   int hit_cap;
   int* cell_fluid;    // key_max + 3: fluid particles per cell

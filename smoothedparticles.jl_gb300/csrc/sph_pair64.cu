@@ -7,10 +7,14 @@
 // to it (IEEE division and square root are correctly rounded on both sides).
 //
 // Traversal: sph_cellwarp.cuh (cell-aligned warps, shared-memory staged
-// candidates, FP32 classification with an FP64 band test, per-lane hit
-// queues processed in order).  The FP64 pipe is the bound of these passes
-// (1/58 of the FP32 rate on GB300); the queues keep each FP64 instruction on
-// a hit, with the warp's lanes processing their hits together.
+// candidates, FP32 classification with an FP64 band test, per-target hit
+// lists processed in order by every lane together).  The FP64 pipe is the
+// bound of these passes (1/58 of the FP32 rate on GB300), so the evaluation
+// order below keeps FP64 operations per hit few: mass folded into the kernel
+// constants, fused multiply-adds for the sums, integer tests of x > 1 and
+// v.x < 0, 2/(rho_p + rho_q) from a correctly rounded reciprocal, and the
+// force pass reusing the distances the density pass stored.  The CPU
+// restatement evaluates the same expressions.
 //
 // Why the FP32 classification is exact: positions are stored relative to
 // their cell's origin, |xl| < 1.02 h; the neighbour-cell offset is an integer
@@ -55,6 +59,8 @@ struct Proc64 {
   double rhop, prp;
   double acc, ax, ay, az, sx, sy, sz, wp, wg, ws;
   int c0, c1, c2;
+  double* rmem = nullptr;  // distances beside the list
+  int rmode = 0;           // 1 store them, 2 read them
 
   __device__ Proc64(const State& s_, const Consts& k_) : s(s_), k(k_) {
     acc = ax = ay = az = sx = sy = sz = wp = wg = ws = 0.0;
@@ -74,8 +80,19 @@ struct Proc64 {
       if (e == kCwSkip) continue;  // a band candidate beyond the support
       const int q = e & kCwIndexMask;
       double d[3];
-      const double ss = dist2_64<DIM>(s, xp, q, d);
-      const double r = sqrt(ss);
+      double r;
+      if (OP == SPH_OP_FORCE && rmode == 2) {
+        // the separation for the direction; the distance as the density
+        // pass computed it from the same positions
+        d[0] = xp[0] - __ldg(&s.x[0][q]);
+        d[1] = xp[1] - __ldg(&s.x[1][q]);
+        d[2] = DIM == 3 ? xp[2] - __ldg(&s.x[2][q]) : 0.0;
+        r = __ldg(&rmem[(size_t)j * stride]);
+      } else {
+        r = sqrt(dist2_64<DIM>(s, xp, q, d));
+        if ((OP == SPH_OP_DENSITY || OP == SPH_OP_DENSITY_REF) && rmode == 1)
+          rmem[(size_t)j * stride] = r;
+      }
       const bool fluid = OP != SPH_OP_FORCE || __ldg(&s.type[q]) == kFluid;
       if (fluid) ++c0; else ++c1;
       // kernel pieces in the oracle's order: x = r (1/h), t = 1 - x (0 beyond
@@ -110,7 +127,8 @@ struct Proc64 {
         const double inv_rb = two_over(rhop + rhoq);
         double pi = 0.0;
         if (lt0(vdx)) {
-          pi = ((k.ca * vdx) / (ss + k.eta2)) * inv_rb;
+          // mu = h v.x / (r^2 + eta^2) with r^2 as r r and the reciprocal
+          pi = ((k.ca * vdx) * __drcp_rn(r * r + k.eta2)) * inv_rb;
           ++c2;
         }
         const double cf = -ker * ((prp + __ldg(&s.Pr[q])) + pi);
