@@ -51,22 +51,28 @@ struct orc_system {
 };
 
 /* ---------------------------------------------------------------- kernels */
-/* kernels.jl:108-115 (wendland2), :156-163 (wendland3) */
-static inline double ker_w(const orc_system* s, double r) {
-  double x = r * s->inv_h;
-  if (x > 1.0) return 0.0;
-  double t = 1.0 - x;
-  double t2 = t * t;
-  double t4 = t2 * t2;
-  return (s->cw * t4) * (1.0 + 4.0 * x);
+/* The Wendland quintic (kernels.jl:108-115 wendland2, :156-163 wendland3)
+ * and its derivative over r (kernels.jl:140-147, :188-195) are @fastmath in
+ * the reference; both implementations evaluate them in this one order:
+ * t = 1 - r (1/h) as one fused operation, 0 beyond the support,
+ * W = (C_w t^4)(5 - 4t) (5 - 4t = 1 + 4x), rDW = C_r t^3. */
+static inline double ker_t(const orc_system* s, double r) {
+  const double t = fma(-r, s->inv_h, 1.0);
+  return t < 0.0 ? 0.0 : t;
 }
-/* kernels.jl:140-147 (rDwendland2), :188-195 (rDwendland3) */
+static inline double ker_w(const orc_system* s, double r) {
+  const double t = ker_t(s, r);
+  const double t2 = t * t;
+  return (s->cw * (t2 * t2)) * fma(-4.0, t, 5.0);
+}
 static inline double ker_rdw(const orc_system* s, double r) {
-  double x = r * s->inv_h;
-  if (x > 1.0) return 0.0;
-  double t = 1.0 - x;
-  double t2 = t * t;
-  return s->cr * (t2 * t);
+  const double t = ker_t(s, r);
+  return s->cr * ((t * t) * t);
+}
+/* the distance a kernel is evaluated at: sqrt((d0 d0 + d1 d1) + d2 d2) with
+ * the sum fused (the support test keeps the reference's unfused dist) */
+static inline double ker_r(const double d[3]) {
+  return sqrt(fma(d[2], d[2], fma(d[1], d[1], d[0] * d[0])));
 }
 
 /* ------------------------------------------------------------ construction */
@@ -329,19 +335,17 @@ static int64_t binary_one(orc_system* s, int op, int64_t p) {
       /* pairs the operator acts on: every neighbour, except that the wall
        * pressure only sums fluid neighbours */
       if (op != ORC_OP_WALL_PRESSURE || tq == ORC_FLUID) ++pairs;
-      /* The kernel pieces on a hit (kernels.jl:108-195 are @fastmath; this
-       * is the one evaluation order both implementations use): x = r (1/h),
-       * t = 1 - x (0 beyond the support), W = (C_w t^4)(1 + 4x),
-       * rDW = C_r t^3, with the particle mass folded into the constants and
-       * the sums formed with fused multiply-adds. */
-      const double x = r * s->inv_h;
-      const double t = x > 1.0 ? 0.0 : 1.0 - x;
+      /* the kernel pieces on a hit (ker_w / ker_rdw above) at the kernel
+       * distance, with the particle mass folded into the constants and the
+       * sums formed with fused multiply-adds */
+      const double rk = ker_r(d);
+      const double t = ker_t(s, rk);
       const double t2 = t * t;
       if (op == ORC_OP_DENSITY || op == ORC_OP_DENSITY_REF) {
-        acc = fma(s->mcw * (t2 * t2), fma(4.0, x, 1.0), acc); /* + m W */
+        acc = fma(s->mcw * (t2 * t2), fma(-4.0, t, 5.0), acc); /* + m W */
       } else if (op == ORC_OP_WALL_PRESSURE) {
         if (tq == ORC_FLUID) {
-          const double w = (s->cw * (t2 * t2)) * fma(4.0, x, 1.0);
+          const double w = (s->cw * (t2 * t2)) * fma(-4.0, t, 5.0);
           const double gd = fma(g[2], d[2], fma(g[1], d[1], g[0] * d[0]));
           wp = fma(s->P[q], w, wp);
           wg = fma(s->rho[q] * gd, w, wg);
@@ -356,13 +360,13 @@ static int64_t binary_one(orc_system* s, int op, int64_t p) {
         if (vdx < 0.0) {
           /* Monaghan: -alpha c0 mu / rho_bar, mu = h v.x / (r^2 + eta^2),
            * r^2 as r r, the quotient as a product with the reciprocal */
-          pi = ((s->ca * vdx) * (1.0 / (r * r + s->eta2))) * inv_rb;
+          pi = ((s->ca * vdx) * (1.0 / (rk * rk + s->eta2))) * inv_rb;
         }
         const double cf = -ker * ((prp + s->Pr[q]) + pi);
         ax = fma(cf, d[0], ax);
         ay = fma(cf, d[1], ay);
         az = fma(cf, d[2], az);
-        const double wx = ((s->mcw * (t2 * t2)) * fma(4.0, x, 1.0)) * inv_rb; /* m W / rho_bar */
+        const double wx = ((s->mcw * (t2 * t2)) * fma(-4.0, t, 5.0)) * inv_rb; /* m W / rho_bar */
         sx = fma(-wx, dv0, sx); /* + wx (v_q - v_p) */
         sy = fma(-wx, dv1, sy);
         sz = fma(-wx, dv2, sz);

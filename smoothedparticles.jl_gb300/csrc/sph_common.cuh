@@ -147,12 +147,6 @@ __device__ __forceinline__ void decode_key(const Geometry& g, int key, int& cx, 
   cz = t / l1;
 }
 
-// x > 1 for x >= +0 (x = r / h), as an integer comparison of the bit patterns
-// (IEEE order equals integer order for non-negative doubles): no FP64 slot
-__device__ __forceinline__ bool gt1(double x) {
-  return __double_as_longlong(x) > 0x3FF0000000000000LL;
-}
-
 // v < 0.0 exactly (false for -0 and NaN), on the integer pipe
 __device__ __forceinline__ bool lt0(double v) {
   const long long b = __double_as_longlong(v);
@@ -170,22 +164,22 @@ __device__ __forceinline__ double two_over(double y) {
   return (e >= 1 && e <= 0x7FD) ? __longlong_as_double(b + (1LL << 52)) : __ddiv_rn(2.0, y);
 }
 
-// kernels.jl:108-115 / :156-163 in the evaluation order written in the oracle
-__device__ __forceinline__ double ker_w(const Consts& k, double r) {
-  const double x = r * k.inv_h;
-  if (x > 1.0) return 0.0;
-  const double t = 1.0 - x;
-  const double t2 = t * t;
-  const double t4 = t2 * t2;
-  return (k.cw * t4) * (1.0 + 4.0 * x);
+// The Wendland quintic and its derivative over r (kernels.jl:108-195, which
+// are @fastmath) in the one evaluation order the CPU restatement also uses:
+// t = 1 - r (1/h) as one fused operation, 0 beyond the support,
+// W = (C_w t^4)(5 - 4t) (5 - 4t = 1 + 4x), rDW = C_r t^3.
+__device__ __forceinline__ double ker_t(const Consts& k, double r) {
+  const double t = __fma_rn(-r, k.inv_h, 1.0);
+  return lt0(t) ? 0.0 : t;
 }
-// kernels.jl:140-147 / :188-195
-__device__ __forceinline__ double ker_rdw(const Consts& k, double r) {
-  const double x = r * k.inv_h;
-  if (x > 1.0) return 0.0;
-  const double t = 1.0 - x;
+__device__ __forceinline__ double ker_w(const Consts& k, double r) {
+  const double t = ker_t(k, r);
   const double t2 = t * t;
-  return k.cr * (t2 * t);
+  return (k.cw * (t2 * t2)) * __fma_rn(-4.0, t, 5.0);
+}
+__device__ __forceinline__ double ker_rdw(const Consts& k, double r) {
+  const double t = ker_t(k, r);
+  return k.cr * ((t * t) * t);
 }
 
 // structs.jl:97-106 for an arbitrary point: -1 when a coordinate is NaN,

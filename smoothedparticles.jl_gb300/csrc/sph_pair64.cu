@@ -34,18 +34,20 @@ namespace sphgpu {
 namespace {
 
 
+// d = x_p - x_q and the kernel distance sqrt((d0 d0 + d1 d1) + d2 d2) with the
+// sum fused (the support test, within_rn, keeps the reference's unfused form)
 template <int DIM>
-__device__ __forceinline__ double dist2_64(const State& s, const double* xp, int q, double* d) {
+__device__ __forceinline__ double kdist64(const State& s, const double* xp, int q, double* d) {
   d[0] = xp[0] - __ldg(&s.x[0][q]);
   d[1] = xp[1] - __ldg(&s.x[1][q]);
-  double ss = d[0] * d[0] + d[1] * d[1];
+  double ss = __fma_rn(d[1], d[1], d[0] * d[0]);
   if (DIM == 3) {
     d[2] = xp[2] - __ldg(&s.x[2][q]);
-    ss = ss + d[2] * d[2];
+    ss = __fma_rn(d[2], d[2], ss);
   } else {
     d[2] = 0.0;
   }
-  return ss;
+  return sqrt(ss);
 }
 
 // The operator bodies on a hit, in FP64 (list entry = q | neighbour cell << 27;
@@ -89,23 +91,21 @@ struct Proc64 {
         d[2] = DIM == 3 ? xp[2] - __ldg(&s.x[2][q]) : 0.0;
         r = __ldg(&rmem[(size_t)j * stride]);
       } else {
-        r = sqrt(dist2_64<DIM>(s, xp, q, d));
+        r = kdist64<DIM>(s, xp, q, d);
         if ((OP == SPH_OP_DENSITY || OP == SPH_OP_DENSITY_REF) && rmode == 1)
           rmem[(size_t)j * stride] = r;
       }
       const bool fluid = OP != SPH_OP_FORCE || __ldg(&s.type[q]) == kFluid;
       if (fluid) ++c0; else ++c1;
-      // kernel pieces in the oracle's order: x = r (1/h), t = 1 - x (0 beyond
-      // the support); W = (C_w t^4)(1 + 4x), rDW = C_r t^3; mass folded into
-      // the constants; sums with fused multiply-adds
-      const double x = r * k.inv_h;
-      const double t = gt1(x) ? 0.0 : 1.0 - x;
+      // kernel pieces in the oracle's order (ker_w / ker_rdw), mass folded
+      // into the constants, sums with fused multiply-adds
+      const double t = ker_t(k, r);
       const double t2 = t * t;
       if (OP == SPH_OP_DENSITY || OP == SPH_OP_DENSITY_REF) {
-        acc = __fma_rn(k.mcw * (t2 * t2), __fma_rn(4.0, x, 1.0), acc);
+        acc = __fma_rn(k.mcw * (t2 * t2), __fma_rn(-4.0, t, 5.0), acc);
       } else if (OP == SPH_OP_WALL_PRESSURE) {
         // Adami, Hu & Adams (2012) wall pressure, g . (x_w - x_f)
-        const double w = (k.cw * (t2 * t2)) * __fma_rn(4.0, x, 1.0);
+        const double w = (k.cw * (t2 * t2)) * __fma_rn(-4.0, t, 5.0);
         double gd = __fma_rn(k.g[1], d[1], k.g[0] * d[0]);
         if (DIM == 3) gd = __fma_rn(k.g[2], d[2], gd);
         wp = __fma_rn(__ldg(&s.P[q]), w, wp);
@@ -135,7 +135,7 @@ struct Proc64 {
         ax = __fma_rn(cf, d[0], ax);
         ay = __fma_rn(cf, d[1], ay);
         if (DIM == 3) az = __fma_rn(cf, d[2], az);
-        const double wx = ((k.mcw * (t2 * t2)) * __fma_rn(4.0, x, 1.0)) * inv_rb;
+        const double wx = ((k.mcw * (t2 * t2)) * __fma_rn(-4.0, t, 5.0)) * inv_rb;
         sx = __fma_rn(-wx, dv0, sx);
         sy = __fma_rn(-wx, dv1, sy);
         if (DIM == 3) sz = __fma_rn(-wx, dv2, sz);
