@@ -350,6 +350,7 @@ def run_ensemble(args, torch, dev):
     table = autotune.tune_batch(mem, steps=4)
     t_tune = time.perf_counter() - t0
     b = sphgpu.Batch(mem)
+    autotune.apply(mem, table, b)
     b.step(2 * max(2, (args.warmup + 1) // 2))
     b.synchronize()
     for g in mem:
@@ -390,7 +391,10 @@ def run_ensemble(args, torch, dev):
         "member_steps_per_s": len(cases) * S / (ms * 1e-3),
         "particle_steps_per_s": sum(n) * S / (ms * 1e-3),
         "graph": {"kernels_per_graph": bst["kernels_per_graph"], "steps_per_graph": 2,
-                  "graph_launches_timed": S // 2, "kernels_timed": bst["kernels"] - l0},
+                  "graph_launches_timed": S // 2, "kernels_timed": bst["kernels"] - l0,
+                  "fused": b.fused,
+                  "note": ("fused steps: each kernel of the step is one launch over all members"
+                           if b.fused else "one graph branch per member")},
         "unbatched": {"value": pairs_plain / t_plain, "ms_per_step": 1e3 * t_plain / S,
                       "note": "same members, sph_step per member on its own stream, host timer"},
         "autotune": {str(k): {"warps_per_block": v[0],

@@ -306,6 +306,14 @@ int sph_batch_destroy(sph_batch* batch);
 const char* sph_batch_last_error(const sph_batch* batch);
 int sph_batch_step(sph_batch* batch, int nsteps);
 int sph_batch_synchronize(sph_batch* batch);
+/* Fused steps (default when every member is mixed precision and of one
+ * dimension): each kernel of the step is one launch over all members, so a
+ * graph holds ~44 kernels for two steps whatever the member count; off: one
+ * graph branch per member.  Results are the same either way. */
+int sph_batch_set_fused(sph_batch* batch, int on);
+/* Warps per block (2, 4 or 8) of the fused pair passes; without fused steps
+ * each member's own sph_set_tuning applies.  Results do not depend on it. */
+int sph_batch_set_tuning(sph_batch* batch, int warps_per_block);
 /* kernels in one captured graph, graph launches so far, kernels executed */
 int sph_batch_stats(sph_batch* batch, int64_t* kernels_per_graph, int64_t* graph_launches,
                     int64_t* kernels);

@@ -33,6 +33,13 @@ struct sph_batch {
   long long launches = 0;
   long long graph_launches = 0;
   std::string err;
+  // fused mode (mixed-precision members of one dimension): every kernel of
+  // the step is one launch over all members
+  bool fusable = false;
+  bool fused = false;
+  int fused_warps = 4;  // warps per block of the fused pair passes
+  void* fdev = nullptr;  // device copy of the member arguments and block tables
+  long long counted = 0;  // kernels counted while capturing
 };
 
 namespace {
@@ -1000,9 +1007,105 @@ static void batch_drop_graph(sph_batch* b) {
   b->graph = nullptr;
 }
 
+static void batch_hook(void* owner, int, int phase, int kernels) {
+  if (phase == 1) ((sph_batch*)owner)->counted += kernels;
+}
+
+// Two steps of every member as one launch per kernel (sph_bin.cu, sph_pair32.cu,
+// sph_unary.cu): argument arrays [0] (cur -> alt as the members hold them) and
+// [1] (swapped); step 0 bins with [0] and runs the passes on [1], step 1 the
+// other way round, so the ping-pong ends where it started, as two sph_steps do.
+static int batch_capture_fused(sph_batch* b) {
+  const int M = (int)b->members.size();
+  std::vector<MemberArgs> args[2];
+  for (int j = 0; j < M; ++j) {
+    sph_system* m = b->members[j];
+    MemberArgs a{};
+    a.cur = m->cur;
+    a.alt = m->alt;
+    a.g = m->geo;
+    a.k = m->k;
+    a.b = m->b;
+    a.cap = m->n_host;
+    args[0].push_back(a);
+    std::swap(a.cur, a.alt);
+    args[1].push_back(a);
+  }
+  std::vector<int2> maps[kShapeCount];
+  for (int sh = 0; sh < kShapeCount; ++sh)
+    for (int j = 0; j < M; ++j) {
+      const sph_system* m = b->members[j];
+      const int nb = fused_blocks(sh, m->n_host, m->geo.key_max, m->b.max_items, b->fused_warps);
+      for (int i = 0; i < nb; ++i) maps[sh].push_back(make_int2(j, i));
+    }
+  size_t bytes = 2 * align_up(sizeof(MemberArgs) * M);
+  for (int sh = 0; sh < kShapeCount; ++sh) bytes += align_up(sizeof(int2) * maps[sh].size());
+  if (b->fdev) cudaFree(b->fdev);
+  b->fdev = nullptr;
+  if (cudaMalloc(&b->fdev, bytes) != cudaSuccess) {
+    cudaGetLastError();
+    return bfail(b, SPH_ERR_NOMEM, "cannot allocate the fused batch tables");
+  }
+  char* p = (char*)b->fdev;
+  FusedBatch fb{};
+  for (int q = 0; q < 2; ++q) {
+    if (cudaMemcpy(p, args[q].data(), sizeof(MemberArgs) * M, cudaMemcpyHostToDevice) != cudaSuccess)
+      return bfail(b, SPH_ERR_CUDA, "copying the member arguments failed");
+    fb.args[q] = (const MemberArgs*)p;
+    p += align_up(sizeof(MemberArgs) * M);
+  }
+  for (int sh = 0; sh < kShapeCount; ++sh) {
+    if (cudaMemcpy(p, maps[sh].data(), sizeof(int2) * maps[sh].size(), cudaMemcpyHostToDevice) !=
+        cudaSuccess)
+      return bfail(b, SPH_ERR_CUDA, "copying the block tables failed");
+    fb.map[sh] = (const int2*)p;
+    fb.blocks[sh] = (int)maps[sh].size();
+    p += align_up(sizeof(int2) * maps[sh].size());
+  }
+  fb.members = M;
+  fb.dim = b->members[0]->params.dim;
+  fb.warps = b->fused_warps;
+  cudaError_t e = cudaStreamBeginCapture(b->origin, cudaStreamCaptureModeThreadLocal);
+  if (e != cudaSuccess) return bfail(b, SPH_ERR_CUDA, "cudaStreamBeginCapture failed");
+  b->counted = 0;
+  const LaunchCtx c{b->origin, b, batch_hook};
+  for (int step = 0; step < 2 && e == cudaSuccess; ++step) {
+    const int q = 1 - step;  // the passes work on the gather's destination
+    e = launch_fused_binning(c, fb, step);
+    if (e == cudaSuccess) e = launch_fused_pair(c, fb, q, SPH_OP_DENSITY, 1, 1, 1, 1);
+    if (e == cudaSuccess) e = launch_fused_pair(c, fb, q, SPH_OP_WALL_PRESSURE, 0, 0, 0, 0);
+    if (e == cudaSuccess) e = launch_fused_pair(c, fb, q, SPH_OP_FORCE, 0, 1, 0, 2);
+    if (e == cudaSuccess) e = launch_fused_unary(c, fb, q, SPH_OP_KICK);
+  }
+  cudaGraph_t g = nullptr;
+  const cudaError_t e2 = cudaStreamEndCapture(b->origin, &g);
+  if (e != cudaSuccess || e2 != cudaSuccess || !g) {
+    cudaGetLastError();
+    if (g) cudaGraphDestroy(g);
+    return bfail(b, SPH_ERR_CUDA, "capturing the fused steps failed");
+  }
+  b->graph = g;
+  if (cudaGraphInstantiate(&b->exec, g, 0) != cudaSuccess) {
+    cudaGetLastError();
+    batch_drop_graph(b);
+    return bfail(b, SPH_ERR_CUDA, "cudaGraphInstantiate failed");
+  }
+  b->kernels_per_graph = b->counted;
+  // the members' host-side view after two steps (sph_step's flags)
+  for (int j = 0; j < M; ++j) {
+    sph_system* m = b->members[j];
+    m->cells_valid = true;
+    m->aux_fluid = m->aux_wall = true;
+    m->lists_valid = true;
+    b->generations[j] = m->generation;
+  }
+  return SPH_OK;
+}
+
 // Captures two fused steps of every member into one graph.
 static int batch_capture(sph_batch* b) {
   batch_drop_graph(b);
+  if (b->fused) return batch_capture_fused(b);
   std::vector<long long> before(b->members.size());
   std::vector<bool> prof(b->members.size());
   for (size_t j = 0; j < b->members.size(); ++j) {
@@ -1058,6 +1161,12 @@ int sph_batch_create(sph_system* const* members, int count, sph_batch** out) {
   }
   sph_batch* b = new sph_batch();
   b->members.assign(members, members + count);
+  b->fusable = true;
+  for (int j = 0; j < count; ++j)
+    if (members[j]->params.precision != SPH_PREC_MIXED ||
+        members[j]->params.dim != members[0]->params.dim)
+      b->fusable = false;
+  b->fused = b->fusable;
   b->generations.assign(count, -1);
   b->device = members[0]->device;
   DeviceGuard guard(b->device);
@@ -1081,6 +1190,7 @@ int sph_batch_destroy(sph_batch* b) {
   DeviceGuard guard(b->device);
   if (b->origin) cudaStreamSynchronize(b->origin);
   batch_drop_graph(b);
+  if (b->fdev) cudaFree(b->fdev);
   for (auto e : b->joins)
     if (e) cudaEventDestroy(e);
   if (b->fork) cudaEventDestroy(b->fork);
@@ -1131,6 +1241,28 @@ int sph_batch_step(sph_batch* b, int nsteps) {
       b->launches += m->total_launches - l0;
       m->total_launches = l0;
     }
+  }
+  return SPH_OK;
+}
+
+int sph_batch_set_fused(sph_batch* b, int on) {
+  if (!b) return SPH_ERR_ARG;
+  if (on && !b->fusable)
+    return bfail(b, SPH_ERR_UNSUPPORTED, "fused steps need mixed-precision members of one dimension");
+  if ((on != 0) != b->fused) {
+    b->fused = on != 0;
+    batch_drop_graph(b);  // captured again on the next step
+  }
+  return SPH_OK;
+}
+
+int sph_batch_set_tuning(sph_batch* b, int warps_per_block) {
+  if (!b) return SPH_ERR_ARG;
+  if (warps_per_block != 2 && warps_per_block != 4 && warps_per_block != 8)
+    return bfail(b, SPH_ERR_ARG, "warps per block must be 2, 4 or 8");
+  if (warps_per_block != b->fused_warps) {
+    b->fused_warps = warps_per_block;
+    if (b->fused) batch_drop_graph(b);
   }
   return SPH_OK;
 }

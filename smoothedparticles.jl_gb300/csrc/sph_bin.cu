@@ -29,10 +29,9 @@ namespace {
 constexpr int kThreads = 256;
 
 template <int DIM>
-__global__ void __launch_bounds__(kThreads) bin_keys_kernel(State s, Geometry g, Consts k,
-                                                            BinScratch b, int step_mode) {
+__device__ __forceinline__ void bin_keys_body(const State& s, const Geometry& g, const Consts& k, const BinScratch& b, int step_mode, int blk) {
   const int n = *b.d_n;
-  const int i = blockIdx.x * kThreads + threadIdx.x;
+  const int i = blk * kThreads + threadIdx.x;
   if (i >= n) return;
   double x[3];
   x[0] = s.x[0][i];
@@ -83,6 +82,12 @@ __global__ void __launch_bounds__(kThreads) bin_keys_kernel(State s, Geometry g,
   b.slots[i] = base + __popc(peers & lanemask_lt());
 }
 
+template <int DIM>
+__global__ void __launch_bounds__(kThreads) bin_keys_kernel(State s, Geometry g, Consts k,
+                                                            BinScratch b, int step_mode) {
+  bin_keys_body<DIM>(s, g, k, b, step_mode, blockIdx.x);
+}
+
 // Block-wide exclusive scan of one int per thread (blockDim.x == 1024 or a
 // multiple of 32); returns the exclusive prefix, *total gets the block sum.
 __device__ __forceinline__ int block_exclusive_scan(int v, int* warp_sums, int* total) {
@@ -116,7 +121,7 @@ __device__ __forceinline__ int block_exclusive_scan(int v, int* warp_sums, int* 
 }
 
 // core.jl:71-81 replayed on reference indices (one CTA of 1024 threads).
-__global__ void __launch_bounds__(1024) bin_remove_kernel(BinScratch b) {
+__device__ __forceinline__ void bin_remove_body(const BinScratch& b, int blk) {
   const int k = *b.d_nrem;
   if (k == 0) return;
   const int N = *b.d_n;
@@ -151,9 +156,13 @@ __global__ void __launch_bounds__(1024) bin_remove_kernel(BinScratch b) {
   }
 }
 
-__global__ void __launch_bounds__(kThreads) bin_scatter_kernel(State s, Geometry g, BinScratch b) {
+__global__ void __launch_bounds__(1024) bin_remove_kernel(BinScratch b) {
+  bin_remove_body(b, blockIdx.x);
+}
+
+__device__ __forceinline__ void bin_scatter_body(const State& s, const Geometry& g, const BinScratch& b, int blk) {
   const int n = *b.d_n;
-  const int i = blockIdx.x * kThreads + threadIdx.x;
+  const int i = blk * kThreads + threadIdx.x;
   if (i >= n) return;
   const int key = b.keys[i];
   const int dst = b.cell_start[key] + b.slots[i];
@@ -164,11 +173,15 @@ __global__ void __launch_bounds__(kThreads) bin_scatter_kernel(State s, Geometry
   b.rid_tmp[dst] = rid;
 }
 
+__global__ void __launch_bounds__(kThreads) bin_scatter_kernel(State s, Geometry g, BinScratch b) {
+  bin_scatter_body(s, g, b, blockIdx.x);
+}
+
 // One warp per cell: slot of element e = number of elements of the cell with
 // a larger reference index (reference indices are unique).
-__global__ void __launch_bounds__(kThreads) bin_rank_kernel(Geometry g, BinScratch b) {
+__device__ __forceinline__ void bin_rank_body(const Geometry& g, const BinScratch& b, int blk) {
   const int lane = threadIdx.x & 31;
-  const int cell = blockIdx.x * (kThreads / 32) + (threadIdx.x >> 5) + 1;
+  const int cell = blk * (kThreads / 32) + (threadIdx.x >> 5) + 1;
   if (cell > g.key_max) return;
   const int st = b.cell_start[cell];
   const int en = b.cell_start[cell + 1];
@@ -194,12 +207,14 @@ __global__ void __launch_bounds__(kThreads) bin_rank_kernel(Geometry g, BinScrat
   }
 }
 
+__global__ void __launch_bounds__(kThreads) bin_rank_kernel(Geometry g, BinScratch b) {
+  bin_rank_body(g, b, blockIdx.x);
+}
+
 template <int DIM>
-__global__ void __launch_bounds__(kThreads) bin_gather_kernel(State cur, State alt, Geometry g,
-                                                              Consts k, BinScratch b,
-                                                              int gather_all) {
+__device__ __forceinline__ void bin_gather_body(const State& cur, const State& alt, const Geometry& g, const Consts& k, const BinScratch& b, int gather_all, int blk) {
   const int n_new = b.cell_start[g.key_max + 1];
-  const int dst = blockIdx.x * kThreads + threadIdx.x;
+  const int dst = blk * kThreads + threadIdx.x;
   if (dst == 0) *b.d_n = n_new;
   if (dst >= n_new) return;
   const int src = b.perm[dst];
@@ -243,17 +258,28 @@ __global__ void __launch_bounds__(kThreads) bin_gather_kernel(State cur, State a
   }
 }
 
+template <int DIM>
+__global__ void __launch_bounds__(kThreads) bin_gather_kernel(State cur, State alt, Geometry g,
+                                                              Consts k, BinScratch b,
+                                                              int gather_all) {
+  bin_gather_body<DIM>(cur, alt, g, k, b, gather_all, blockIdx.x);
+}
+
 // ---- pair-pass work list: cell k gets ceil(c_k / 32) items of <= 32 targets
-__global__ void __launch_bounds__(kThreads) items_count_kernel(Geometry g, BinScratch b) {
-  const int k = blockIdx.x * kThreads + threadIdx.x;  // 0 .. key_max + 2
+__device__ __forceinline__ void items_count_body(const Geometry& g, const BinScratch& b, int blk) {
+  const int k = blk * kThreads + threadIdx.x;  // 0 .. key_max + 2
   if (k > g.key_max + 2) return;
   int c = 0;
   if (k >= 1 && k <= g.key_max) c = (b.cell_start[k + 1] - b.cell_start[k] + 31) >> 5;
   b.counts[k] = c;  // the bucket counts are no longer needed once the starts exist
 }
 
-__global__ void __launch_bounds__(kThreads) items_write_kernel(Geometry g, BinScratch b) {
-  const int k = blockIdx.x * kThreads + threadIdx.x + 1;
+__global__ void __launch_bounds__(kThreads) items_count_kernel(Geometry g, BinScratch b) {
+  items_count_body(g, b, blockIdx.x);
+}
+
+__device__ __forceinline__ void items_write_body(const Geometry& g, const BinScratch& b, int blk) {
+  const int k = blk * kThreads + threadIdx.x + 1;
   if (k > g.key_max) return;
   const int st = b.cell_start[k];
   const int c = b.cell_start[k + 1] - st;
@@ -261,11 +287,15 @@ __global__ void __launch_bounds__(kThreads) items_write_kernel(Geometry g, BinSc
   for (int t = 0; t < c; t += 32, ++off) b.items[off] = make_int2(st + t, min(32, c - t));
 }
 
+__global__ void __launch_bounds__(kThreads) items_write_kernel(Geometry g, BinScratch b) {
+  items_write_body(g, b, blockIdx.x);
+}
+
 // ---- mask slots of the mixed-precision pair passes: every item of a cell
 // with fluid gets one slot per 32-candidate chunk of the cell's neighbour
 // cells (the chunk sequence of the pair traversal)
-__global__ void __launch_bounds__(kThreads) chunks_count_kernel(Geometry g, BinScratch b) {
-  const int k = blockIdx.x * kThreads + threadIdx.x;  // 0 .. key_max + 2
+__device__ __forceinline__ void chunks_count_body(const Geometry& g, const BinScratch& b, int blk) {
+  const int k = blk * kThreads + threadIdx.x;  // 0 .. key_max + 2
   if (k > g.key_max + 2) return;
   int v = 0;
   if (k >= 1 && k <= g.key_max && b.cell_fluid[k] > 0) {
@@ -279,14 +309,18 @@ __global__ void __launch_bounds__(kThreads) chunks_count_kernel(Geometry g, BinS
   b.counts[k] = v;  // the item counts are no longer needed once items exist
 }
 
+__global__ void __launch_bounds__(kThreads) chunks_count_kernel(Geometry g, BinScratch b) {
+  chunks_count_body(g, b, blockIdx.x);
+}
+
 // ---- generic exclusive scan (3 kernels)
 constexpr int kScanThreads = 512;
 constexpr int kScanItems = 8;
 constexpr int kScanTile = kScanThreads * kScanItems;
 
-__global__ void __launch_bounds__(kScanThreads) scan_reduce_kernel(const int* in, int len, int* tmp) {
+__device__ __forceinline__ void scan_reduce_body(const int* in, int len, int* tmp, int blk) {
   __shared__ int warp_sums[33];
-  const int base = blockIdx.x * kScanTile;
+  const int base = blk * kScanTile;
   int v = 0;
 #pragma unroll
   for (int t = 0; t < kScanItems; ++t) {
@@ -295,10 +329,14 @@ __global__ void __launch_bounds__(kScanThreads) scan_reduce_kernel(const int* in
   }
   int total;
   block_exclusive_scan(v, warp_sums, &total);
-  if (threadIdx.x == 0) tmp[blockIdx.x] = total;
+  if (threadIdx.x == 0) tmp[blk] = total;
 }
 
-__global__ void __launch_bounds__(1024) scan_blocks_kernel(int* tmp, int nblocks) {
+__global__ void __launch_bounds__(kScanThreads) scan_reduce_kernel(const int* in, int len, int* tmp) {
+  scan_reduce_body(in, len, tmp, blockIdx.x);
+}
+
+__device__ __forceinline__ void scan_blocks_body(int* tmp, int nblocks, int blk) {
   __shared__ int warp_sums[33];
   int carry = 0;
   for (int base = 0; base < nblocks; base += blockDim.x) {
@@ -311,10 +349,13 @@ __global__ void __launch_bounds__(1024) scan_blocks_kernel(int* tmp, int nblocks
   }
 }
 
-__global__ void __launch_bounds__(kScanThreads) scan_apply_kernel(const int* in, int* out, int len,
-                                                                  const int* tmp) {
+__global__ void __launch_bounds__(1024) scan_blocks_kernel(int* tmp, int nblocks) {
+  scan_blocks_body(tmp, nblocks, blockIdx.x);
+}
+
+__device__ __forceinline__ void scan_apply_body(const int* in, int* out, int len, const int* tmp, int blk) {
   __shared__ int warp_sums[33];
-  const int base = blockIdx.x * kScanTile + threadIdx.x * kScanItems;
+  const int base = blk * kScanTile + threadIdx.x * kScanItems;
   int vals[kScanItems];
   int sum = 0;
 #pragma unroll
@@ -324,7 +365,7 @@ __global__ void __launch_bounds__(kScanThreads) scan_apply_kernel(const int* in,
     sum += vals[t];
   }
   int total;
-  int run = block_exclusive_scan(sum, warp_sums, &total) + tmp[blockIdx.x];
+  int run = block_exclusive_scan(sum, warp_sums, &total) + tmp[blk];
 #pragma unroll
   for (int t = 0; t < kScanItems; ++t) {
     const int idx = base + t;
@@ -333,7 +374,173 @@ __global__ void __launch_bounds__(kScanThreads) scan_apply_kernel(const int* in,
   }
 }
 
+__global__ void __launch_bounds__(kScanThreads) scan_apply_kernel(const int* in, int* out, int len,
+                                                                  const int* tmp) {
+  scan_apply_body(in, out, len, tmp, blockIdx.x);
+}
+
+// ---- fused batches: the same bodies, one launch over all members; block i
+// of a shape works on map[i] = (member, block of that member)
+struct FusedArgs {
+  const MemberArgs* __restrict__ m;
+  const int2* __restrict__ map;
+};
+
+__device__ __forceinline__ const MemberArgs& fused_member(const FusedArgs& f, int2& e) {
+  e = f.map[blockIdx.x];
+  return f.m[e.x];
+}
+
+__global__ void __launch_bounds__(kThreads) fused_clear_kernel(FusedArgs f) {
+  int2 e;
+  const MemberArgs& m = fused_member(f, e);
+  const int k = e.y * kThreads + threadIdx.x;
+  if (k < m.g.key_max + 3) {
+    m.b.counts[k] = 0;
+    m.b.cell_fluid[k] = 0;
+  }
+  if (e.y == 0 && threadIdx.x == 0) *m.b.d_nrem = 0;
+}
+
+template <int DIM>
+__global__ void __launch_bounds__(kThreads) fused_keys_kernel(FusedArgs f) {
+  int2 e;
+  const MemberArgs& m = fused_member(f, e);
+  bin_keys_body<DIM>(m.cur, m.g, m.k, m.b, 1, e.y);
+}
+
+__global__ void __launch_bounds__(1024) fused_remove_kernel(FusedArgs f) {
+  int2 e;
+  const MemberArgs& m = fused_member(f, e);
+  bin_remove_body(m.b, e.y);
+}
+
+// which: 0 counts -> cell_start, 1 counts -> item_off, 2 counts -> chunk_off
+__device__ __forceinline__ int* fused_scan_out(const MemberArgs& m, int which) {
+  return which == 0 ? m.b.cell_start : which == 1 ? m.b.item_off : m.b.chunk_off;
+}
+
+__global__ void __launch_bounds__(kScanThreads) fused_scan_reduce_kernel(FusedArgs f) {
+  int2 e;
+  const MemberArgs& m = fused_member(f, e);
+  scan_reduce_body(m.b.counts, m.g.key_max + 3, m.b.scan_tmp, e.y);
+}
+
+__global__ void __launch_bounds__(1024) fused_scan_blocks_kernel(FusedArgs f) {
+  int2 e;
+  const MemberArgs& m = fused_member(f, e);
+  scan_blocks_body(m.b.scan_tmp, (m.g.key_max + 3 + kScanTile - 1) / kScanTile, e.y);
+}
+
+__global__ void __launch_bounds__(kScanThreads) fused_scan_apply_kernel(FusedArgs f, int which) {
+  int2 e;
+  const MemberArgs& m = fused_member(f, e);
+  scan_apply_body(m.b.counts, fused_scan_out(m, which), m.g.key_max + 3, m.b.scan_tmp, e.y);
+}
+
+__global__ void __launch_bounds__(kThreads) fused_scatter_kernel(FusedArgs f) {
+  int2 e;
+  const MemberArgs& m = fused_member(f, e);
+  bin_scatter_body(m.cur, m.g, m.b, e.y);
+}
+
+__global__ void __launch_bounds__(kThreads) fused_rank_kernel(FusedArgs f) {
+  int2 e;
+  const MemberArgs& m = fused_member(f, e);
+  bin_rank_body(m.g, m.b, e.y);
+}
+
+__global__ void __launch_bounds__(kThreads) fused_items_count_kernel(FusedArgs f) {
+  int2 e;
+  const MemberArgs& m = fused_member(f, e);
+  items_count_body(m.g, m.b, e.y);
+}
+
+__global__ void __launch_bounds__(kThreads) fused_items_write_kernel(FusedArgs f) {
+  int2 e;
+  const MemberArgs& m = fused_member(f, e);
+  items_write_body(m.g, m.b, e.y);
+}
+
+template <int DIM>
+__global__ void __launch_bounds__(kThreads) fused_gather_kernel(FusedArgs f) {
+  int2 e;
+  const MemberArgs& m = fused_member(f, e);
+  bin_gather_body<DIM>(m.cur, m.alt, m.g, m.k, m.b, kGatherStep, e.y);
+}
+
+__global__ void __launch_bounds__(kThreads) fused_chunks_count_kernel(FusedArgs f) {
+  int2 e;
+  const MemberArgs& m = fused_member(f, e);
+  chunks_count_body(m.g, m.b, e.y);
+}
+
 }  // namespace
+
+int fused_blocks(int shape, int cap, int key_max, int max_items, int warps) {
+  const int nb = key_max + 3;
+  switch (shape) {
+    case kShapeParticles: return (cap + kThreads - 1) / kThreads;
+    case kShapeBuckets: return (nb + kThreads - 1) / kThreads;
+    case kShapeCells: return (key_max + kThreads - 1) / kThreads;
+    case kShapeRank: return (key_max + (kThreads / 32) - 1) / (kThreads / 32);
+    case kShapeScanTiles: return (nb + kScanTile - 1) / kScanTile;
+    case kShapeMember: return 1;
+    case kShapeItems: return (max_items + warps - 1) / warps;
+    default: return 0;
+  }
+}
+
+// The binning of one fused step (launch_binning for every member): members'
+// state args[p].cur -> args[p].alt.
+cudaError_t launch_fused_binning(const LaunchCtx& c, const FusedBatch& fb, int p) {
+  auto fa = [&](int shape) { return FusedArgs{fb.args[p], fb.map[shape]}; };
+  auto grid = [&](int shape) { return (unsigned)fb.blocks[shape]; };
+  cudaStream_t st = c.stream;
+  mark(c, SPH_KERNEL_BIN_KEYS, 0);
+  fused_clear_kernel<<<grid(kShapeBuckets), kThreads, 0, st>>>(fa(kShapeBuckets));
+  if (fb.dim == 2)
+    fused_keys_kernel<2><<<grid(kShapeParticles), kThreads, 0, st>>>(fa(kShapeParticles));
+  else
+    fused_keys_kernel<3><<<grid(kShapeParticles), kThreads, 0, st>>>(fa(kShapeParticles));
+  mark(c, SPH_KERNEL_BIN_KEYS, 1, 2);
+  mark(c, SPH_KERNEL_BIN_REMOVE, 0);
+  fused_remove_kernel<<<grid(kShapeMember), 1024, 0, st>>>(fa(kShapeMember));
+  mark(c, SPH_KERNEL_BIN_REMOVE, 1);
+  auto scan = [&](int which) {
+    mark(c, SPH_KERNEL_BIN_SCAN, 0);
+    fused_scan_reduce_kernel<<<grid(kShapeScanTiles), kScanThreads, 0, st>>>(fa(kShapeScanTiles));
+    fused_scan_blocks_kernel<<<grid(kShapeMember), 1024, 0, st>>>(fa(kShapeMember));
+    fused_scan_apply_kernel<<<grid(kShapeScanTiles), kScanThreads, 0, st>>>(fa(kShapeScanTiles),
+                                                                             which);
+    mark(c, SPH_KERNEL_BIN_SCAN, 1, 3);
+  };
+  scan(0);
+  mark(c, SPH_KERNEL_BIN_SCATTER, 0);
+  fused_scatter_kernel<<<grid(kShapeParticles), kThreads, 0, st>>>(fa(kShapeParticles));
+  mark(c, SPH_KERNEL_BIN_SCATTER, 1);
+  mark(c, SPH_KERNEL_BIN_RANK, 0);
+  fused_rank_kernel<<<grid(kShapeRank), kThreads, 0, st>>>(fa(kShapeRank));
+  mark(c, SPH_KERNEL_BIN_RANK, 1);
+  mark(c, SPH_KERNEL_BIN_SCAN, 0);
+  fused_items_count_kernel<<<grid(kShapeBuckets), kThreads, 0, st>>>(fa(kShapeBuckets));
+  mark(c, SPH_KERNEL_BIN_SCAN, 1);
+  scan(1);
+  mark(c, SPH_KERNEL_BIN_SCAN, 0);
+  fused_items_write_kernel<<<grid(kShapeCells), kThreads, 0, st>>>(fa(kShapeCells));
+  mark(c, SPH_KERNEL_BIN_SCAN, 1);
+  mark(c, SPH_KERNEL_BIN_GATHER, 0);
+  if (fb.dim == 2)
+    fused_gather_kernel<2><<<grid(kShapeParticles), kThreads, 0, st>>>(fa(kShapeParticles));
+  else
+    fused_gather_kernel<3><<<grid(kShapeParticles), kThreads, 0, st>>>(fa(kShapeParticles));
+  mark(c, SPH_KERNEL_BIN_GATHER, 1);
+  mark(c, SPH_KERNEL_BIN_SCAN, 0);
+  fused_chunks_count_kernel<<<grid(kShapeBuckets), kThreads, 0, st>>>(fa(kShapeBuckets));
+  mark(c, SPH_KERNEL_BIN_SCAN, 1);
+  scan(2);
+  return cudaGetLastError();
+}
 
 size_t scan_tmp_ints(int len) { return (size_t)((len + kScanTile - 1) / kScanTile) + 1; }
 

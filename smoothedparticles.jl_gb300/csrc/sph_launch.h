@@ -27,6 +27,48 @@ inline void mark(const LaunchCtx& c, int kernel, int phase, int kernels = 1) {
 constexpr int kGatherAll = 1;   // every field (create_cell_list!)
 constexpr int kGatherStep = 0;  // only what survives a fused step (x, v, rho_ref, ids)
 
+// ---- fused batches: one launch per kernel of the step for all members.
+// Members' launch arguments live in device memory; for every launch shape a
+// table gives each block its (member, block of that member).
+struct MemberArgs {
+  State cur;      // the state the step starts from
+  State alt;      // the binning's gather destination (the pair passes' state)
+  Geometry g;
+  Consts k;
+  BinScratch b;
+  int cap;        // particle capacity (the count upper bound)
+};
+
+enum FusedShape {
+  kShapeParticles = 0,  // ceil(cap / 256) blocks of 256 threads
+  kShapeBuckets,        // ceil((key_max + 3) / 256)
+  kShapeCells,          // ceil(key_max / 256)
+  kShapeRank,           // ceil(key_max / 8): one warp per cell
+  kShapeScanTiles,      // ceil((key_max + 3) / 4096): scan tiles
+  kShapeMember,         // one block per member
+  kShapeItems,          // ceil(max_items / warps): the pair passes' warps
+  kShapeCount
+};
+
+struct FusedBatch {
+  const MemberArgs* args[2];  // [0]: cur -> alt as given; [1]: cur and alt swapped
+  const int2* map[kShapeCount];
+  int blocks[kShapeCount];
+  int members;
+  int dim;
+  int warps;  // warps per block of the fused pair passes (2, 4 or 8)
+};
+
+// Blocks of each shape for one member (the single-system launch grids).
+int fused_blocks(int shape, int cap, int key_max, int max_items, int warps);
+// The binning of one fused step for every member (sph_bin.cu): args[p].cur ->
+// args[p].alt; the pair passes (sph_pair32.cu) and the kick (sph_unary.cu) of
+// the step then work on args[1 - p].cur (= args[p].alt).
+cudaError_t launch_fused_binning(const LaunchCtx& c, const FusedBatch& fb, int p);
+cudaError_t launch_fused_pair(const LaunchCtx& c, const FusedBatch& fb, int p, int op, int self,
+                              int reset, int fuse_eos, int list_mode);
+cudaError_t launch_fused_unary(const LaunchCtx& c, const FusedBatch& fb, int p, int op);
+
 // ---- binning (sph_bin.cu)
 // Whole create_cell_list!: keys (optionally with the fused kick + drift),
 // removal replay, counting sort by cell, per-cell descending reference-index

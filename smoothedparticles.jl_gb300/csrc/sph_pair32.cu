@@ -427,13 +427,13 @@ __device__ __forceinline__ void mx_pass(const State& s, const Geometry& g, const
 }
 
 template <int DIM, int OP, int WARPS>
-__global__ void __launch_bounds__(32 * WARPS) pair32_kernel(State s, Geometry g, Consts k,
-                                                            BinScratch b, int self, int reset,
-                                                            int fuse_eos, int list_mode) {
-  __shared__ MxShared<OP> shared[WARPS];
+__device__ __forceinline__ void pair32_body(const State& s, const Geometry& g, const Consts& k,
+                                            const BinScratch& b, int self, int reset,
+                                            int fuse_eos, int list_mode, int blk,
+                                            MxShared<OP>* shared) {
   const int lane = threadIdx.x & 31;
   const int w = threadIdx.x >> 5;
-  const int item = blockIdx.x * WARPS + w;
+  const int item = blk * WARPS + w;
   int first = 0, count = 0;
   if (!cw_item(b, g, item, first, count)) return;  // warp-uniform
   const int i = first + lane;
@@ -525,6 +525,68 @@ __global__ void __launch_bounds__(32 * WARPS) pair32_kernel(State s, Geometry g,
   cw_count<OP>(b, p.c0, p.c1, p.c2);
 }
 
+template <int DIM, int OP, int WARPS>
+__global__ void __launch_bounds__(32 * WARPS) pair32_kernel(State s, Geometry g, Consts k,
+                                                            BinScratch b, int self, int reset,
+                                                            int fuse_eos, int list_mode) {
+  __shared__ MxShared<OP> shared[WARPS];
+  pair32_body<DIM, OP, WARPS>(s, g, k, b, self, reset, fuse_eos, list_mode, blockIdx.x, shared);
+}
+
+// fused batches: block i works on map[i] = (member, block of that member)
+template <int DIM, int OP, int WARPS>
+__global__ void __launch_bounds__(32 * WARPS) pair32_fused_kernel(
+    const MemberArgs* __restrict__ margs, const int2* __restrict__ map, int self, int reset,
+    int fuse_eos, int list_mode) {
+  __shared__ MxShared<OP> shared[WARPS];
+  const int2 e = map[blockIdx.x];
+  const MemberArgs& m = margs[e.x];
+  pair32_body<DIM, OP, WARPS>(m.cur, m.g, m.k, m.b, self, reset, fuse_eos, list_mode, e.y,
+                              shared);
+}
+
+template <int DIM, int OP, int WARPS>
+void fused_launch(const FusedBatch& fb, int p, cudaStream_t st, int self, int reset, int fuse_eos,
+                  int list_mode) {
+  pair32_fused_kernel<DIM, OP, WARPS><<<(unsigned)fb.blocks[kShapeItems], 32 * WARPS, 0, st>>>(
+      fb.args[p], fb.map[kShapeItems], self, reset, fuse_eos, list_mode);
+}
+
+template <int DIM, int OP>
+void fused_launch_w(const FusedBatch& fb, int p, cudaStream_t st, int self, int reset,
+                    int fuse_eos, int list_mode) {
+  if (fb.warps == 2)
+    fused_launch<DIM, OP, 2>(fb, p, st, self, reset, fuse_eos, list_mode);
+  else if (fb.warps == 8)
+    fused_launch<DIM, OP, 8>(fb, p, st, self, reset, fuse_eos, list_mode);
+  else
+    fused_launch<DIM, OP, 4>(fb, p, st, self, reset, fuse_eos, list_mode);
+}
+
+template <int DIM>
+cudaError_t launch_fused_dim(const LaunchCtx& c, const FusedBatch& fb, int p, int op, int self,
+                             int reset, int fuse_eos, int list_mode) {
+  const int kid = op == SPH_OP_FORCE           ? SPH_KERNEL_FORCE
+                  : op == SPH_OP_WALL_PRESSURE ? SPH_KERNEL_WALL
+                                               : SPH_KERNEL_DENSITY;
+  mark(c, kid, 0);
+  switch (op) {
+    case SPH_OP_DENSITY:
+      fused_launch_w<DIM, SPH_OP_DENSITY>(fb, p, c.stream, self, reset, fuse_eos, 1);
+      break;
+    case SPH_OP_WALL_PRESSURE:
+      fused_launch_w<DIM, SPH_OP_WALL_PRESSURE>(fb, p, c.stream, 0, 0, 0, 0);
+      break;
+    case SPH_OP_FORCE:
+      fused_launch_w<DIM, SPH_OP_FORCE>(fb, p, c.stream, self, reset, 0, list_mode);
+      break;
+    default:
+      return cudaErrorNotSupported;
+  }
+  mark(c, kid, 1);
+  return cudaGetLastError();
+}
+
 template <int DIM>
 cudaError_t launch_dim(const LaunchCtx& c, const State& s, const Geometry& g, const Consts& k,
                        const BinScratch& b, int cap, int op, int self, int reset, int fuse_eos,
@@ -567,6 +629,12 @@ cudaError_t launch_dim(const LaunchCtx& c, const State& s, const Geometry& g, co
 }
 
 }  // namespace
+
+cudaError_t launch_fused_pair(const LaunchCtx& c, const FusedBatch& fb, int p, int op, int self,
+                              int reset, int fuse_eos, int list_mode) {
+  return fb.dim == 2 ? launch_fused_dim<2>(c, fb, p, op, self, reset, fuse_eos, list_mode)
+                     : launch_fused_dim<3>(c, fb, p, op, self, reset, fuse_eos, list_mode);
+}
 
 cudaError_t launch_pair_mixed(const LaunchCtx& c, const State& s, const Geometry& g,
                               const Consts& k, const BinScratch& b, int cap, int op, int self,

@@ -14,9 +14,10 @@ namespace {
 constexpr int kThreads = 256;
 
 template <int DIM>
-__global__ void __launch_bounds__(kThreads) unary_kernel(State s, Consts k, BinScratch b, int op) {
+__device__ __forceinline__ void unary_body(const State& s, const Consts& k, const BinScratch& b,
+                                           int op, int blk) {
   const int n = *b.d_n;
-  const int i = blockIdx.x * kThreads + threadIdx.x;
+  const int i = blk * kThreads + threadIdx.x;
   if (i >= n) return;
   const bool fluid = s.type[i] == kFluid;
   switch (op) {
@@ -80,6 +81,20 @@ __global__ void __launch_bounds__(kThreads) unary_kernel(State s, Consts k, BinS
     default:
       break;
   }
+}
+
+template <int DIM>
+__global__ void __launch_bounds__(kThreads) unary_kernel(State s, Consts k, BinScratch b, int op) {
+  unary_body<DIM>(s, k, b, op, blockIdx.x);
+}
+
+// fused batches: block i works on map[i] = (member, block of that member)
+template <int DIM>
+__global__ void __launch_bounds__(kThreads) unary_fused_kernel(const MemberArgs* __restrict__ margs,
+                                                               const int2* __restrict__ map, int op) {
+  const int2 e = map[blockIdx.x];
+  const MemberArgs& m = margs[e.x];
+  unary_body<DIM>(m.cur, m.k, m.b, op, e.y);
 }
 
 template <int DIM>
@@ -191,6 +206,17 @@ cudaError_t launch_upload(const LaunchCtx& c, const State& s, const Consts& k,
   else
     upload_kernel<3><<<blocks, kThreads, 0, c.stream>>>(s, b, n, x, v, rho, rho_ref, type);
   mark(c, SPH_KERNEL_IO, 1);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_fused_unary(const LaunchCtx& c, const FusedBatch& fb, int p, int op) {
+  mark(c, SPH_KERNEL_UNARY, 0);
+  const unsigned grid = (unsigned)fb.blocks[kShapeParticles];
+  if (fb.dim == 2)
+    unary_fused_kernel<2><<<grid, kThreads, 0, c.stream>>>(fb.args[p], fb.map[kShapeParticles], op);
+  else
+    unary_fused_kernel<3><<<grid, kThreads, 0, c.stream>>>(fb.args[p], fb.map[kShapeParticles], op);
+  mark(c, SPH_KERNEL_UNARY, 1);
   return cudaGetLastError();
 }
 

@@ -307,6 +307,9 @@ class Batch:
         if rc != 0:
             raise SphError(rc, "sph_batch_create failed (members must hold particles, one device)")
         self._h = h
+        self.fused = (len({m.precision for m in self.members}) == 1 and
+                      self.members[0].precision == MIXED and
+                      len({m.dim for m in self.members}) == 1)
 
     def _check(self, rc):
         if rc != 0:
@@ -315,6 +318,17 @@ class Batch:
 
     def step(self, nsteps: int = 2):
         self._check(self._lib.sph_batch_step(self._h, int(nsteps)))
+
+    def set_tuning(self, warps_per_block: int):
+        """Warps per block of the fused pair passes (2, 4 or 8)."""
+        self._check(self._lib.sph_batch_set_tuning(self._h, int(warps_per_block)))
+
+    def set_fused(self, on: bool):
+        """Fused steps (one launch per kernel over all members; the default
+        for mixed-precision members of one dimension) or one graph branch per
+        member.  Results are the same."""
+        self._check(self._lib.sph_batch_set_fused(self._h, 1 if on else 0))
+        self.fused = bool(on)
 
     def synchronize(self):
         self._check(self._lib.sph_batch_synchronize(self._h))

@@ -184,6 +184,8 @@ PROTOTYPES = {
     "sph_batch_synchronize": (C.c_int, [_P]),
     "sph_batch_stats": (C.c_int, [_P, C.POINTER(_I64), C.POINTER(_I64), C.POINTER(_I64)]),
     "sph_batch_stream": (C.c_int, [_P, C.POINTER(_P)]),
+    "sph_batch_set_fused": (C.c_int, [_P, C.c_int]),
+    "sph_batch_set_tuning": (C.c_int, [_P, C.c_int]),
     "sph_memory_estimate": (C.c_int, [C.POINTER(sph_params), _I64, C.POINTER(C.c_uint64)]),
     "sph_memory_usage": (C.c_int, [_P, C.POINTER(C.c_uint64)]),
     "sph_query": (C.c_int, [_P, C.POINTER(C.c_int)]),

@@ -42,6 +42,9 @@ def test_apply_table():
     sy = [_FakeSystem(3000), _FakeSystem(50000), _FakeSystem(5000)]
     autotune.apply(sy, {11: (2, {}), 15: (8, {})})
     assert [g.w for g in sy] == [2, 8, 4]
+    fused = _FakeSystem(0)           # stands in for a batch
+    autotune.apply(sy, {"fused": (8, {})}, fused)
+    assert fused.w == 8 and [g.w for g in sy] == [2, 8, 4]
 
 
 def test_memory_estimate_host_only(sph_lib):

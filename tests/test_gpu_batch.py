@@ -100,3 +100,32 @@ def test_ensemble_members_batched(gpu):
     b.synchronize()
     for m, r in zip(mem, ref):
         assert_equal(m, r)
+
+
+def test_fused_equals_branches_and_alone(gpu):
+    """Fused steps (one launch per kernel over all members) against one graph
+    branch per member and against stepping alone: identical fields."""
+    cases = [c for c in ensemble_cases(24, seed=11) if c.n < 20000][:6]
+    fused = [make(c, sphgpu.MIXED) for c in cases]
+    branch = [make(c, sphgpu.MIXED) for c in cases]
+    ref = [make(c, sphgpu.MIXED) for c in cases]
+    bf = sphgpu.Batch(fused)
+    bb = sphgpu.Batch(branch)
+    bb.set_fused(False)
+    for nsteps in (4, 5):
+        bf.step(nsteps)
+        bb.step(nsteps)
+        for r in ref:
+            r.step(nsteps)
+    bf.synchronize()
+    bb.synchronize()
+    for a, b2, r in zip(fused, branch, ref):
+        assert_equal(a, r)
+        assert_equal(b2, r)
+        assert a.pair_count() == r.pair_count()
+    kf = bf.stats()["kernels_per_graph"]
+    kb = bb.stats()["kernels_per_graph"]
+    assert kf < 60 < kb            # ~44 launches for two steps of all members
+    fp = sphgpu.Batch([make(cases[0], sphgpu.FP64)])
+    with pytest.raises(sphgpu.SphError):
+        fp.set_fused(True)         # FP64 members step as graph branches
