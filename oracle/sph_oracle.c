@@ -336,13 +336,14 @@ static int64_t binary_one(orc_system* s, int op, int64_t p) {
        * pressure only sums fluid neighbours */
       if (op != ORC_OP_WALL_PRESSURE || tq == ORC_FLUID) ++pairs;
       /* the kernel pieces on a hit (ker_w / ker_rdw above) at the kernel
-       * distance, with the particle mass folded into the constants and the
-       * sums formed with fused multiply-adds */
+       * distance, with the particle mass folded into the constants; the
+       * density adds m W rounded (a per-pair value), the other sums are
+       * formed with fused multiply-adds */
       const double rk = ker_r(d);
       const double t = ker_t(s, rk);
       const double t2 = t * t;
       if (op == ORC_OP_DENSITY || op == ORC_OP_DENSITY_REF) {
-        acc = fma(s->mcw * (t2 * t2), fma(-4.0, t, 5.0), acc); /* + m W */
+        acc = acc + (s->mcw * (t2 * t2)) * fma(-4.0, t, 5.0); /* + m W */
       } else if (op == ORC_OP_WALL_PRESSURE) {
         if (tq == ORC_FLUID) {
           const double w = (s->cw * (t2 * t2)) * fma(-4.0, t, 5.0);

@@ -156,7 +156,6 @@ size_t carve(sph_system* s, char* base, size_t C) {
   b.inv_rid = (int*)take(4 * C);
   b.max_items = max_work_items((int)C, s->geo.key_max);
   b.items = (int2*)take(8 * (size_t)b.max_items);
-  b.item_partial = (int*)take(4 * (size_t)b.max_items);
   if (s->params.precision == SPH_PREC_MIXED) {
     // hit masks: a full 3D item (32 targets, cells of ~64 particles) has 54
     // chunks, ~1.7 per particle; 2D items ~0.4 per particle.  Items beyond
@@ -165,18 +164,28 @@ size_t carve(sph_system* s, char* base, size_t C) {
     b.ck_cap = (int)(cap < 0x3ffffffLL * 16 ? cap : 0x3ffffffLL * 16);
     b.ck_mask = (unsigned*)take(4 * 32 * (size_t)b.ck_cap);
     b.hit_cap = 0;
-    b.hits = nullptr;
+    b.rows = nullptr;
     b.hit_count = nullptr;
-    b.hitr = nullptr;
+    b.roff = b.rcur = nullptr;
+    b.pair_p = b.pair_q = nullptr;
+    b.pair_m = nullptr;
+    b.pair_cap = 0;
   } else {
-    // hits per target: ~256 in the 3D lattice interior (H = 4 dr), ~68 in
-    // 2D (H = 4.8 dr); the capacity leaves room for compression, and an
-    // overflow only sends that warp back to a full traversal
+    // rows: hits per target ~256 in the 3D lattice interior (H = 4 dr), ~68
+    // in 2D (H = 4.8 dr); the capacity leaves room for compression, and an
+    // overflowed row only sends its target back to a traversal
     b.hit_cap = D == 3 ? 384 : 160;
-    b.hits = (int*)take(4 * (size_t)b.hit_cap * C);
+    b.rows = (RowEntry*)take(sizeof(RowEntry) * (size_t)b.hit_cap * C);
     b.hit_count = (int*)take(4 * C);
-    // the density pass's distance of every entry, read by the force pass
-    b.hitr = (double*)take(8 * (size_t)b.hit_cap * C);
+    b.roff = (int*)take(4 * (size_t)s->geo.n_diff * C);
+    b.rcur = (int*)take(4 * (size_t)s->geo.n_diff * C);
+    // unordered pairs: a fluid-fluid pair fills two row entries, so half the
+    // rows' capacity is ample (a longer list sends every target to the
+    // traversal)
+    b.pair_cap = (long long)(b.hit_cap / 2) * (long long)C + 1024;
+    b.pair_p = (int*)take(4 * (size_t)b.pair_cap);
+    b.pair_q = (int*)take(4 * (size_t)b.pair_cap);
+    b.pair_m = (unsigned*)take(4 * (size_t)b.pair_cap);
     b.ck_cap = 0;
     b.ck_mask = nullptr;
   }
@@ -236,8 +245,16 @@ int pair_pass(sph_system* s, int op, int self, int reset, int fuse_eos) {
   // walls' records
   if (op == SPH_OP_DENSITY) s->aux_fluid = fuse_eos != 0;
   if (op == SPH_OP_WALL_PRESSURE) s->aux_wall = true;
-  // the density passes keep every fluid target's hit list for the force pass
-  if (op == SPH_OP_DENSITY || op == SPH_OP_DENSITY_REF) s->lists_valid = true;
+  // the density passes keep the hit masks (mixed) or the rows (FP64, the
+  // density pass only) for the force pass; an FP64 force pass turns the
+  // rows' m W into its own factors, and a traversing pass uses its targets'
+  // rows as scratch
+  if (s->params.precision == SPH_PREC_MIXED) {
+    if (op == SPH_OP_DENSITY || op == SPH_OP_DENSITY_REF) s->lists_valid = true;
+  } else {
+    if (op == SPH_OP_DENSITY) s->lists_valid = true;
+    else if (op == SPH_OP_DENSITY_REF || op == SPH_OP_FORCE) s->lists_valid = false;
+  }
   return SPH_OK;
 }
 
@@ -435,6 +452,8 @@ int sph_create(const sph_params* p, int device, sph_system** out) {
   s->b.d_err = (int*)(c + 512);
   s->b.d_pairs = (unsigned long long*)(c + 768);
   s->b.d_cat = (unsigned long long*)(c + 1024);
+  s->b.d_npairs = (unsigned long long*)(c + 1280);
+  s->b.d_pover = (int*)(c + 1288);
   if (cudaMemsetAsync(cells, 0, bytes, s->stream) != cudaSuccess ||
       cudaStreamSynchronize(s->stream) != cudaSuccess) {
     cudaGetLastError();

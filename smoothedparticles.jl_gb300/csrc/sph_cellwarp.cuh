@@ -1,5 +1,7 @@
-// sph_cellwarp.cuh -- the traversal of the FP64 pair passes (the mixed passes
-// in sph_pair32.cu stage candidates the same way but keep hit masks).
+// sph_cellwarp.cuh -- the per-target traversal of the FP64 pair passes (the
+// mixed passes in sph_pair32.cu stage candidates the same way but keep hit
+// masks; the FP64 density and force passes of a step evaluate each pair once
+// in sph_tile64.cu and come here only for rows that overflowed).
 //
 // One warp per work item: up to 32 targets of ONE cell (the work list is built
 // with the binning).  All lanes share the cell, so they share the neighbour
@@ -13,15 +15,12 @@
 // A candidate is classified in FP32; only candidates within a thin band around
 // the support radius take the reference's FP64 test (proof in sph_pair64.cu).
 //
-// Hits are appended, in traversal order, to the target's list in global
-// memory (see cw_list).  After the traversal every lane processes its own
-// list in order, so each target's sums are formed in exactly the reference's
-// order, and the lanes' lists have nearly equal lengths (the FP64 work runs
-// with full warps).  The force pass of the same binning reads the lists back
-// instead of traversing again, together with each entry's distance, which
-// the density pass stores beside the list.  A list that would exceed hit_cap
-// is processed early and its item is marked partial (the force pass then
-// traverses it).
+// Hits are appended, in traversal order, to a list in the target's row of
+// global memory (see cw_list).  After the traversal every lane processes its
+// own list in order, so each target's sums are formed in exactly the
+// reference's order, and the lanes' lists have nearly equal lengths (the FP64
+// work runs with full warps).  A list that would exceed hit_cap is processed
+// early.
 #pragma once
 
 #include "sph_common.cuh"
@@ -74,7 +73,7 @@ __device__ __forceinline__ void cw_offsets(const Geometry& g, const Consts& k, C
 // as whole 32-byte sectors (no partially written sectors for the L2 to fill
 // from DRAM); the process phase reads each list sequentially.
 __device__ __forceinline__ int* cw_list(const BinScratch& b, int i) {
-  return b.hits + (size_t)i * b.hit_cap;
+  return reinterpret_cast<int*>(b.rows + (size_t)i * b.hit_cap);
 }
 constexpr int kCwRow = 1;  // elements between consecutive entries of one list
 
@@ -125,20 +124,14 @@ __device__ __forceinline__ void cw_resolve(const State& s, const Consts& k, CwSh
 // neighbour cell c, or kCwSkip when the operator ignores it (a skipped hit
 // is not an interaction of the operator);
 // P::process(list, stride, cnt) consumes cnt entries list[0], list[stride], ...
-// skipping kCwSkip entries; P::rmem / P::rmode: the entries' distances beside
-// the list (rmode 1: process stores them, 2: process reads them, 0: neither).
-// Returns the number of entries left in the list; sets `partial` when the
-// list was processed early; `keep`: the pass keeps its lists (and distances).  FLUID_CELLS_ONLY: skip
-// neighbour cells without fluid (for operators that ignore wall neighbours).
+// skipping kCwSkip entries.  FLUID_CELLS_ONLY: skip neighbour cells without
+// fluid (for operators that ignore wall neighbours).
 template <int DIM, bool FLUID_CELLS_ONLY, class P>
-__device__ __forceinline__ int cw_traverse(const State& s, const Geometry& g, const Consts& k,
-                                           const BinScratch& b, CwShared& sh, int lane,
-                                           const CwTarget& t, P& proc, bool& partial, bool keep) {
+__device__ __forceinline__ void cw_traverse(const State& s, const Geometry& g, const Consts& k,
+                                            const BinScratch& b, CwShared& sh, int lane,
+                                            const CwTarget& t, P& proc) {
   int* const list = cw_list(b, t.i);  // dereferenced only by active lanes
   const int cap = b.hit_cap;
-  // a keeping pass records each entry's distance for the force pass
-  proc.rmode = keep && b.hitr ? 1 : 0;
-  proc.rmem = b.hitr ? b.hitr + (size_t)t.i * cap : nullptr;
   int cnt = 0;
   int nb = 0;  // deferred band candidates of this lane
   cw_offsets(g, k, sh, lane, t);
@@ -160,7 +153,6 @@ __device__ __forceinline__ int cw_traverse(const State& s, const Geometry& g, co
         if (t.active) cw_flush_tail(sh, lane, list, cnt);
         proc.process(list, kCwRow, cnt);
         cnt = 0;
-        partial = true;
       }
       __syncwarp();
       if (lane < m) sh.buf[lane] = __ldg(&s.pl[base + lane]);
@@ -214,7 +206,6 @@ __device__ __forceinline__ int cw_traverse(const State& s, const Geometry& g, co
   if (t.active) cw_flush_tail(sh, lane, list, cnt);
   __syncwarp();
   proc.process(list, kCwRow, cnt);
-  return cnt;
 }
 
 // Loads the warp's work item.  Returns false when the warp has no item.
@@ -250,29 +241,40 @@ __device__ __forceinline__ void cw_count(const BinScratch& b, int c0, int c1, in
   }
 }
 
-// The pair passes' common skeleton.  list_mode: 0 traverse only, 1 traverse
-// and keep the lists (density passes), 2 read the lists kept by the density
-// pass of this binning (force pass; partial items traverse).
+// The pair passes' common skeleton.  list_mode 0: traverse; 3: sum the rows
+// the tile passes of this binning wrote (sph_tile64.cu), and traverse for the
+// targets whose rows overflowed (the other lanes idle meanwhile).
 template <int DIM, int OP, class P>
 __device__ __forceinline__ void cw_pass(const State& s, const Geometry& g, const Consts& k,
-                                        const BinScratch& b, CwShared& sh, int lane, int item,
+                                        const BinScratch& b, CwShared& sh, int lane,
                                         const CwTarget& t, P& proc, int list_mode) {
-  if (list_mode == 2 && __ldg(&b.item_partial[item]) == 0) {
-    cw_offsets(g, k, sh, lane, t);
-    // the density pass stored each entry's distance next to the list
-    proc.rmode = b.hitr ? 2 : 0;
-    proc.rmem = b.hitr ? b.hitr + (size_t)t.i * b.hit_cap : nullptr;
-    if (t.active) proc.process(cw_list(b, t.i), kCwRow, __ldg(&b.hit_count[t.i]));
-    __syncwarp();
+  if (list_mode == 3) {
+    const int cnt = t.active ? __ldg(&b.hit_count[t.i]) : 0;
+    const bool over = cnt > b.hit_cap || (t.active && *b.d_pover != 0);
+    if (t.active && !over) proc.rows(b, t.i, cnt);
+    if (!__any_sync(0xffffffffu, over)) return;
+    CwTarget u = t;
+    u.active = over;
+    cw_traverse<DIM, OP == SPH_OP_WALL_PRESSURE>(s, g, k, b, sh, lane, u, proc);
     return;
   }
-  bool partial = false;
-  const int left = cw_traverse<DIM, OP == SPH_OP_WALL_PRESSURE>(s, g, k, b, sh, lane, t, proc,
-                                                                partial, list_mode == 1);
-  if (list_mode == 1) {
-    if (t.active) b.hit_count[t.i] = left;
-    if (lane == 0) b.item_partial[item] = partial ? 1 : 0;
+  cw_traverse<DIM, OP == SPH_OP_WALL_PRESSURE>(s, g, k, b, sh, lane, t, proc);
+}
+
+// d = x_p - x_q and the kernel distance sqrt((d0 d0 + d1 d1) + d2 d2) with the
+// sum fused (the support test, within_rn, keeps the reference's unfused form)
+template <int DIM>
+__device__ __forceinline__ double kdist64(const State& s, const double* xp, int q, double* d) {
+  d[0] = xp[0] - __ldg(&s.x[0][q]);
+  d[1] = xp[1] - __ldg(&s.x[1][q]);
+  double ss = __fma_rn(d[1], d[1], d[0] * d[0]);
+  if (DIM == 3) {
+    d[2] = xp[2] - __ldg(&s.x[2][q]);
+    ss = __fma_rn(d[2], d[2], ss);
+  } else {
+    d[2] = 0.0;
   }
+  return sqrt(ss);
 }
 
 }  // namespace sphgpu

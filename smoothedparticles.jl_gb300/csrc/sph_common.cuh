@@ -77,6 +77,29 @@ struct Consts {
   float gf[3];
 };
 
+// One entry of an FP64 target's row (32 bytes, one DRAM sector, written
+// whole): the neighbour index (bit 31 set for walls) and two values -- after
+// the density pass m W and the kernel distance, after the force pass the
+// pressure factor and the XSPH factor.
+struct __align__(32) RowEntry {
+  unsigned long long q;
+  double a, b, c;
+};
+
+__device__ __forceinline__ void row_store(RowEntry* e, unsigned long long q, double a, double b) {
+  asm volatile("st.global.v4.b64 [%0], {%1, %2, %3, %4};" ::"l"(e), "l"(q), "d"(a), "d"(b),
+               "d"(0.0)
+               : "memory");
+}
+
+// a row entry written by an earlier kernel
+__device__ __forceinline__ void row_load(const RowEntry* e, unsigned long long& q, double& a,
+                                         double& b) {
+  double c;
+  asm("ld.global.nc.v4.b64 {%0, %1, %2, %3}, [%4];" : "=l"(q), "=d"(a), "=d"(b), "=d"(c) : "l"(e));
+  (void)c;
+}
+
 // Scratch of the binning (counting sort by cell key).
 struct BinScratch {
   int* keys;        // per particle (storage order before the sort)
@@ -104,15 +127,26 @@ struct BinScratch {
   int2* items;      // (first target, count)
   int* item_off;    // key_max + 3: exclusive prefix of items per cell
   int max_items;    // capacity of `items`
-  // FP64 passes: hit lists (layout in sph_cellwarp.cuh: cw_list), t <
-  // hit_count[i] (entry = neighbour index | neighbour-cell number << 27),
-  // written by the density passes and read back by the force pass of the
-  // same binning (null in mixed-precision systems)
-  int* hits;
+  // FP64 passes (null in mixed-precision systems).  Every fluid target i
+  // owns a row of hit_cap entries at rows + i * hit_cap, its neighbours in
+  // the reference's order; hit_count[i] entries are used (> hit_cap: the
+  // row overflowed and the target traverses instead).  The row is split into
+  // one segment per neighbour-cell slot c (key_diff order), starting at
+  // roff[i * n_diff + c] (sph_tile64.cu).  A traversal (sph_cellwarp.cuh)
+  // uses the rows of its own targets as scratch.
+  RowEntry* rows;
   int* hit_count;
-  double* hitr;       // the distance of every hit list entry (same layout as hits)
-  int* item_partial;  // 1 when an item's list overflowed hit_cap
+  int* roff;          // n_diff per particle: first entry of each slot's segment
+  int* rcur;          // n_diff per particle: hits per slot
   int hit_cap;
+  // the step's unordered pairs (sph_tile64.cu), pair_cap at most: the two
+  // particles and (rank in p's segment, rank in q's segment, slot, walls)
+  int* pair_p;
+  int* pair_q;
+  unsigned* pair_m;
+  long long pair_cap;
+  unsigned long long* d_npairs;  // pairs listed (may exceed pair_cap)
+  int* d_pover;                  // the list overflowed: every target traverses
   int* cell_fluid;    // key_max + 3: fluid particles per cell
   // mixed-precision passes: one 32-bit hit mask per lane and 32-candidate
   // chunk of the neighbour sequence (sph_pair32.cu); item j of cell k owns

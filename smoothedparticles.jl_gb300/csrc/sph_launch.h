@@ -84,12 +84,20 @@ size_t scan_tmp_ints(int len);
 // op: SPH_OP_DENSITY / SPH_OP_DENSITY_REF / SPH_OP_FORCE.  reset: start the
 // accumulators at 0 (the folded reset_*! of a step) instead of the stored
 // values; fuse_eos: apply the Tait EOS in the density epilogue.
-// lists_valid: the hit lists of the last density pass belong to the current
-// binning and positions, so the force pass may read them instead of
-// traversing again.
+// lists_valid: the rows of the last density pass belong to the current
+// binning and positions, so the force pass may evaluate into them instead of
+// traversing.
 cudaError_t launch_pair_fp64(const LaunchCtx& c, const State& s, const Geometry& g,
                              const Consts& k, const BinScratch& b, int cap, int op, int self,
                              int reset, int fuse_eos, int lists_valid);
+// ---- FP64 pair evaluation once per pair (sph_tile64.cu)
+// phase 0 (density pass): counts, row offsets, m W and distances into the
+// rows; phase 1 (force pass, after the density pass of the same binning):
+// pressure and XSPH factors into the rows.  Launches kTilesLaunches[phase]
+// kernels.
+constexpr int kTilesLaunches[2] = {3, 1};
+cudaError_t launch_tiles_fp64(const LaunchCtx& c, const State& s, const Geometry& g,
+                              const Consts& k, const BinScratch& b, int cap, int phase);
 // ---- mixed-precision pair passes (sph_pair32.cu)
 // aux_fresh: the FP32 neighbour copies (vr, rhof) of the fluid particles are
 // current (written by a fused density pass since the last state change);

@@ -6,15 +6,18 @@
 // written, in the order the CPU restatement uses, so results are bit-identical
 // to it (IEEE division and square root are correctly rounded on both sides).
 //
-// Traversal: sph_cellwarp.cuh (cell-aligned warps, shared-memory staged
-// candidates, FP32 classification with an FP64 band test, per-target hit
-// lists processed in order by every lane together).  The FP64 pipe is the
-// bound of these passes (1/58 of the FP32 rate on GB300), so the evaluation
-// order below keeps FP64 operations per hit few: mass folded into the kernel
-// constants, fused multiply-adds for the sums, integer tests of x > 1 and
-// v.x < 0, 2/(rho_p + rho_q) from a correctly rounded reciprocal, and the
-// force pass reusing the distances the density pass stored.  The CPU
-// restatement evaluates the same expressions.
+// The density and force passes of a step evaluate each pair once
+// (sph_tile64.cu) and sum every target's row here, in the reference's
+// order; targets whose rows overflowed, and the other operators, use the
+// per-target traversal of sph_cellwarp.cuh (cell-aligned warps,
+// shared-memory staged candidates, FP32 classification with an FP64 band
+// test, per-target hit lists processed in order by every lane together).
+// The FP64 pipe is the bound of these passes (1/58 of the FP32 rate on
+// GB300), so the evaluation order below keeps FP64 operations per hit few:
+// mass folded into the kernel constants, fused multiply-adds for the force
+// sums, integer tests of x > 1 and v.x < 0, 2/(rho_p + rho_q) from a
+// correctly rounded reciprocal.  The CPU restatement evaluates the same
+// expressions.
 //
 // Why the FP32 classification is exact: positions are stored relative to
 // their cell's origin, |xl| < 1.02 h; the neighbour-cell offset is an integer
@@ -34,22 +37,6 @@ namespace sphgpu {
 namespace {
 
 
-// d = x_p - x_q and the kernel distance sqrt((d0 d0 + d1 d1) + d2 d2) with the
-// sum fused (the support test, within_rn, keeps the reference's unfused form)
-template <int DIM>
-__device__ __forceinline__ double kdist64(const State& s, const double* xp, int q, double* d) {
-  d[0] = xp[0] - __ldg(&s.x[0][q]);
-  d[1] = xp[1] - __ldg(&s.x[1][q]);
-  double ss = __fma_rn(d[1], d[1], d[0] * d[0]);
-  if (DIM == 3) {
-    d[2] = xp[2] - __ldg(&s.x[2][q]);
-    ss = __fma_rn(d[2], d[2], ss);
-  } else {
-    d[2] = 0.0;
-  }
-  return sqrt(ss);
-}
-
 // The operator bodies on a hit, in FP64 (list entry = q | neighbour cell << 27;
 // the force looks up whether q is a wall).
 template <int DIM, int OP>
@@ -61,8 +48,6 @@ struct Proc64 {
   double rhop, prp;
   double acc, ax, ay, az, sx, sy, sz, wp, wg, ws;
   int c0, c1, c2;
-  double* rmem = nullptr;  // distances beside the list
-  int rmode = 0;           // 1 store them, 2 read them
 
   __device__ Proc64(const State& s_, const Consts& k_) : s(s_), k(k_) {
     acc = ax = ay = az = sx = sy = sz = wp = wg = ws = 0.0;
@@ -82,27 +67,15 @@ struct Proc64 {
       if (e == kCwSkip) continue;  // a band candidate beyond the support
       const int q = e & kCwIndexMask;
       double d[3];
-      double r;
-      if (OP == SPH_OP_FORCE && rmode == 2) {
-        // the separation for the direction; the distance as the density
-        // pass computed it from the same positions
-        d[0] = xp[0] - __ldg(&s.x[0][q]);
-        d[1] = xp[1] - __ldg(&s.x[1][q]);
-        d[2] = DIM == 3 ? xp[2] - __ldg(&s.x[2][q]) : 0.0;
-        r = __ldg(&rmem[(size_t)j * stride]);
-      } else {
-        r = kdist64<DIM>(s, xp, q, d);
-        if ((OP == SPH_OP_DENSITY || OP == SPH_OP_DENSITY_REF) && rmode == 1)
-          rmem[(size_t)j * stride] = r;
-      }
+      const double r = kdist64<DIM>(s, xp, q, d);
       const bool fluid = OP != SPH_OP_FORCE || __ldg(&s.type[q]) == kFluid;
       if (fluid) ++c0; else ++c1;
       // kernel pieces in the oracle's order (ker_w / ker_rdw), mass folded
-      // into the constants, sums with fused multiply-adds
+      // into the constants, the force sums with fused multiply-adds
       const double t = ker_t(k, r);
       const double t2 = t * t;
       if (OP == SPH_OP_DENSITY || OP == SPH_OP_DENSITY_REF) {
-        acc = __fma_rn(k.mcw * (t2 * t2), __fma_rn(-4.0, t, 5.0), acc);
+        acc = acc + (k.mcw * (t2 * t2)) * __fma_rn(-4.0, t, 5.0);
       } else if (OP == SPH_OP_WALL_PRESSURE) {
         // Adami, Hu & Adams (2012) wall pressure, g . (x_w - x_f)
         const double w = (k.cw * (t2 * t2)) * __fma_rn(-4.0, t, 5.0);
@@ -146,6 +119,43 @@ struct Proc64 {
         ax = __fma_rn(cf, d[0], ax);
         ay = __fma_rn(cf, d[1], ay);
         if (DIM == 3) az = __fma_rn(cf, d[2], az);
+      }
+    }
+  }
+
+  // Sums target i's row (sph_tile64.cu wrote each entry's m W, or its
+  // pressure and XSPH factors, once per pair): the same terms, accumulated
+  // in the same order, as process() over the traversal's list.
+  __device__ __forceinline__ void rows(const BinScratch& b, int i, int cnt) {
+    const RowEntry* row = b.rows + (size_t)i * b.hit_cap;
+    if (OP == SPH_OP_DENSITY) {
+      for (int j = 0; j < cnt; ++j) acc = acc + __ldg(&row[j].a);
+      c0 += cnt;
+    } else if (OP == SPH_OP_FORCE) {
+      const int n = *b.d_n;
+      for (int j = 0; j < cnt; ++j) {
+        unsigned long long e;
+        double cf, wx;
+        row_load(row + j, e, cf, wx);
+        const int q = (int)(e & 0x7fffffffu);
+        if (q >= n) {  // an entry the tile passes did not write: report, skip
+          atomicOr(b.d_err, kErrBounds);
+          continue;
+        }
+        const double d0 = xp[0] - __ldg(&s.x[0][q]);
+        const double d1 = xp[1] - __ldg(&s.x[1][q]);
+        ax = __fma_rn(cf, d0, ax);
+        ay = __fma_rn(cf, d1, ay);
+        if (DIM == 3) az = __fma_rn(cf, xp[2] - __ldg(&s.x[2][q]), az);
+        if ((e & 0x80000000u) == 0u) {
+          // fluid neighbour: + wx (v_q - v_p)
+          sx = __fma_rn(-wx, vp[0] - __ldg(&s.v[0][q]), sx);
+          sy = __fma_rn(-wx, vp[1] - __ldg(&s.v[1][q]), sy);
+          if (DIM == 3) sz = __fma_rn(-wx, vp[2] - __ldg(&s.v[2][q]), sz);
+          ++c0;
+        } else {
+          ++c1;
+        }
       }
     }
   }
@@ -197,7 +207,7 @@ __global__ void __launch_bounds__(32 * WARPS) pair64_kernel(State s, Geometry g,
       p.prp = s.Pr[i];
     }
   }
-  cw_pass<DIM, OP>(s, g, k, b, shared[w], lane, item, t, p, list_mode);
+  cw_pass<DIM, OP>(s, g, k, b, shared[w], lane, t, p, list_mode);
 
   if (valid && !t.active) {
     // a folded reset_*! still zeroes the targets the operator skips
@@ -369,7 +379,7 @@ __global__ void __launch_bounds__(128) debug_pairs_kernel(State s, Geometry g, C
 }
 template <int DIM>
 cudaError_t launch_pair_dim(const LaunchCtx& c, const State& s, const Geometry& g,
-                            const Consts& k, const BinScratch& b, int, int op, int self,
+                            const Consts& k, const BinScratch& b, int cap, int op, int self,
                             int reset, int fuse_eos, int list_mode) {
   const int W = k.warps;
   const int blocks = (b.max_items + W - 1) / W;
@@ -377,16 +387,22 @@ cudaError_t launch_pair_dim(const LaunchCtx& c, const State& s, const Geometry& 
                   : op == SPH_OP_WALL_PRESSURE ? SPH_KERNEL_WALL
                                                : SPH_KERNEL_DENSITY;
   mark(c, kid, 0);
+  // the density and force passes of a step: every pair evaluated once into
+  // the rows (sph_tile64.cu), which the pass below then sums
+  if (list_mode == 3) {
+    const cudaError_t e = launch_tiles_fp64(c, s, g, k, b, cap, op == SPH_OP_FORCE ? 1 : 0);
+    if (e != cudaSuccess) return e;
+  }
   switch (op) {
     case SPH_OP_DENSITY:
-      if (W == 2) pair64_kernel<DIM, SPH_OP_DENSITY, 2><<<blocks, 64, 0, c.stream>>>(s, g, k, b, self, reset, fuse_eos, 1);
-      else if (W == 8) pair64_kernel<DIM, SPH_OP_DENSITY, 8><<<blocks, 256, 0, c.stream>>>(s, g, k, b, self, reset, fuse_eos, 1);
-      else pair64_kernel<DIM, SPH_OP_DENSITY, 4><<<blocks, 128, 0, c.stream>>>(s, g, k, b, self, reset, fuse_eos, 1);
+      if (W == 2) pair64_kernel<DIM, SPH_OP_DENSITY, 2><<<blocks, 64, 0, c.stream>>>(s, g, k, b, self, reset, fuse_eos, list_mode);
+      else if (W == 8) pair64_kernel<DIM, SPH_OP_DENSITY, 8><<<blocks, 256, 0, c.stream>>>(s, g, k, b, self, reset, fuse_eos, list_mode);
+      else pair64_kernel<DIM, SPH_OP_DENSITY, 4><<<blocks, 128, 0, c.stream>>>(s, g, k, b, self, reset, fuse_eos, list_mode);
       break;
     case SPH_OP_DENSITY_REF:
-      if (W == 2) pair64_kernel<DIM, SPH_OP_DENSITY_REF, 2><<<blocks, 64, 0, c.stream>>>(s, g, k, b, self, reset, 0, 1);
-      else if (W == 8) pair64_kernel<DIM, SPH_OP_DENSITY_REF, 8><<<blocks, 256, 0, c.stream>>>(s, g, k, b, self, reset, 0, 1);
-      else pair64_kernel<DIM, SPH_OP_DENSITY_REF, 4><<<blocks, 128, 0, c.stream>>>(s, g, k, b, self, reset, 0, 1);
+      if (W == 2) pair64_kernel<DIM, SPH_OP_DENSITY_REF, 2><<<blocks, 64, 0, c.stream>>>(s, g, k, b, self, reset, 0, 0);
+      else if (W == 8) pair64_kernel<DIM, SPH_OP_DENSITY_REF, 8><<<blocks, 256, 0, c.stream>>>(s, g, k, b, self, reset, 0, 0);
+      else pair64_kernel<DIM, SPH_OP_DENSITY_REF, 4><<<blocks, 128, 0, c.stream>>>(s, g, k, b, self, reset, 0, 0);
       break;
     case SPH_OP_WALL_PRESSURE:
       if (W == 2) pair64_kernel<DIM, SPH_OP_WALL_PRESSURE, 2><<<blocks, 64, 0, c.stream>>>(s, g, k, b, 0, 0, 0, 0);
@@ -399,7 +415,7 @@ cudaError_t launch_pair_dim(const LaunchCtx& c, const State& s, const Geometry& 
       else pair64_kernel<DIM, SPH_OP_FORCE, 4><<<blocks, 128, 0, c.stream>>>(s, g, k, b, self, reset, 0, list_mode);
       break;
   }
-  mark(c, kid, 1);
+  mark(c, kid, 1, list_mode == 3 ? 1 + kTilesLaunches[op == SPH_OP_FORCE ? 1 : 0] : 1);
   return cudaGetLastError();
 }
 
@@ -409,7 +425,9 @@ cudaError_t launch_pair_fp64(const LaunchCtx& c, const State& s, const Geometry&
                              const Consts& k, const BinScratch& b, int cap, int op, int self,
                              int reset, int fuse_eos, int lists_valid) {
   if (cap <= 0) return cudaSuccess;
-  const int lm = lists_valid ? 2 : 0;
+  // rows: the density pass always builds them; the force pass sums them when
+  // the density pass of this binning built them, else it traverses
+  const int lm = op == SPH_OP_DENSITY || (op == SPH_OP_FORCE && lists_valid) ? 3 : 0;
   return k.dim == 2 ? launch_pair_dim<2>(c, s, g, k, b, cap, op, self, reset, fuse_eos, lm)
                     : launch_pair_dim<3>(c, s, g, k, b, cap, op, self, reset, fuse_eos, lm);
 }

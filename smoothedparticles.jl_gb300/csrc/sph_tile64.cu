@@ -1,0 +1,441 @@
+// sph_tile64.cu -- the FP64 density and force passes of a step with every
+// pair evaluated once.
+//
+// Each pair's contribution is a symmetric scalar times a vector that changes
+// sign with the direction, exactly in IEEE arithmetic: the kernel distance r
+// (squares of negated differences), m W(r), rho_p + rho_q and
+// P_p/rho_p^2 + P_q/rho_q^2 (commutative additions), (v_p - v_q).(x_p - x_q)
+// (products of two negated differences), hence the viscosity term, the
+// pressure factor cf and the XSPH factor wx.  Both directions of a pair
+// therefore contribute bit-identical factors, and a target's sums only need
+// them in its own neighbour order.  The pair set is symmetric too: outside
+// the FP32 band the FP32 decision equals the exact test, inside the band it
+// is the exact test, which squares the differences.
+//
+// Rows: every fluid target owns hit_cap entries (neighbour index, distance,
+// two factors).  Its neighbours in the reference's order (core.jl:96-105) are
+// the slots of key_diff in turn, each slot's cell in stored order, so the row
+// is one segment per slot: the segment of (target i, slot c) holds i's hits
+// in cell key(i) + key_diff[c], in ascending index order.
+//
+// Tiles: one warp per (cell a, forward slot c >= the centre slot), with
+// b = a + key_diff[c].  The tile owns the segments (p in a, slot c) and
+// (q in b, slot mirror(c)), where mirror(c) = n_diff - 1 - c is the slot from
+// b back to a; every segment has exactly one writer, so nothing is atomic
+// but the pair list's tail.  A tile classifies a x b in blocks of 32 x 32:
+// lane u tests column q_u against the 32 staged rows (bit i of its column
+// mask); the row masks are the transposes (ballots).  The rank of q in p's
+// segment is the number of p's hits in the earlier column blocks (a cursor)
+// plus the bits of p's row mask below q, and likewise for p in q's segment.
+// The tile of the cell itself (c = centre) takes each unordered pair once
+// (p < q); its diagonal blocks are symmetric.
+//
+// Passes of a step (launch order):
+//   tiles    classify once: rcur := hits per (target, slot); the pair list
+//            (p, q, both ranks, slot, wall bits)
+//   scan     roff := exclusive prefix over the target's slots; hit_count
+//   density  per pair: r and m W into both rows (at roff + rank)
+//   [sum]    sph_pair64.cu: rho = the row's sum, self term, EOS
+//   force    per pair: cf and wx into both rows (a fluid-wall pair only into
+//            the fluid target's row: walls are not force targets)
+//   [sum]    sph_pair64.cu: a += cf d, xs += -wx dv over the row
+//
+// A row longer than hit_cap, or a target next to a cell of more than 65535
+// particles (the tiles' 16-bit local indices), is marked overflowed by the
+// scan; its sum passes traverse instead.  A pair list longer than pair_cap
+// sends every target to the traversal.
+//
+// Built with --fmad=false like sph_pair64.cu: the expressions below round
+// where they are written, in the oracle's order.
+#include <algorithm>
+
+#include "sph_cellwarp.cuh"
+#include "sph_launch.h"
+#include "sphgpu.h"
+
+namespace sphgpu {
+
+namespace {
+
+constexpr int kTileWarps = 4;
+constexpr int kTileList = 512;         // pairs buffered per warp before they are listed
+constexpr float kTileFar = 1.0e18f;    // coordinate of an empty staging slot
+// pair_m: rank in p's segment (10 bits), rank in q's segment (10), slot (5),
+// p is a wall, q is a wall.  A rank of kRankNone (>= every hit_cap) marks a
+// side without a row entry.
+constexpr unsigned kRankNone = 1023u;
+constexpr unsigned kPWall = 1u << 25, kQWall = 1u << 26;
+constexpr int kNoRow = 1 << 24;  // segment offset of a target without a row
+
+struct TileShared {
+  float4 pa[32];          // rows: cell-relative positions minus b's offset, type bits in .w
+  unsigned rmask[32];     // row masks of the current block (bit u = column u)
+  int rcur[32];           // row cursors at the start of the current block
+  uint2 list[kTileList];  // pairs: (p_local | q_local << 16, pair_m)
+};
+
+// Appends the warp's buffered pairs to the pair list.
+__device__ __forceinline__ void tile_emit(const BinScratch& b, const TileShared& sh, int lane,
+                                          int n, int sa, int sb) {
+  unsigned long long base = 0;
+  if (lane == 0) base = atomicAdd(b.d_npairs, (unsigned long long)n);
+  base = __shfl_sync(0xffffffffu, base, 0);
+  if (base + (unsigned long long)n > (unsigned long long)b.pair_cap) {
+    if (lane == 0) *b.d_pover = 1;
+    return;
+  }
+  for (int e = lane; e < n; e += 32) {
+    const uint2 en = sh.list[e];
+    const size_t o = (size_t)base + e;
+    b.pair_p[o] = sa + (int)(en.x & 0xffffu);
+    b.pair_q[o] = sb + (int)(en.x >> 16);
+    b.pair_m[o] = en.y;
+  }
+}
+
+// One tile: cell a = [sa, sa + na), slot c, cell nk = [sb, sb + nb).
+template <int DIM>
+__device__ __forceinline__ void tile_run(const State& s, const Geometry& g, const Consts& k,
+                                         const BinScratch& b, TileShared& sh, int lane, int a,
+                                         int nk, int c, int sa, int na, int sb, int nb) {
+  const unsigned full = 0xffffffffu;
+  const int nd = g.n_diff;
+  const bool self = c == (nd >> 1);
+  const int mc = nd - 1 - c;
+  const int cap = b.hit_cap;
+  const unsigned below = lanemask_lt();
+  // b's origin relative to a's (the traversal's cw_offset)
+  int acx, acy, acz, bcx, bcy, bcz;
+  decode_key(g, a, acx, acy, acz);
+  decode_key(g, nk, bcx, bcy, bcz);
+  const float ox = (float)(bcx - acx) * k.hf;
+  const float oy = (float)(bcy - acy) * k.hf;
+  const float oz = (float)(bcz - acz) * k.hf;
+  const int nA = (na + 31) >> 5, nB = (nb + 31) >> 5;
+  int ln = 0;  // pairs buffered
+  for (int ia = 0; ia < nA; ++ia) {
+    const int ma = min(32, na - 32 * ia);
+    const int p = sa + 32 * ia + lane;
+    float4 pr = make_float4(kTileFar, kTileFar, kTileFar, __int_as_float(-1));
+    int rc = 0;  // this lane's row cursor: p's hits in the blocks so far
+    if (lane < ma) {
+      pr = __ldg(&s.pl[p]);
+      // the row's position relative to b's origin, rounded as the
+      // traversal's (xl_p - offset)
+      pr.x = pr.x - ox;
+      pr.y = pr.y - oy;
+      pr.z = pr.z - oz;
+      // in the own cell's tile, earlier blocks counted p's hits as a column
+      if (self && ia > 0) rc = b.rcur[(size_t)p * nd + c];
+    }
+    __syncwarp();
+    sh.pa[lane] = pr;
+    const unsigned afl = __ballot_sync(full, lane < ma && __float_as_int(pr.w) == kFluid);
+    __syncwarp();
+    for (int jb = self ? ia : 0; jb < nB; ++jb) {
+      const bool diag = self && jb == ia;
+      const int mb = min(32, nb - 32 * jb);
+      const int q = sb + 32 * jb + lane;
+      // this lane's column particle (the diagonal block: the row itself,
+      // offset 0)
+      float4 pc = pr;
+      if (!diag)
+        pc = lane < mb ? __ldg(&s.pl[q])
+                       : make_float4(kTileFar, kTileFar, kTileFar, __int_as_float(-1));
+      const bool qfl = lane < mb && __float_as_int(pc.w) == kFluid;
+      unsigned cm = 0u, bm = 0u;
+      if (lane < mb) {
+        for (int i = 0; i < ma; ++i) {
+          const float4 r4 = sh.pa[i];
+          const float dx = r4.x - pc.x;
+          const float dy = r4.y - pc.y;
+          float ss = dx * dx + dy * dy;
+          if (DIM == 3) {
+            const float dz = r4.z - pc.z;
+            ss = ss + dz * dz;
+          }
+          if (!(ss > k.s_hi)) {
+            cm |= 1u << i;
+            if (!(ss < k.s_lo)) bm |= 1u << i;
+          }
+        }
+        // a particle is not its own neighbour (core.jl:105)
+        const int di = q - (sa + 32 * ia);
+        if (di >= 0 && di < 32) {
+          cm &= ~(1u << di);
+          bm &= ~(1u << di);
+        }
+        // a pair of walls takes part in neither pass
+        if (!qfl) {
+          cm &= afl;
+          bm &= afl;
+        }
+      }
+      // band candidates: the reference's FP64 test, all lanes together
+      while (__any_sync(full, bm != 0u)) {
+        if (bm) {
+          const int i = __ffs(bm) - 1;
+          bm &= bm - 1u;
+          const int pi = sa + 32 * ia + i;
+          double xr[3];
+          xr[0] = __ldg(&s.x[0][pi]);
+          xr[1] = __ldg(&s.x[1][pi]);
+          xr[2] = DIM == 3 ? __ldg(&s.x[2][pi]) : 0.0;
+          if (!within_rn<DIM>(s, k, xr, q)) cm &= ~(1u << i);
+        }
+      }
+      // row masks (bit u = column u); the diagonal block is symmetric
+      unsigned rm = cm;
+      if (!diag) {
+        rm = 0u;
+        for (int i = 0; i < ma; ++i) {
+          const unsigned v = __ballot_sync(full, (cm >> i) & 1u);
+          if (lane == i) rm = v;
+        }
+      }
+      // the column's cursor (in the diagonal block: the particle's own)
+      int cc = rc;
+      size_t cj = 0;
+      if (!diag && lane < mb) {
+        cj = (size_t)q * nd + mc;
+        cc = ia == 0 ? 0 : b.rcur[cj];
+      }
+      sh.rmask[lane] = rm;
+      sh.rcur[lane] = rc;
+      __syncwarp();
+      // the block's pairs with their ranks in both segments; a pair neither
+      // of whose sides has a row entry is dropped
+      unsigned em = diag ? (cm & below) : cm;
+      for (;;) {
+        const bool has = em != 0u;
+        if (__ballot_sync(full, has) == 0u) break;
+        bool keep = false;
+        unsigned meta = 0u, loc = 0u;
+        if (has) {
+          const int i = __ffs(em) - 1;
+          em &= em - 1u;
+          unsigned pr_ = kRankNone, qr_ = kRankNone;
+          if ((afl >> i) & 1u) {
+            const int v = sh.rcur[i] + __popc(sh.rmask[i] & below);
+            if (v < cap) pr_ = (unsigned)v;
+          }
+          if (qfl) {
+            const int v = cc + __popc(cm & ((1u << i) - 1u));
+            if (v < cap) qr_ = (unsigned)v;
+          }
+          keep = pr_ != kRankNone || qr_ != kRankNone;
+          meta = pr_ | (qr_ << 10) | ((unsigned)c << 20) | (((afl >> i) & 1u) ? 0u : kPWall) |
+                 (qfl ? 0u : kQWall);
+          loc = (unsigned)(32 * ia + i) | ((unsigned)(32 * jb + lane) << 16);
+        }
+        const unsigned kb = __ballot_sync(full, keep);
+        if (ln + __popc(kb) > kTileList) {
+          __syncwarp();
+          tile_emit(b, sh, lane, ln, sa, sb);
+          ln = 0;
+          __syncwarp();
+        }
+        if (keep) sh.list[ln + __popc(kb & below)] = make_uint2(loc, meta);
+        ln += __popc(kb);
+      }
+      if (!diag && lane < mb) b.rcur[cj] = cc + __popc(cm);
+      __syncwarp();
+      rc += __popc(rm);
+    }
+    if (lane < ma) b.rcur[(size_t)p * nd + c] = rc;
+  }
+  if (ln > 0) {
+    __syncwarp();
+    tile_emit(b, sh, lane, ln, sa, sb);
+  }
+  __syncwarp();
+}
+
+// Warps stride over the tile slots (work item, forward slot); a tile is
+// taken by its cell's first item.
+template <int DIM>
+__global__ void __launch_bounds__(32 * kTileWarps) tile_kernel(State s, Geometry g, Consts k,
+                                                               BinScratch b, int warps_total) {
+  __shared__ TileShared shared[kTileWarps];
+  TileShared& sh = shared[threadIdx.x >> 5];
+  const int lane = threadIdx.x & 31;
+  const int ctr = g.n_diff >> 1;
+  const int nf = ctr + 1;
+  const long long n_slots = (long long)__ldg(&b.item_off[g.key_max + 1]) * nf;
+  for (long long w = (long long)blockIdx.x * kTileWarps + (threadIdx.x >> 5); w < n_slots;
+       w += warps_total) {
+    const int item = (int)(w / nf);
+    const int c = ctr + (int)(w - (long long)item * nf);
+    const int first = __ldg(&b.items[item]).x;
+    const int a = __ldg(&s.cell[first]);
+    const int sa = __ldg(&b.cell_start[a]);
+    if (first != sa) continue;
+    const int nk = a + g.key_diff[c];
+    if (nk < 1 || nk > g.key_max) continue;  // core.jl:98
+    if (__ldg(&b.cell_fluid[a]) == 0 && __ldg(&b.cell_fluid[nk]) == 0) continue;
+    const int na = __ldg(&b.cell_start[a + 1]) - sa;
+    const int sb = __ldg(&b.cell_start[nk]);
+    const int nb = __ldg(&b.cell_start[nk + 1]) - sb;
+    if (nb == 0 || na > 0xffff || nb > 0xffff) continue;
+    tile_run<DIM>(s, g, k, b, sh, lane, a, nk, c, sa, na, sb, nb);
+  }
+}
+
+// Row offsets of every fluid target from its per-slot counts.
+__global__ void __launch_bounds__(256) row_scan_kernel(State s, Geometry g, BinScratch b) {
+  const int n = *b.d_n;
+  const int i = blockIdx.x * 256 + threadIdx.x;
+  if (i >= n || s.type[i] != kFluid) return;
+  const int key = s.cell[i];
+  const int nd = g.n_diff;
+  bool over = __ldg(&b.cell_start[key + 1]) - __ldg(&b.cell_start[key]) > 0xffff;
+  int run = 0;
+  for (int c = 0; c < nd; ++c) {
+    const int nk = key + g.key_diff[c];
+    int cnt = 0;
+    if (nk >= 1 && nk <= g.key_max) {
+      const int m = __ldg(&b.cell_start[nk + 1]) - __ldg(&b.cell_start[nk]);
+      if (m > 0xffff) over = true;
+      else if (m > 0) cnt = b.rcur[(size_t)i * nd + c];
+    }
+    b.roff[(size_t)i * nd + c] = run;
+    run += cnt;
+  }
+  if (over || run > b.hit_cap) {
+    // an overflowed target has no row entries: its offsets lie beyond the
+    // row, so the pair passes treat its side like a wall's (and leave the
+    // row to the traversal, which uses it as scratch)
+    for (int c = 0; c < nd; ++c) b.roff[(size_t)i * nd + c] = kNoRow;
+    run = b.hit_cap + 1;
+  }
+  b.hit_count[i] = run;
+}
+
+// The FP64 evaluation of the listed pairs into the rows (PH 0: density,
+// 1: force).  Threads stride over the list.  A side writes its entry only
+// when its target is fluid and has a row (walls and overflowed targets have
+// none); every entry is written whole.
+template <int DIM, int PH>
+__global__ void __launch_bounds__(256) pair_list_kernel(State s, Geometry g, Consts k,
+                                                        BinScratch b, int threads_total) {
+  if (*b.d_pover) return;  // every target traverses
+  const long long np = (long long)*b.d_npairs;
+  const int nd = g.n_diff;
+  const size_t cap = (size_t)b.hit_cap;
+  int av = 0;
+  for (long long e = (long long)blockIdx.x * 256 + threadIdx.x; e < np; e += threads_total) {
+    const int p = __ldg(&b.pair_p[e]);
+    const int q = __ldg(&b.pair_q[e]);
+    const unsigned m = __ldg(&b.pair_m[e]);
+    const int c = (int)((m >> 20) & 31u);
+    const bool fp = (m & kPWall) == 0u, fq = (m & kQWall) == 0u;
+    // entry positions (a rank of kRankNone, or a target without a row, lands
+    // beyond hit_cap)
+    const int vp = fp ? __ldg(&b.roff[(size_t)p * nd + c]) + (int)(m & 1023u) : b.hit_cap;
+    const int vq = fq ? __ldg(&b.roff[(size_t)q * nd + (nd - 1 - c)]) + (int)((m >> 10) & 1023u)
+                      : b.hit_cap;
+    const bool wp = vp < b.hit_cap, wq = vq < b.hit_cap;
+    if (!wp && !wq) continue;
+    RowEntry* const ep = b.rows + (size_t)p * cap + vp;
+    RowEntry* const eq = b.rows + (size_t)q * cap + vq;
+    const unsigned long long qbits = (unsigned)q | (fq ? 0u : 0x80000000u);
+    const unsigned long long pbits = (unsigned)p | (fp ? 0u : 0x80000000u);
+    if (PH == 0) {
+      double xp[3], d[3];
+      xp[0] = __ldg(&s.x[0][p]);
+      xp[1] = __ldg(&s.x[1][p]);
+      xp[2] = DIM == 3 ? __ldg(&s.x[2][p]) : 0.0;
+      const double r = kdist64<DIM>(s, xp, q, d);
+      const double t = ker_t(k, r);
+      const double t2 = t * t;
+      const double w = (k.mcw * (t2 * t2)) * __fma_rn(-4.0, t, 5.0);  // m W
+      if (wp) row_store(ep, qbits, w, r);
+      if (wq) row_store(eq, pbits, w, r);
+    } else {
+      // m W and r as the density pass of this binning stored them
+      unsigned long long unused;
+      double w, r;
+      row_load(wp ? ep : eq, unused, w, r);
+      const double t = ker_t(k, r);
+      const double t2 = t * t;
+      const double ker = k.mcr * (t2 * t);  // m rDW
+      const double sp = __ldg(&s.Pr[p]) + __ldg(&s.Pr[q]);
+      if (fp && fq) {
+        // pressure (collapse_symplectic.jl:114-118) + Monaghan viscosity +
+        // XSPH, in p's direction (q's is the same factor)
+        const double d0 = __ldg(&s.x[0][p]) - __ldg(&s.x[0][q]);
+        const double d1 = __ldg(&s.x[1][p]) - __ldg(&s.x[1][q]);
+        const double dv0 = __ldg(&s.v[0][p]) - __ldg(&s.v[0][q]);
+        const double dv1 = __ldg(&s.v[1][p]) - __ldg(&s.v[1][q]);
+        double vdx = __fma_rn(dv1, d1, dv0 * d0);
+        if (DIM == 3) {
+          const double d2 = __ldg(&s.x[2][p]) - __ldg(&s.x[2][q]);
+          const double dv2 = __ldg(&s.v[2][p]) - __ldg(&s.v[2][q]);
+          vdx = __fma_rn(dv2, d2, vdx);
+        }
+        const double inv_rb = two_over(__ldg(&s.rho[p]) + __ldg(&s.rho[q]));
+        double pi = 0.0;
+        if (lt0(vdx)) {
+          // mu = h v.x / (r^2 + eta^2) with r^2 as r r and the reciprocal
+          pi = ((k.ca * vdx) * __drcp_rn(r * r + k.eta2)) * inv_rb;
+          // one count per direction whose row is summed
+          av += (wp ? 1 : 0) + (wq ? 1 : 0);
+        }
+        const double cf = -ker * (sp + pi);
+        const double wx = w * inv_rb;  // m W / rho_bar
+        if (wp) row_store(ep, qbits, cf, wx);
+        if (wq) row_store(eq, pbits, cf, wx);
+      } else {
+        // fluid-wall: the pressure term with the wall pressure, into the
+        // fluid target's row (a wall has no row entry)
+        const double cf = -ker * sp;
+        if (wp) row_store(ep, qbits, cf, 0.0);
+        if (wq) row_store(eq, pbits, cf, 0.0);
+      }
+    }
+  }
+  if (PH == 1) cw_warp_add(b.d_cat + kCatForceAV, av);
+}
+
+// One resident wave of a kernel (its warps stride over the work; blocks
+// beyond the resident ones would only start after the first wave).
+template <class K>
+int resident_blocks(K kernel, int threads) {
+  int dev = 0, sms = 0, per_sm = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, threads, 0);
+  cudaGetLastError();
+  return std::max(1, sms) * std::max(1, per_sm);
+}
+
+template <int DIM>
+void tiles_dim(cudaStream_t st, const State& s, const Geometry& g, const Consts& k,
+               const BinScratch& b, int cap, int phase) {
+  static const int tile_wave = resident_blocks(tile_kernel<DIM>, 32 * kTileWarps);
+  static const int dens_wave = resident_blocks(pair_list_kernel<DIM, 0>, 256);
+  static const int force_wave = resident_blocks(pair_list_kernel<DIM, 1>, 256);
+  if (phase == 0) {
+    const long long slots = (long long)b.max_items * (g.n_diff / 2 + 1);
+    const int tb = (int)std::max(
+        1LL, std::min<long long>((slots + kTileWarps - 1) / kTileWarps, tile_wave));
+    cudaMemsetAsync(b.d_npairs, 0, 16, st);  // pair count and overflow flag
+    tile_kernel<DIM><<<tb, 32 * kTileWarps, 0, st>>>(s, g, k, b, tb * kTileWarps);
+    row_scan_kernel<<<(cap + 255) / 256, 256, 0, st>>>(s, g, b);
+    pair_list_kernel<DIM, 0><<<dens_wave, 256, 0, st>>>(s, g, k, b, dens_wave * 256);
+  } else {
+    pair_list_kernel<DIM, 1><<<force_wave, 256, 0, st>>>(s, g, k, b, force_wave * 256);
+  }
+}
+
+}  // namespace
+
+cudaError_t launch_tiles_fp64(const LaunchCtx& c, const State& s, const Geometry& g,
+                              const Consts& k, const BinScratch& b, int cap, int phase) {
+  if (cap <= 0) return cudaSuccess;
+  if (k.dim == 2) tiles_dim<2>(c.stream, s, g, k, b, cap, phase);
+  else tiles_dim<3>(c.stream, s, g, k, b, cap, phase);
+  return cudaGetLastError();
+}
+
+}  // namespace sphgpu

@@ -190,6 +190,64 @@ def test_large_2d_first_steps_bitexact(gpu, oracle_mod):
     assert_same_state(g, o, fields=("x", "v", "rho", "P", "a"))
 
 
+def test_row_overflow_bitexact(gpu, oracle_mod):
+    """3D dam break with H = 4.6 dr: interior targets have ~400 neighbours,
+    more than a row holds (384), and fall back to the traversal; targets near
+    the walls and the free surface keep their rows."""
+    c = G.dam_break(3, 0.1, h_factor=2.3)
+    g, o = make(c, oracle_mod)
+    g.init_state()
+    assert g.pair_count(reset=True) == o.init_state()
+    assert_same_state(g, o)
+    for _ in range(3):
+        g.step(1)
+        assert g.pair_count(reset=True) == o.step(1)
+    assert_same_state(g, o)
+    g.synchronize()
+
+
+def _narrow_case(dim, n, seed):
+    """Random fluid and wall particles in a domain one cell wide along x
+    (and two along y in 3D): key + key_diff wraps between rows of cells and
+    reaches the same cell through several slots, which the reference's
+    range test (core.jl:98) keeps, so pairs repeat."""
+    rng = np.random.default_rng(seed)
+    H = 0.1
+    if dim == 2:
+        hi = [0.9 * H, 10.0 * H, 0.0]
+    else:
+        hi = [0.9 * H, 1.9 * H, 4.0 * H]
+    x = np.zeros((n, 3))
+    for d in range(dim):
+        x[:, d] = rng.uniform(0.0, hi[d], n)
+    typ = np.where(rng.uniform(size=n) < 0.2, G.WALL, G.FLUID).astype(np.int32)
+    v = np.zeros((n, 3))
+    v[:, :dim] = rng.normal(0.0, 0.05, (n, dim))
+    v[typ == G.WALL] = 0.0
+    rho0, c0 = 1000.0, 20.0
+    vol = np.prod(hi[:dim]) / n
+    params = dict(dim=dim, h=H, domain_min=[0.0, 0.0, 0.0], domain_max=hi, mass=rho0 * vol,
+                  rho0=rho0, c0=c0, h_smooth=0.5 * H, alpha=0.05, eps_xsph=0.5,
+                  gravity=[0.0, -9.81, 0.0] if dim == 2 else [0.0, 0.0, -9.81],
+                  dt=(0.05 * H) / c0, col_height=hi[dim - 1], vertical_axis=dim - 1)
+    return G.Case(f"narrow_{dim}d_{n}", dim, H / 4.0, x, typ, v, params)
+
+
+@pytest.mark.parametrize("dim,n", [(2, 150), (2, 400), (3, 300)])
+def test_wrapped_cells_bitexact(gpu, oracle_mod, dim, n):
+    c = _narrow_case(dim, n, 7 + n)
+    g, o = make(c, oracle_mod)
+    assert g.geometry()["key_lim"][0] == 1  # one cell along x
+    g.init_state()
+    assert g.pair_count(reset=True) == o.init_state()
+    assert_same_state(g, o)
+    for _ in range(3):
+        g.step(1)
+        assert g.pair_count(reset=True) == o.step(1)
+    assert_same_state(g, o)
+    g.synchronize()
+
+
 def test_bad_arguments_raise(gpu):
     c = G.dam_break(2, 0.1)
     g = sphgpu.ParticleSystem(c.params)
