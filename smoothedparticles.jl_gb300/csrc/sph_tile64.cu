@@ -68,11 +68,48 @@ constexpr unsigned kPWall = 1u << 25, kQWall = 1u << 26;
 constexpr int kNoRow = 1 << 24;  // segment offset of a target without a row
 
 struct TileShared {
-  float4 pa[32];          // rows: cell-relative positions minus b's offset, type bits in .w
+  // rows: cell-relative positions minus b's offset (pairs of rows are read
+  // as one 64-bit word by the packed classification)
+  float rx[32], ry[32], rz[32];
   unsigned rmask[32];     // row masks of the current block (bit u = column u)
   int rcur[32];           // row cursors at the start of the current block
   uint2 list[kTileList];  // pairs: (p_local | q_local << 16, pair_m)
 };
+
+// Two FP32 lanes per 64-bit register (Blackwell's packed FP32 arithmetic).
+__device__ __forceinline__ unsigned long long f2_pack(float lo, float hi) {
+  return (unsigned long long)__float_as_uint(lo) | ((unsigned long long)__float_as_uint(hi) << 32);
+}
+__device__ __forceinline__ unsigned long long f2_sub(unsigned long long a, unsigned long long b) {
+  unsigned long long r;
+  asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(a), "l"(b));
+  return r;
+}
+__device__ __forceinline__ unsigned long long f2_mul(unsigned long long a, unsigned long long b) {
+  unsigned long long r;
+  asm("mul.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(a), "l"(b));
+  return r;
+}
+__device__ __forceinline__ unsigned long long f2_fma(unsigned long long a, unsigned long long b,
+                                                     unsigned long long c) {
+  unsigned long long r;
+  asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(r) : "l"(a), "l"(b), "l"(c));
+  return r;
+}
+
+// 32 x 32 bit transpose across the warp: lane u holds column u's mask (bit i
+// = row i) on entry and row u's mask (bit i = column i) on return.  Each
+// stage swaps the off-diagonal blocks of width j.
+__device__ __forceinline__ unsigned warp_transpose(unsigned x, int lane) {
+  const unsigned m[5] = {0x0000ffffu, 0x00ff00ffu, 0x0f0f0f0fu, 0x33333333u, 0x55555555u};
+#pragma unroll
+  for (int st = 0; st < 5; ++st) {
+    const int j = 16 >> st;
+    const unsigned y = __shfl_xor_sync(0xffffffffu, x, j);
+    x = (lane & j) ? ((x & ~m[st]) | ((y >> j) & m[st])) : ((x & m[st]) | ((y << j) & ~m[st]));
+  }
+  return x;
+}
 
 // Appends the warp's buffered pairs to the pair list.
 __device__ __forceinline__ void tile_emit(const BinScratch& b, const TileShared& sh, int lane,
@@ -129,7 +166,9 @@ __device__ __forceinline__ void tile_run(const State& s, const Geometry& g, cons
       if (self && ia > 0) rc = b.rcur[(size_t)p * nd + c];
     }
     __syncwarp();
-    sh.pa[lane] = pr;
+    sh.rx[lane] = pr.x;
+    sh.ry[lane] = pr.y;
+    sh.rz[lane] = pr.z;
     const unsigned afl = __ballot_sync(full, lane < ma && __float_as_int(pr.w) == kFluid);
     __syncwarp();
     for (int jb = self ? ia : 0; jb < nB; ++jb) {
@@ -145,18 +184,31 @@ __device__ __forceinline__ void tile_run(const State& s, const Geometry& g, cons
       const bool qfl = lane < mb && __float_as_int(pc.w) == kFluid;
       unsigned cm = 0u, bm = 0u;
       if (lane < mb) {
-        for (int i = 0; i < ma; ++i) {
-          const float4 r4 = sh.pa[i];
-          const float dx = r4.x - pc.x;
-          const float dy = r4.y - pc.y;
-          float ss = dx * dx + dy * dy;
+        // two rows per packed operation; empty row slots are far away.  Any
+        // FP32 rounding of the squared distance is within the band's margin.
+        const unsigned long long cx = f2_pack(pc.x, pc.x), cy = f2_pack(pc.y, pc.y);
+        const unsigned long long cz = f2_pack(pc.z, pc.z);
+        const unsigned long long* rx2 = reinterpret_cast<const unsigned long long*>(sh.rx);
+        const unsigned long long* ry2 = reinterpret_cast<const unsigned long long*>(sh.ry);
+        const unsigned long long* rz2 = reinterpret_cast<const unsigned long long*>(sh.rz);
+#pragma unroll
+        for (int i2 = 0; i2 < 16; ++i2) {
+          const unsigned long long dx = f2_sub(rx2[i2], cx);
+          const unsigned long long dy = f2_sub(ry2[i2], cy);
+          unsigned long long ss = f2_fma(dy, dy, f2_mul(dx, dx));
           if (DIM == 3) {
-            const float dz = r4.z - pc.z;
-            ss = ss + dz * dz;
+            const unsigned long long dz = f2_sub(rz2[i2], cz);
+            ss = f2_fma(dz, dz, ss);
           }
-          if (!(ss > k.s_hi)) {
-            cm |= 1u << i;
-            if (!(ss < k.s_lo)) bm |= 1u << i;
+          const float s0 = __uint_as_float((unsigned)ss);
+          const float s1 = __uint_as_float((unsigned)(ss >> 32));
+          if (!(s0 > k.s_hi)) {
+            cm |= 1u << (2 * i2);
+            if (!(s0 < k.s_lo)) bm |= 1u << (2 * i2);
+          }
+          if (!(s1 > k.s_hi)) {
+            cm |= 2u << (2 * i2);
+            if (!(s1 < k.s_lo)) bm |= 2u << (2 * i2);
           }
         }
         // a particle is not its own neighbour (core.jl:105)
@@ -185,14 +237,7 @@ __device__ __forceinline__ void tile_run(const State& s, const Geometry& g, cons
         }
       }
       // row masks (bit u = column u); the diagonal block is symmetric
-      unsigned rm = cm;
-      if (!diag) {
-        rm = 0u;
-        for (int i = 0; i < ma; ++i) {
-          const unsigned v = __ballot_sync(full, (cm >> i) & 1u);
-          if (lane == i) rm = v;
-        }
-      }
+      const unsigned rm = diag ? cm : warp_transpose(cm, lane);
       // the column's cursor (in the diagonal block: the particle's own)
       int cc = rc;
       size_t cj = 0;
@@ -204,8 +249,14 @@ __device__ __forceinline__ void tile_run(const State& s, const Geometry& g, cons
       sh.rcur[lane] = rc;
       __syncwarp();
       // the block's pairs with their ranks in both segments; a pair neither
-      // of whose sides has a row entry is dropped
+      // of whose sides has a row entry is dropped.  A column takes its rows
+      // in ascending order, so its rank in the column's segment counts up
+      // from the cursor (in the diagonal block the bits below the lane are
+      // all of the column's bits below each row taken).
       unsigned em = diag ? (cm & below) : cm;
+      int qrank = cc;
+      const unsigned lbase = (unsigned)(32 * ia) | ((unsigned)(32 * jb + lane) << 16);
+      const unsigned mbase = ((unsigned)c << 20) | (qfl ? 0u : kQWall);
       for (;;) {
         const bool has = em != 0u;
         if (__ballot_sync(full, has) == 0u) break;
@@ -214,19 +265,17 @@ __device__ __forceinline__ void tile_run(const State& s, const Geometry& g, cons
         if (has) {
           const int i = __ffs(em) - 1;
           em &= em - 1u;
-          unsigned pr_ = kRankNone, qr_ = kRankNone;
-          if ((afl >> i) & 1u) {
+          const bool pfl = (afl >> i) & 1u;
+          unsigned pr_ = kRankNone;
+          if (pfl) {
             const int v = sh.rcur[i] + __popc(sh.rmask[i] & below);
             if (v < cap) pr_ = (unsigned)v;
           }
-          if (qfl) {
-            const int v = cc + __popc(cm & ((1u << i) - 1u));
-            if (v < cap) qr_ = (unsigned)v;
-          }
-          keep = pr_ != kRankNone || qr_ != kRankNone;
-          meta = pr_ | (qr_ << 10) | ((unsigned)c << 20) | (((afl >> i) & 1u) ? 0u : kPWall) |
-                 (qfl ? 0u : kQWall);
-          loc = (unsigned)(32 * ia + i) | ((unsigned)(32 * jb + lane) << 16);
+          const unsigned qr_ = (qfl && qrank < cap) ? (unsigned)qrank : kRankNone;
+          ++qrank;
+          keep = (pr_ & qr_) != kRankNone;
+          meta = pr_ | (qr_ << 10) | mbase | (pfl ? 0u : kPWall);
+          loc = lbase + (unsigned)i;
         }
         const unsigned kb = __ballot_sync(full, keep);
         if (ln + __popc(kb) > kTileList) {
