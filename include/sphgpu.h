@@ -352,7 +352,9 @@ int sph_cell_list_noalloc(const sph_params* params, int64_t n, const double* d_x
 
 /* Issue-rate microbenchmark of one arithmetic pipe on `device` (no reference
  * counterpart; the roofline denominators of the pair passes):
- * which = 0 FP64 FMA, 1 FP32 FMA, 2 FP64 add.  Returns thread-instructions/s. */
+ * which = 0 FP64 FMA, 1 FP32 FMA, 2 FP64 add, 3 int64 -> FP64 conversion,
+ * 4 FP64 FMA with a conversion beside each (FMA rate).  Returns
+ * thread-instructions/s. */
 int sph_pipe_peak(int device, int which, double* instr_per_s);
 
 #ifdef __cplusplus

@@ -167,6 +167,7 @@ size_t carve(sph_system* s, char* base, size_t C) {
     b.rows = nullptr;
     b.hit_count = nullptr;
     b.roff = b.rcur = nullptr;
+    b.xfix[0] = b.xfix[1] = b.xfix[2] = nullptr;
     b.pair_p = b.pair_q = nullptr;
     b.pair_m = nullptr;
     b.pair_cap = 0;
@@ -177,6 +178,7 @@ size_t carve(sph_system* s, char* base, size_t C) {
     b.hit_cap = D == 3 ? 384 : 160;
     b.rows = (RowEntry*)take(sizeof(RowEntry) * (size_t)b.hit_cap * C);
     b.hit_count = (int*)take(4 * C);
+    for (int d = 0; d < 3; ++d) b.xfix[d] = d < D ? (long long*)take(8 * C) : nullptr;
     b.roff = (int*)take(4 * (size_t)s->geo.n_diff * C);
     b.rcur = (int*)take(4 * (size_t)s->geo.n_diff * C);
     // unordered pairs: a fluid-fluid pair fills two row entries, so half the
@@ -381,6 +383,14 @@ static int setup_host(const sph_params* p, sph_system* s) {
   while (std::sqrt(smax) > H) smax = std::nextafter(smax, 0.0);
   while (std::sqrt(std::nextafter(smax, HUGE_VAL)) <= H) smax = std::nextafter(smax, HUGE_VAL);
   k.s_max = smax;
+  // fixed-point positions X = x 2^fx_k with |X| < 2^62 inside the domain box
+  // (particles outside it are removed by the binning)
+  double span = 0.0;
+  for (int d = 0; d < p->dim; ++d)
+    span = std::max(span, std::max(std::fabs(p->domain_min[d]), std::fabs(p->domain_max[d])));
+  int e = 0;
+  std::frexp(span, &e);  // span < 2^e
+  k.fx_k = std::max(-1000, std::min(1000, 62 - e));
   k.inv_hf = (float)k.inv_h;
   k.cwf = (float)k.cw;
   k.crf = (float)k.cr;
@@ -454,6 +464,7 @@ int sph_create(const sph_params* p, int device, sph_system** out) {
   s->b.d_cat = (unsigned long long*)(c + 1024);
   s->b.d_npairs = (unsigned long long*)(c + 1280);
   s->b.d_pover = (int*)(c + 1288);
+  s->b.d_rover = (int*)(c + 1292);
   if (cudaMemsetAsync(cells, 0, bytes, s->stream) != cudaSuccess ||
       cudaStreamSynchronize(s->stream) != cudaSuccess) {
     cudaGetLastError();

@@ -241,23 +241,13 @@ __device__ __forceinline__ void cw_count(const BinScratch& b, int c0, int c1, in
   }
 }
 
-// The pair passes' common skeleton.  list_mode 0: traverse; 3: sum the rows
-// the tile passes of this binning wrote (sph_tile64.cu), and traverse for the
-// targets whose rows overflowed (the other lanes idle meanwhile).
+// The pair passes' common skeleton: the traversal of the warp's item (the
+// density and force passes of a step sum rows instead, sph_pair64.cu, and
+// come here only for targets whose rows overflowed).
 template <int DIM, int OP, class P>
 __device__ __forceinline__ void cw_pass(const State& s, const Geometry& g, const Consts& k,
                                         const BinScratch& b, CwShared& sh, int lane,
-                                        const CwTarget& t, P& proc, int list_mode) {
-  if (list_mode == 3) {
-    const int cnt = t.active ? __ldg(&b.hit_count[t.i]) : 0;
-    const bool over = cnt > b.hit_cap || (t.active && *b.d_pover != 0);
-    if (t.active && !over) proc.rows(b, t.i, cnt);
-    if (!__any_sync(0xffffffffu, over)) return;
-    CwTarget u = t;
-    u.active = over;
-    cw_traverse<DIM, OP == SPH_OP_WALL_PRESSURE>(s, g, k, b, sh, lane, u, proc);
-    return;
-  }
+                                        const CwTarget& t, P& proc, int) {
   cw_traverse<DIM, OP == SPH_OP_WALL_PRESSURE>(s, g, k, b, sh, lane, t, proc);
 }
 

@@ -72,6 +72,9 @@ struct Consts {
   double s_max;
   // folded constants of the FP64 pair arithmetic: m C_w, m C_r, -(alpha c0) h_smooth
   double mcw, mcr, ca;
+  // scale of the positions' fixed-point copies: X = x 2^fx_k, |X| < 2^62
+  // over the domain box
+  int fx_k;
   // FP32 copies for the mixed-precision pair arithmetic
   float inv_hf, cwf, crf, massf, eta2f, alpha_c0f, h_smoothf, rho0f;
   float gf[3];
@@ -93,11 +96,12 @@ __device__ __forceinline__ void row_store(RowEntry* e, unsigned long long q, dou
 }
 
 // a row entry written by an earlier kernel
-__device__ __forceinline__ void row_load(const RowEntry* e, unsigned long long& q, double& a,
-                                         double& b) {
-  double c;
-  asm("ld.global.nc.v4.b64 {%0, %1, %2, %3}, [%4];" : "=l"(q), "=d"(a), "=d"(b), "=d"(c) : "l"(e));
-  (void)c;
+__device__ __forceinline__ RowEntry row_load(const RowEntry* e) {
+  RowEntry r;
+  asm("ld.global.nc.v4.b64 {%0, %1, %2, %3}, [%4];"
+      : "=l"(r.q), "=d"(r.a), "=d"(r.b), "=d"(r.c)
+      : "l"(e));
+  return r;
 }
 
 // Scratch of the binning (counting sort by cell key).
@@ -136,6 +140,7 @@ struct BinScratch {
   // uses the rows of its own targets as scratch.
   RowEntry* rows;
   int* hit_count;
+  long long* xfix[3];  // positions as exact fixed-point integers (fx_fix), per step
   int* roff;          // n_diff per particle: first entry of each slot's segment
   int* rcur;          // n_diff per particle: hits per slot
   int hit_cap;
@@ -147,6 +152,7 @@ struct BinScratch {
   long long pair_cap;
   unsigned long long* d_npairs;  // pairs listed (may exceed pair_cap)
   int* d_pover;                  // the list overflowed: every target traverses
+  int* d_rover;                  // some target's row overflowed (it traverses)
   int* cell_fluid;    // key_max + 3: fluid particles per cell
   // mixed-precision passes: one 32-bit hit mask per lane and 32-candidate
   // chunk of the neighbour sequence (sph_pair32.cu); item j of cell k owns
@@ -245,6 +251,74 @@ __device__ __forceinline__ bool within_rn(const State& s, const Consts& k, const
     ss = __dadd_rn(ss, __dmul_rn(d2, d2));
   }
   return !(ss > k.s_max);
+}
+
+// Exact position differences on the integer pipes.  GB300 executes FP64
+// arithmetic and int64 <-> FP64 conversions on one slow pipe, so the
+// separations x_p - x_q of the FP64 pair passes are formed from fixed-point
+// copies X = x 2^k: D = X_p - X_q is the exact difference in units of 2^-k,
+// and RN(D) 2^-k = RN(x_p - x_q) is the correctly rounded FP64 subtraction
+// (scaling by a power of two commutes with rounding in the normal range).
+// A position without an exact copy (|x| below 2^(52-k), -0, subnormal or
+// out of range) takes the FP64 subtraction.
+constexpr long long kFxNone = (long long)0x8000000000000000ull;
+
+__device__ __forceinline__ long long fx_fix(double x, int k) {
+  const unsigned long long b = (unsigned long long)__double_as_longlong(x);
+  const int E = (int)((b >> 52) & 0x7ff);
+  if (E == 0) return b == 0ull ? 0 : kFxNone;  // +0 is exact; -0 and subnormals are not
+  if (E == 0x7ff) return kFxNone;
+  const unsigned long long m = (b & 0xfffffffffffffull) | (1ull << 52);
+  const int t = E - 1075 + k;
+  unsigned long long X;
+  if (t >= 0) {
+    if (t > 9) return kFxNone;  // |X| >= 2^62
+    X = m << t;
+  } else {
+    if (t < -52 || (m & ((1ull << -t) - 1ull)) != 0ull) return kFxNone;  // not a multiple of 2^-k
+    X = m >> -t;
+  }
+  return (b >> 63) ? -(long long)X : (long long)X;
+}
+
+// RN(X_p - X_q) 2^-k as a double (ties to even), both copies exact
+__device__ __forceinline__ double fx_diff(long long Xp, long long Xq, int k) {
+  const long long D = Xp - Xq;
+  if (D == 0) return 0.0;
+  const unsigned long long neg = (unsigned long long)(D >> 63);
+  const unsigned long long a = ((unsigned long long)D ^ neg) - neg;
+  const int L = 63 - __clzll((long long)a);  // the leading one
+  unsigned long long m;
+  if (L <= 52) {
+    m = a << (52 - L);
+  } else {
+    const int sh = L - 52;
+    m = a >> sh;
+    const unsigned long long rem = a & ((1ull << sh) - 1ull), half = 1ull << (sh - 1);
+    m += (rem > half || (rem == half && (m & 1ull))) ? 1ull : 0ull;
+  }
+  // m holds the leading one at bit 52 (or 2^53 after rounding up): adding it
+  // to the exponent field one below the leading one's places it exactly
+  return __longlong_as_double((long long)((neg & 0x8000000000000000ull) +
+                                          ((unsigned long long)(L - k + 1022) << 52) + m));
+}
+
+// The FP64 subtraction for positions without exact copies, out of line so
+// that it is not evaluated speculatively beside the integer path.
+static __device__ __noinline__ double fx_fallback(double xp, const double* xq) { return xp - __ldg(xq); }
+
+// x_p - x_q along axis d, with p's own copy Xp and position xp at hand
+__device__ __forceinline__ double fx_sep1(long long Xp, const double* xp, const State& s,
+                                          const long long* const* xfix, int k, int d, int q) {
+  const long long Xq = __ldg(&xfix[d][q]);
+  if (Xp == kFxNone || Xq == kFxNone) return fx_fallback(__ldg(xp), &s.x[d][q]);
+  return fx_diff(Xp, Xq, k);
+}
+
+// x_p - x_q along axis d: from the fixed-point copies when both are exact
+__device__ __forceinline__ double fx_sep(const State& s, const long long* const* xfix, int k,
+                                         int d, int p, int q) {
+  return fx_sep1(__ldg(&xfix[d][p]), &s.x[d][p], s, xfix, k, d, q);
 }
 
 __device__ __forceinline__ unsigned lanemask_lt() {

@@ -23,6 +23,19 @@ inline void mark(const LaunchCtx& c, int kernel, int phase, int kernels = 1) {
   if (c.mark) c.mark(c.owner, kernel, phase, kernels);
 }
 
+// Blocks of one resident wave of `kernel` on the current device (kernels
+// whose warps stride over their work launch this many: blocks beyond the
+// resident ones would only start after the first wave).
+template <class K>
+int resident_blocks(K kernel, int threads) {
+  int dev = 0, sms = 0, per_sm = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, threads, 0);
+  cudaGetLastError();
+  return (sms > 0 ? sms : 1) * (per_sm > 0 ? per_sm : 1);
+}
+
 // Fields moved by the reorder gather.
 constexpr int kGatherAll = 1;   // every field (create_cell_list!)
 constexpr int kGatherStep = 0;  // only what survives a fused step (x, v, rho_ref, ids)
@@ -96,6 +109,9 @@ cudaError_t launch_pair_fp64(const LaunchCtx& c, const State& s, const Geometry&
 // pressure and XSPH factors into the rows.  Launches kTilesLaunches[phase]
 // kernels.
 constexpr int kTilesLaunches[2] = {3, 1};
+// launches of the density (0) and force (1) passes of a step: the tile
+// kernels, the row sums and the traversal of overflowed rows
+constexpr int kRowPassLaunches[2] = {kTilesLaunches[0] + 2, kTilesLaunches[1] + 2};
 cudaError_t launch_tiles_fp64(const LaunchCtx& c, const State& s, const Geometry& g,
                               const Consts& k, const BinScratch& b, int cap, int phase);
 // ---- mixed-precision pair passes (sph_pair32.cu)

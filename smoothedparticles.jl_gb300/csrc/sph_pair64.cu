@@ -28,6 +28,8 @@
 // than 2^-18 h^2.  The band [h^2 (1 - 2^-14), h^2 (1 + 2^-14)] is 16x wider
 // than that, and outside the band the reference's test sqrt(fl64(s)) > h
 // cannot disagree with the FP32 decision.
+#include <algorithm>
+
 #include "sph_cellwarp.cuh"
 #include "sph_launch.h"
 #include "sphgpu.h"
@@ -133,20 +135,23 @@ struct Proc64 {
       c0 += cnt;
     } else if (OP == SPH_OP_FORCE) {
       const int n = *b.d_n;
+      // the separations from the fixed-point copies (exact, integer pipes)
+      const long long X0 = b.xfix[0][i], X1 = b.xfix[1][i];
+      const long long X2 = DIM == 3 ? b.xfix[2][i] : 0;
       for (int j = 0; j < cnt; ++j) {
-        unsigned long long e;
-        double cf, wx;
-        row_load(row + j, e, cf, wx);
+        const RowEntry en = row_load(row + j);
+        const unsigned long long e = en.q;
+        const double cf = en.a, wx = en.b;
         const int q = (int)(e & 0x7fffffffu);
         if (q >= n) {  // an entry the tile passes did not write: report, skip
           atomicOr(b.d_err, kErrBounds);
           continue;
         }
-        const double d0 = xp[0] - __ldg(&s.x[0][q]);
-        const double d1 = xp[1] - __ldg(&s.x[1][q]);
+        const double d0 = fx_sep1(X0, &s.x[0][i], s, b.xfix, k.fx_k, 0, q);
+        const double d1 = fx_sep1(X1, &s.x[1][i], s, b.xfix, k.fx_k, 1, q);
         ax = __fma_rn(cf, d0, ax);
         ay = __fma_rn(cf, d1, ay);
-        if (DIM == 3) az = __fma_rn(cf, xp[2] - __ldg(&s.x[2][q]), az);
+        if (DIM == 3) az = __fma_rn(cf, fx_sep1(X2, &s.x[2][i], s, b.xfix, k.fx_k, 2, q), az);
         if ((e & 0x80000000u) == 0u) {
           // fluid neighbour: + wx (v_q - v_p)
           sx = __fma_rn(-wx, vp[0] - __ldg(&s.v[0][q]), sx);
@@ -161,111 +166,163 @@ struct Proc64 {
   }
 };
 
+// A target's accumulators start at the stored value (apply! accumulates) or
+// at 0; the force also needs the target's own velocity, density and P/rho^2.
+template <int DIM, int OP>
+__device__ __forceinline__ void target_prologue(const State& s, int i, int reset,
+                                                Proc64<DIM, OP>& p) {
+  if (OP == SPH_OP_DENSITY) {
+    if (!reset) p.acc = s.rho[i];
+  } else if (OP == SPH_OP_DENSITY_REF) {
+    if (!reset) p.acc = s.rho_ref[i];
+  } else if (OP == SPH_OP_FORCE) {
+    if (!reset) {
+      p.ax = s.a[0][i]; p.ay = s.a[1][i];
+      p.sx = s.xs[0][i]; p.sy = s.xs[1][i];
+      if (DIM == 3) { p.az = s.a[2][i]; p.sz = s.xs[2][i]; }
+    }
+#pragma unroll
+    for (int d = 0; d < DIM; ++d) p.vp[d] = s.v[d][i];
+    p.rhop = s.rho[i];
+    p.prp = s.Pr[i];
+  }
+}
+
+// A folded reset_*! still zeroes the targets the operator skips.
+template <int DIM, int OP>
+__device__ __forceinline__ void skipped_target(const State& s, int i, int reset) {
+  if (!reset) return;
+  if (OP == SPH_OP_DENSITY) {
+    s.rho[i] = 0.0;
+  } else if (OP == SPH_OP_DENSITY_REF) {
+    s.rho_ref[i] = 0.0;
+  } else if (OP == SPH_OP_FORCE) {
+#pragma unroll
+    for (int d = 0; d < DIM; ++d) { s.a[d][i] = 0.0; s.xs[d][i] = 0.0; }
+  }
+}
+
+// The epilogue of an acted-on target: self term (core.jl:155-157), fused
+// EOS, stores.
+template <int DIM, int OP>
+__device__ __forceinline__ void target_epilogue(const State& s, const Consts& k, int i,
+                                                const Proc64<DIM, OP>& p, int self, int fuse_eos) {
+  if (OP == SPH_OP_DENSITY || OP == SPH_OP_DENSITY_REF) {
+    double acc = p.acc;
+    if (self) acc = acc + k.mass * ker_w(k, 0.0);
+    if (OP == SPH_OP_DENSITY) {
+      s.rho[i] = acc;
+      if (fuse_eos) {
+        const double ratio = acc / s.rho_ref[i];
+        const double r2 = ratio * ratio;
+        const double r4 = r2 * r2;
+        const double r7 = (r4 * r2) * ratio;
+        const double P = k.B * (r7 - 1.0);
+        s.P[i] = P;
+        s.Pr[i] = P / (acc * acc);
+      }
+    } else {
+      s.rho_ref[i] = acc;
+    }
+  } else if (OP == SPH_OP_WALL_PRESSURE) {
+    const double P = p.ws > 0.0 ? (p.wp + p.wg) / p.ws : 0.0;
+    s.P[i] = P;
+    s.Pr[i] = P / (k.rho0 * k.rho0);
+    s.rho[i] = k.rho0;
+  } else {
+    double ax = p.ax, ay = p.ay, az = p.az, sx = p.sx, sy = p.sy, sz = p.sz;
+    if (self) {
+      const double ker = k.mass * ker_rdw(k, 0.0);
+      const double inv_rb = 2.0 / (p.rhop + p.rhop);
+      const double cf = -ker * ((p.prp + p.prp) + 0.0);
+      const double wx = (k.mass * ker_w(k, 0.0)) * inv_rb;
+      ax = ax + cf * 0.0;
+      ay = ay + cf * 0.0;
+      az = az + cf * 0.0;
+      sx = sx + wx * (p.vp[0] - p.vp[0]);
+      sy = sy + wx * (p.vp[1] - p.vp[1]);
+      sz = sz + wx * (p.vp[2] - p.vp[2]);
+    }
+    s.a[0][i] = ax;
+    s.a[1][i] = ay;
+    s.xs[0][i] = sx;
+    s.xs[1][i] = sy;
+    if (DIM == 3) {
+      s.a[2][i] = az;
+      s.xs[2][i] = sz;
+    }
+  }
+}
+
+// One warp per work item; the warps stride over the items (one resident
+// wave of blocks, so that a launch with little to do costs little).
 template <int DIM, int OP, int WARPS>
 __global__ void __launch_bounds__(32 * WARPS) pair64_kernel(State s, Geometry g, Consts k,
                                                             BinScratch b, int self, int reset,
-                                                            int fuse_eos, int list_mode) {
+                                                            int fuse_eos, int list_mode,
+                                                            int warps_total) {
   __shared__ CwShared shared[WARPS];
   const int lane = threadIdx.x & 31;
   const int w = threadIdx.x >> 5;
-  const int item = blockIdx.x * WARPS + w;
-  int first = 0, count = 0;
-  if (!cw_item(b, g, item, first, count)) return;  // warp-uniform
-  const int i = first + lane;
-  const bool valid = lane < count;
-  const int ti = valid ? s.type[i] : -1;
+  // list_mode 3: row_sum_kernel took every target whose row is complete;
+  // only overflowed rows traverse here
+  if (list_mode == 3 && *b.d_rover == 0 && *b.d_pover == 0) return;
+  const int total = __ldg(&b.item_off[g.key_max + 1]);
   // the wall pressure acts on wall targets, every other operator on fluid ones
   const int want = OP == SPH_OP_WALL_PRESSURE ? kWall : kFluid;
-  CwTarget t;
-  t.active = valid && ti == want;
-  t.i = i;
-  t.key = s.cell[first];
-  decode_key(g, t.key, t.cx, t.cy, t.cz);
-  t.pi4 = valid ? s.pl[i] : make_float4(0.f, 0.f, 0.f, 0.f);
-  t.xp[0] = valid ? s.x[0][i] : 0.0;
-  t.xp[1] = valid ? s.x[1][i] : 0.0;
-  t.xp[2] = (DIM == 3 && valid) ? s.x[2][i] : 0.0;
-  Proc64<DIM, OP> p(s, k);
-  p.xp[0] = t.xp[0];
-  p.xp[1] = t.xp[1];
-  p.xp[2] = t.xp[2];
-  if (t.active) {
-    // accumulators start at the stored value (apply! accumulates) or at 0
-    if (OP == SPH_OP_DENSITY) {
-      if (!reset) p.acc = s.rho[i];
-    } else if (OP == SPH_OP_DENSITY_REF) {
-      if (!reset) p.acc = s.rho_ref[i];
-    } else if (OP == SPH_OP_FORCE) {
-      if (!reset) {
-        p.ax = s.a[0][i]; p.ay = s.a[1][i];
-        p.sx = s.xs[0][i]; p.sy = s.xs[1][i];
-        if (DIM == 3) { p.az = s.a[2][i]; p.sz = s.xs[2][i]; }
-      }
-#pragma unroll
-      for (int d = 0; d < DIM; ++d) p.vp[d] = s.v[d][i];
-      p.rhop = s.rho[i];
-      p.prp = s.Pr[i];
-    }
+  for (int item = blockIdx.x * WARPS + w; item < total; item += warps_total) {
+    const int2 it = __ldg(&b.items[item]);
+    const int first = it.x, count = it.y;
+    const int i = first + lane;
+    const bool valid = lane < count;
+    const int ti = valid ? s.type[i] : -1;
+    CwTarget t;
+    t.active = valid && ti == want;
+    if (list_mode == 3)
+      t.active = t.active && (__ldg(&b.hit_count[i]) > b.hit_cap || *b.d_pover != 0);
+    else if (valid && ti != want)
+      skipped_target<DIM, OP>(s, i, reset);
+    // an item without targets of the operator has nothing to traverse
+    if (!__any_sync(0xffffffffu, t.active)) continue;
+    t.i = i;
+    t.key = s.cell[first];
+    decode_key(g, t.key, t.cx, t.cy, t.cz);
+    t.pi4 = valid ? s.pl[i] : make_float4(0.f, 0.f, 0.f, 0.f);
+    t.xp[0] = valid ? s.x[0][i] : 0.0;
+    t.xp[1] = valid ? s.x[1][i] : 0.0;
+    t.xp[2] = (DIM == 3 && valid) ? s.x[2][i] : 0.0;
+    Proc64<DIM, OP> p(s, k);
+    p.xp[0] = t.xp[0];
+    p.xp[1] = t.xp[1];
+    p.xp[2] = t.xp[2];
+    if (t.active) target_prologue<DIM, OP>(s, i, reset, p);
+    cw_pass<DIM, OP>(s, g, k, b, shared[w], lane, t, p, 0);
+    if (t.active) target_epilogue<DIM, OP>(s, k, i, p, self, fuse_eos);
+    cw_count<OP>(b, p.c0, p.c1, p.c2);
   }
-  cw_pass<DIM, OP>(s, g, k, b, shared[w], lane, t, p, list_mode);
+}
 
-  if (valid && !t.active) {
-    // a folded reset_*! still zeroes the targets the operator skips
-    if (reset) {
-      if (OP == SPH_OP_DENSITY) {
-        s.rho[i] = 0.0;
-      } else if (OP == SPH_OP_DENSITY_REF) {
-        s.rho_ref[i] = 0.0;
-      } else if (OP == SPH_OP_FORCE) {
-#pragma unroll
-        for (int d = 0; d < DIM; ++d) { s.a[d][i] = 0.0; s.xs[d][i] = 0.0; }
-      }
-    }
-  } else if (t.active) {
-    // epilogue: self term (core.jl:155-157), fused EOS, stores
-    if (OP == SPH_OP_DENSITY || OP == SPH_OP_DENSITY_REF) {
-      double acc = p.acc;
-      if (self) acc = acc + k.mass * ker_w(k, 0.0);
-      if (OP == SPH_OP_DENSITY) {
-        s.rho[i] = acc;
-        if (fuse_eos) {
-          const double ratio = acc / s.rho_ref[i];
-          const double r2 = ratio * ratio;
-          const double r4 = r2 * r2;
-          const double r7 = (r4 * r2) * ratio;
-          const double P = k.B * (r7 - 1.0);
-          s.P[i] = P;
-          s.Pr[i] = P / (acc * acc);
-        }
-      } else {
-        s.rho_ref[i] = acc;
-      }
-    } else if (OP == SPH_OP_WALL_PRESSURE) {
-      const double P = p.ws > 0.0 ? (p.wp + p.wg) / p.ws : 0.0;
-      s.P[i] = P;
-      s.Pr[i] = P / (k.rho0 * k.rho0);
-      s.rho[i] = k.rho0;
+// The density and force passes of a step over the rows the tile passes
+// wrote (sph_tile64.cu): one thread per particle; targets whose rows
+// overflowed are left to pair64_kernel.
+template <int DIM, int OP>
+__global__ void __launch_bounds__(256) row_sum_kernel(State s, Consts k, BinScratch b, int self,
+                                                      int reset, int fuse_eos) {
+  const int n = *b.d_n;
+  const int i = blockIdx.x * 256 + threadIdx.x;
+  Proc64<DIM, OP> p(s, k);
+  if (i < n) {
+    if (s.type[i] != kFluid) {
+      skipped_target<DIM, OP>(s, i, reset);
     } else {
-      double ax = p.ax, ay = p.ay, az = p.az, sx = p.sx, sy = p.sy, sz = p.sz;
-      if (self) {
-        const double ker = k.mass * ker_rdw(k, 0.0);
-        const double inv_rb = 2.0 / (p.rhop + p.rhop);
-        const double cf = -ker * ((p.prp + p.prp) + 0.0);
-        const double wx = (k.mass * ker_w(k, 0.0)) * inv_rb;
-        ax = ax + cf * 0.0;
-        ay = ay + cf * 0.0;
-        az = az + cf * 0.0;
-        sx = sx + wx * (p.vp[0] - p.vp[0]);
-        sy = sy + wx * (p.vp[1] - p.vp[1]);
-        sz = sz + wx * (p.vp[2] - p.vp[2]);
-      }
-      s.a[0][i] = ax;
-      s.a[1][i] = ay;
-      s.xs[0][i] = sx;
-      s.xs[1][i] = sy;
-      if (DIM == 3) {
-        s.a[2][i] = az;
-        s.xs[2][i] = sz;
+      const int cnt = __ldg(&b.hit_count[i]);
+      if (cnt <= b.hit_cap && *b.d_pover == 0) {
+        p.xp[0] = s.x[0][i];
+        p.xp[1] = s.x[1][i];
+        p.xp[2] = DIM == 3 ? s.x[2][i] : 0.0;
+        target_prologue<DIM, OP>(s, i, reset, p);
+        p.rows(b, i, cnt);
+        target_epilogue<DIM, OP>(s, k, i, p, self, fuse_eos);
       }
     }
   }
@@ -377,45 +434,64 @@ __global__ void __launch_bounds__(128) debug_pairs_kernel(State s, Geometry g, C
   }
   if (!pass) counts[rid] = cnt;
 }
+// pair64_kernel with one warp per work item (the block scheduler balances
+// the uneven items), or, for the sweep over overflowed rows (list_mode 3,
+// usually nothing to do), one resident wave of blocks striding over them
+template <int DIM, int OP, int WARPS>
+void pair64_launch(cudaStream_t st, const BinScratch& b, int threads, const State& s,
+                   const Geometry& g, const Consts& k, const BinScratch& bb, int self, int reset,
+                   int fuse_eos, int list_mode) {
+  static const int wave = resident_blocks(pair64_kernel<DIM, OP, WARPS>, 32 * WARPS);
+  const int all = std::max(1, (b.max_items + WARPS - 1) / WARPS);
+  const int blocks = list_mode == 3 ? std::min(all, wave) : all;
+  pair64_kernel<DIM, OP, WARPS><<<blocks, threads, 0, st>>>(s, g, k, bb, self, reset, fuse_eos,
+                                                           list_mode, blocks * WARPS);
+}
+
 template <int DIM>
 cudaError_t launch_pair_dim(const LaunchCtx& c, const State& s, const Geometry& g,
                             const Consts& k, const BinScratch& b, int cap, int op, int self,
                             int reset, int fuse_eos, int list_mode) {
   const int W = k.warps;
-  const int blocks = (b.max_items + W - 1) / W;
   const int kid = op == SPH_OP_FORCE           ? SPH_KERNEL_FORCE
                   : op == SPH_OP_WALL_PRESSURE ? SPH_KERNEL_WALL
                                                : SPH_KERNEL_DENSITY;
   mark(c, kid, 0);
   // the density and force passes of a step: every pair evaluated once into
-  // the rows (sph_tile64.cu), which the pass below then sums
+  // the rows (sph_tile64.cu), the rows summed, then the traversal of the
+  // targets whose rows overflowed (its warps return at once otherwise)
   if (list_mode == 3) {
     const cudaError_t e = launch_tiles_fp64(c, s, g, k, b, cap, op == SPH_OP_FORCE ? 1 : 0);
     if (e != cudaSuccess) return e;
+    const int rb = (cap + 255) / 256;
+    if (op == SPH_OP_FORCE)
+      row_sum_kernel<DIM, SPH_OP_FORCE><<<rb, 256, 0, c.stream>>>(s, k, b, self, reset, 0);
+    else
+      row_sum_kernel<DIM, SPH_OP_DENSITY><<<rb, 256, 0, c.stream>>>(s, k, b, self, reset, fuse_eos);
   }
   switch (op) {
     case SPH_OP_DENSITY:
-      if (W == 2) pair64_kernel<DIM, SPH_OP_DENSITY, 2><<<blocks, 64, 0, c.stream>>>(s, g, k, b, self, reset, fuse_eos, list_mode);
-      else if (W == 8) pair64_kernel<DIM, SPH_OP_DENSITY, 8><<<blocks, 256, 0, c.stream>>>(s, g, k, b, self, reset, fuse_eos, list_mode);
-      else pair64_kernel<DIM, SPH_OP_DENSITY, 4><<<blocks, 128, 0, c.stream>>>(s, g, k, b, self, reset, fuse_eos, list_mode);
+      if (W == 2) pair64_launch<DIM, SPH_OP_DENSITY, 2>(c.stream, b, 64, s, g, k, b, self, reset, fuse_eos, list_mode);
+      else if (W == 8) pair64_launch<DIM, SPH_OP_DENSITY, 8>(c.stream, b, 256, s, g, k, b, self, reset, fuse_eos, list_mode);
+      else pair64_launch<DIM, SPH_OP_DENSITY, 4>(c.stream, b, 128, s, g, k, b, self, reset, fuse_eos, list_mode);
       break;
     case SPH_OP_DENSITY_REF:
-      if (W == 2) pair64_kernel<DIM, SPH_OP_DENSITY_REF, 2><<<blocks, 64, 0, c.stream>>>(s, g, k, b, self, reset, 0, 0);
-      else if (W == 8) pair64_kernel<DIM, SPH_OP_DENSITY_REF, 8><<<blocks, 256, 0, c.stream>>>(s, g, k, b, self, reset, 0, 0);
-      else pair64_kernel<DIM, SPH_OP_DENSITY_REF, 4><<<blocks, 128, 0, c.stream>>>(s, g, k, b, self, reset, 0, 0);
+      if (W == 2) pair64_launch<DIM, SPH_OP_DENSITY_REF, 2>(c.stream, b, 64, s, g, k, b, self, reset, 0, 0);
+      else if (W == 8) pair64_launch<DIM, SPH_OP_DENSITY_REF, 8>(c.stream, b, 256, s, g, k, b, self, reset, 0, 0);
+      else pair64_launch<DIM, SPH_OP_DENSITY_REF, 4>(c.stream, b, 128, s, g, k, b, self, reset, 0, 0);
       break;
     case SPH_OP_WALL_PRESSURE:
-      if (W == 2) pair64_kernel<DIM, SPH_OP_WALL_PRESSURE, 2><<<blocks, 64, 0, c.stream>>>(s, g, k, b, 0, 0, 0, 0);
-      else if (W == 8) pair64_kernel<DIM, SPH_OP_WALL_PRESSURE, 8><<<blocks, 256, 0, c.stream>>>(s, g, k, b, 0, 0, 0, 0);
-      else pair64_kernel<DIM, SPH_OP_WALL_PRESSURE, 4><<<blocks, 128, 0, c.stream>>>(s, g, k, b, 0, 0, 0, 0);
+      if (W == 2) pair64_launch<DIM, SPH_OP_WALL_PRESSURE, 2>(c.stream, b, 64, s, g, k, b, 0, 0, 0, 0);
+      else if (W == 8) pair64_launch<DIM, SPH_OP_WALL_PRESSURE, 8>(c.stream, b, 256, s, g, k, b, 0, 0, 0, 0);
+      else pair64_launch<DIM, SPH_OP_WALL_PRESSURE, 4>(c.stream, b, 128, s, g, k, b, 0, 0, 0, 0);
       break;
     default:
-      if (W == 2) pair64_kernel<DIM, SPH_OP_FORCE, 2><<<blocks, 64, 0, c.stream>>>(s, g, k, b, self, reset, 0, list_mode);
-      else if (W == 8) pair64_kernel<DIM, SPH_OP_FORCE, 8><<<blocks, 256, 0, c.stream>>>(s, g, k, b, self, reset, 0, list_mode);
-      else pair64_kernel<DIM, SPH_OP_FORCE, 4><<<blocks, 128, 0, c.stream>>>(s, g, k, b, self, reset, 0, list_mode);
+      if (W == 2) pair64_launch<DIM, SPH_OP_FORCE, 2>(c.stream, b, 64, s, g, k, b, self, reset, 0, list_mode);
+      else if (W == 8) pair64_launch<DIM, SPH_OP_FORCE, 8>(c.stream, b, 256, s, g, k, b, self, reset, 0, list_mode);
+      else pair64_launch<DIM, SPH_OP_FORCE, 4>(c.stream, b, 128, s, g, k, b, self, reset, 0, list_mode);
       break;
   }
-  mark(c, kid, 1, list_mode == 3 ? 1 + kTilesLaunches[op == SPH_OP_FORCE ? 1 : 0] : 1);
+  mark(c, kid, 1, list_mode == 3 ? kRowPassLaunches[op == SPH_OP_FORCE ? 1 : 0] : 1);
   return cudaGetLastError();
 }
 

@@ -28,10 +28,57 @@ __global__ void add_chains(double* out, int iters, double b) {
   out[blockIdx.x * blockDim.x + threadIdx.x] = x0 + x1 + x2 + x3 + x4 + x5 + x6 + x7;
 }
 
+// int64 -> double conversions (round to nearest), 8 independent chains
+__global__ void i2f_chains(double* out, int iters) {
+  long long k[8];
+  double d[8];
+#pragma unroll
+  for (int j = 0; j < 8; ++j) {
+    k[j] = (long long)threadIdx.x * 7919 + j;
+    d[j] = 0.0;
+  }
+  for (int i = 0; i < iters; ++i) {
+#pragma unroll
+    for (int j = 0; j < 8; ++j) {
+      d[j] = __ll2double_rn(k[j]);
+      k[j] = __double_as_longlong(d[j]) ^ (long long)i;
+    }
+  }
+  double s = 0.0;
+#pragma unroll
+  for (int j = 0; j < 8; ++j) s += d[j];
+  out[blockIdx.x * blockDim.x + threadIdx.x] = s;
+}
+
+// 8 FP64 FMA chains with one int64 -> double conversion beside each FMA:
+// at the FMA rate of fma_chains when the conversions take another pipe
+__global__ void fma_i2f_chains(double* out, int iters, double a, double b) {
+  double x[8], d[8];
+  long long k[8];
+#pragma unroll
+  for (int j = 0; j < 8; ++j) {
+    x[j] = threadIdx.x + j;
+    k[j] = (long long)threadIdx.x * 7919 + j;
+    d[j] = 0.0;
+  }
+  for (int i = 0; i < iters; ++i) {
+#pragma unroll
+    for (int j = 0; j < 8; ++j) {
+      x[j] = x[j] * a + b;
+      d[j] = __ll2double_rn(k[j]);
+      k[j] = __double_as_longlong(d[j]) ^ (long long)i;
+    }
+  }
+  double s = 0.0;
+#pragma unroll
+  for (int j = 0; j < 8; ++j) s += x[j] + d[j];
+  out[blockIdx.x * blockDim.x + threadIdx.x] = s;
+}
+
 }  // namespace
 
 extern "C" int sph_pipe_peak(int device, int which, double* instr_per_s) {
-  if (!instr_per_s || which < 0 || which > 2) return SPH_ERR_ARG;
+  if (!instr_per_s || which < 0 || which > 4) return SPH_ERR_ARG;
   int prev = 0;
   if (cudaGetDevice(&prev) != cudaSuccess || cudaSetDevice(device) != cudaSuccess) {
     cudaGetLastError();
@@ -57,8 +104,12 @@ extern "C" int sph_pipe_peak(int device, int which, double* instr_per_s) {
         fma_chains<double><<<blocks, threads, 0, st>>>((double*)buf, iters, 0.999, 1e-3);
       else if (which == 1)
         fma_chains<float><<<blocks, threads, 0, st>>>((float*)buf, iters, 0.999f, 1e-3f);
-      else
+      else if (which == 2)
         add_chains<<<blocks, threads, 0, st>>>((double*)buf, iters, 1e-3);
+      else if (which == 3)
+        i2f_chains<<<blocks, threads, 0, st>>>((double*)buf, iters);
+      else
+        fma_i2f_chains<<<blocks, threads, 0, st>>>((double*)buf, iters, 0.999, 1e-3);
       cudaEventRecord(e1, st);
       float ms = 0.f;
       if (cudaEventSynchronize(e1) != cudaSuccess || cudaEventElapsedTime(&ms, e0, e1) != cudaSuccess) {

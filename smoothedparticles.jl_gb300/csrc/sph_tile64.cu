@@ -330,11 +330,15 @@ __global__ void __launch_bounds__(32 * kTileWarps) tile_kernel(State s, Geometry
   }
 }
 
-// Row offsets of every fluid target from its per-slot counts.
-__global__ void __launch_bounds__(256) row_scan_kernel(State s, Geometry g, BinScratch b) {
+// Row offsets of every fluid target from its per-slot counts; the
+// positions' fixed-point copies of every particle for the pair kernels.
+__global__ void __launch_bounds__(256) row_scan_kernel(State s, Geometry g, Consts k,
+                                                       BinScratch b) {
   const int n = *b.d_n;
   const int i = blockIdx.x * 256 + threadIdx.x;
-  if (i >= n || s.type[i] != kFluid) return;
+  if (i >= n) return;
+  for (int d = 0; d < k.dim; ++d) b.xfix[d][i] = fx_fix(s.x[d][i], k.fx_k);
+  if (s.type[i] != kFluid) return;
   const int key = s.cell[i];
   const int nd = g.n_diff;
   bool over = __ldg(&b.cell_start[key + 1]) - __ldg(&b.cell_start[key]) > 0xffff;
@@ -356,6 +360,7 @@ __global__ void __launch_bounds__(256) row_scan_kernel(State s, Geometry g, BinS
     // row to the traversal, which uses it as scratch)
     for (int c = 0; c < nd; ++c) b.roff[(size_t)i * nd + c] = kNoRow;
     run = b.hit_cap + 1;
+    *b.d_rover = 1;
   }
   b.hit_count[i] = run;
 }
@@ -390,11 +395,15 @@ __global__ void __launch_bounds__(256) pair_list_kernel(State s, Geometry g, Con
     const unsigned long long qbits = (unsigned)q | (fq ? 0u : 0x80000000u);
     const unsigned long long pbits = (unsigned)p | (fp ? 0u : 0x80000000u);
     if (PH == 0) {
-      double xp[3], d[3];
-      xp[0] = __ldg(&s.x[0][p]);
-      xp[1] = __ldg(&s.x[1][p]);
-      xp[2] = DIM == 3 ? __ldg(&s.x[2][p]) : 0.0;
-      const double r = kdist64<DIM>(s, xp, q, d);
+      // kdist64's distance, the separations formed exactly on the integer pipes
+      const double d0 = fx_sep(s, b.xfix, k.fx_k, 0, p, q);
+      const double d1 = fx_sep(s, b.xfix, k.fx_k, 1, p, q);
+      double ss = __fma_rn(d1, d1, d0 * d0);
+      if (DIM == 3) {
+        const double d2 = fx_sep(s, b.xfix, k.fx_k, 2, p, q);
+        ss = __fma_rn(d2, d2, ss);
+      }
+      const double r = sqrt(ss);
       const double t = ker_t(k, r);
       const double t2 = t * t;
       const double w = (k.mcw * (t2 * t2)) * __fma_rn(-4.0, t, 5.0);  // m W
@@ -402,9 +411,8 @@ __global__ void __launch_bounds__(256) pair_list_kernel(State s, Geometry g, Con
       if (wq) row_store(eq, pbits, w, r);
     } else {
       // m W and r as the density pass of this binning stored them
-      unsigned long long unused;
-      double w, r;
-      row_load(wp ? ep : eq, unused, w, r);
+      const RowEntry en = row_load(wp ? ep : eq);
+      const double w = en.a, r = en.b;
       const double t = ker_t(k, r);
       const double t2 = t * t;
       const double ker = k.mcr * (t2 * t);  // m rDW
@@ -412,13 +420,13 @@ __global__ void __launch_bounds__(256) pair_list_kernel(State s, Geometry g, Con
       if (fp && fq) {
         // pressure (collapse_symplectic.jl:114-118) + Monaghan viscosity +
         // XSPH, in p's direction (q's is the same factor)
-        const double d0 = __ldg(&s.x[0][p]) - __ldg(&s.x[0][q]);
-        const double d1 = __ldg(&s.x[1][p]) - __ldg(&s.x[1][q]);
+        const double d0 = fx_sep(s, b.xfix, k.fx_k, 0, p, q);
+        const double d1 = fx_sep(s, b.xfix, k.fx_k, 1, p, q);
         const double dv0 = __ldg(&s.v[0][p]) - __ldg(&s.v[0][q]);
         const double dv1 = __ldg(&s.v[1][p]) - __ldg(&s.v[1][q]);
         double vdx = __fma_rn(dv1, d1, dv0 * d0);
         if (DIM == 3) {
-          const double d2 = __ldg(&s.x[2][p]) - __ldg(&s.x[2][q]);
+          const double d2 = fx_sep(s, b.xfix, k.fx_k, 2, p, q);
           const double dv2 = __ldg(&s.v[2][p]) - __ldg(&s.v[2][q]);
           vdx = __fma_rn(dv2, d2, vdx);
         }
@@ -446,18 +454,6 @@ __global__ void __launch_bounds__(256) pair_list_kernel(State s, Geometry g, Con
   if (PH == 1) cw_warp_add(b.d_cat + kCatForceAV, av);
 }
 
-// One resident wave of a kernel (its warps stride over the work; blocks
-// beyond the resident ones would only start after the first wave).
-template <class K>
-int resident_blocks(K kernel, int threads) {
-  int dev = 0, sms = 0, per_sm = 0;
-  cudaGetDevice(&dev);
-  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, threads, 0);
-  cudaGetLastError();
-  return std::max(1, sms) * std::max(1, per_sm);
-}
-
 template <int DIM>
 void tiles_dim(cudaStream_t st, const State& s, const Geometry& g, const Consts& k,
                const BinScratch& b, int cap, int phase) {
@@ -468,9 +464,9 @@ void tiles_dim(cudaStream_t st, const State& s, const Geometry& g, const Consts&
     const long long slots = (long long)b.max_items * (g.n_diff / 2 + 1);
     const int tb = (int)std::max(
         1LL, std::min<long long>((slots + kTileWarps - 1) / kTileWarps, tile_wave));
-    cudaMemsetAsync(b.d_npairs, 0, 16, st);  // pair count and overflow flag
+    cudaMemsetAsync(b.d_npairs, 0, 16, st);  // pair count and overflow flags
     tile_kernel<DIM><<<tb, 32 * kTileWarps, 0, st>>>(s, g, k, b, tb * kTileWarps);
-    row_scan_kernel<<<(cap + 255) / 256, 256, 0, st>>>(s, g, b);
+    row_scan_kernel<<<(cap + 255) / 256, 256, 0, st>>>(s, g, k, b);
     pair_list_kernel<DIM, 0><<<dens_wave, 256, 0, st>>>(s, g, k, b, dens_wave * 256);
   } else {
     pair_list_kernel<DIM, 1><<<force_wave, 256, 0, st>>>(s, g, k, b, force_wave * 256);

@@ -451,10 +451,12 @@ def memory_estimate(params: dict, n: int, precision: int = FP64) -> int:
 
 
 def pipe_peak(which: str, device: int = 0) -> float:
-    """Measured issue rate (thread-instructions/s) of 'dfma', 'ffma' or 'dadd'."""
+    """Measured issue rate (thread-instructions/s) of 'dfma', 'ffma', 'dadd',
+    'i2f64' (int64 -> double conversion) or 'dfma_i2f' (FP64 FMAs, each with
+    a conversion beside it: the FMA rate)."""
     lib = L.load()
     out = C.c_double()
-    rc = lib.sph_pipe_peak(device, {"dfma": 0, "ffma": 1, "dadd": 2}[which], C.byref(out))
+    rc = lib.sph_pipe_peak(device, {"dfma": 0, "ffma": 1, "dadd": 2, "i2f64": 3, "dfma_i2f": 4}[which], C.byref(out))
     if rc != 0:
         raise SphError(rc, "sph_pipe_peak failed")
     return out.value
