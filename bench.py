@@ -245,7 +245,10 @@ def timed_steps(g, torch, dev, steps, world):
     return out
 
 
-def kernel_table(kst, cats):
+def kernel_table(kst, cats, steps):
+    """Per kernel family: total and per-launch time, per-step time and, for the
+    pair passes, algorithmic flops per step (the FP64 density and force passes
+    of a step are several kernels each: tiles, pair evaluation, row sums)."""
     flops = {
         "force": cats["force_fluid"] * FLOPS["force_fluid"] + cats["force_wall"] * FLOPS["force_wall"]
         + cats["force_av"] * FLOPS["force_av"],
@@ -256,9 +259,10 @@ def kernel_table(kst, cats):
     rows = {}
     for k, (tms, nl) in kst.items():
         row = {"ms_total": round(tms, 3), "launches": nl, "ms_avg": round(tms / nl, 4),
+               "ms_per_step": round(tms / max(steps, 1), 4),
                "share": round(tms / max(1e-9, tot), 4)}
         if k in flops:
-            row["flops_per_launch"] = flops[k] / nl
+            row["flops_per_step"] = flops[k] / max(steps, 1)
             row["tflops"] = round(flops[k] / (tms * 1e-3) / 1e12, 4)
         rows[k] = row
     return rows
@@ -517,7 +521,7 @@ def run_ours(args):
                  {"steps": target, "fields": field_errors(long64, longmx),
                   "note": "both runs from their own initial state (init_state of the same lattice)"}
                  if long64 is not None else None),
-             "kernels": kernel_table(rmx["kernels"], rmx["cats"]),
+             "kernels": kernel_table(rmx["kernels"], rmx["cats"], args.steps),
              "binning_hbm": None,
              "gpu_launches": rmx["launches"], "clocks": rmx["clocks"]}
     # one step from an identical FP64 state (reference density included): the
@@ -538,21 +542,23 @@ def run_ours(args):
     mixed["error_vs_fp64_one_step"] = field_errors(one_64, one_mx)
 
     # ---- roofline of the dominant kernel of the FP64 step (the force pass)
-    kt = kernel_table(r64["kernels"], r64["cats"])
+    kt = kernel_table(r64["kernels"], r64["cats"], args.steps)
     mixed["binning_hbm"] = binning_roofline(mixed["kernels"], case, True)
     dom = max((k for k in kt if "tflops" in kt[k]), key=lambda k: kt[k]["ms_total"])
     dfma = sphgpu.pipe_peak("dfma", dev)
     ffma = sphgpu.pipe_peak("ffma", dev)
     peak_tflops = 2.0 * dfma / 1e12
-    achieved = kt[dom]["flops_per_launch"] / (kt[dom]["ms_avg"] * 1e-3) / 1e12
+    achieved = kt[dom]["flops_per_step"] / (kt[dom]["ms_per_step"] * 1e-3) / 1e12
     roofline = {"bound": "fp64", "kernel": dom, "achieved": round(achieved, 4),
                 "peak": round(peak_tflops, 4), "unit": "TFLOP/s",
                 "frac": round(achieved / peak_tflops, 4),
+                "per": PASS_KERNELS.get(dom, dom),
                 "traffic": NCU_TRAFFIC.get(dom),
                 "peak_source": "measured in this run: FP64 FMA issue rate x 2 (sph_pipe_peak); "
                                "MEASURED_PEAKS.json has no FP64 figure",
                 "fp32_peak_tflops": round(2.0 * ffma / 1e12, 3),
-                "flops_per_launch": kt[dom]["flops_per_launch"],
+                "flops_per_pass": kt[dom]["flops_per_step"],
+                "ms_per_pass": kt[dom]["ms_per_step"],
                 "note": "algorithmic flops count sqrt and division as 1 each; on GB300 each costs "
                         "~10 FP64 pipe slots, and the FP64 parity path cannot fuse mul+add"}
 
@@ -586,11 +592,18 @@ def run_ours(args):
     return 0
 
 
-# DRAM bytes (read + write) per launch of the FP64 force kernel from the ncu
-# capture summarised in profiles/pair64_force_3d_dr0.0125.md (1,217,046,016 +
-# 700,111,360 B for the 1,699,240-particle dam break at dr = 0.0125), scaled by
-# particle count to the 5,746,633-particle case.
-NCU_TRAFFIC: dict = {"force": int((1217046016 + 700111360) * 5746633 / 1699240)}
+# The kernels of one FP64 force pass of a step (the roofline's unit).
+PASS_KERNELS: dict = {"force": "one force pass: pair_list_kernel (every pair once) + "
+                               "row_sum_kernel (each target's row in order) + the "
+                               "overflow sweep of pair64_kernel"}
+
+# DRAM bytes (read + write) of one FP64 force pass from the ncu capture
+# summarised in profiles/fp64_tiles_3d_dr0.025.md: pair_list_kernel 1,078,398,000
+# + 1,034,598,000 B and row_sum_kernel 1,103,097,000 + 17,072,000 B for the
+# 3D dam break at dr = 0.025 (69,489,136 pair-interactions per step), scaled by
+# pair-interactions to the 5,746,633-particle case (2,077,155,042 per step).
+NCU_TRAFFIC: dict = {"force": int((1078398000 + 1034598000 + 1103097000 + 17072000)
+                                  * 2077155042 / 69489136)}
 
 
 def main():
