@@ -357,6 +357,14 @@ int sph_cell_list_noalloc(const sph_params* params, int64_t n, const double* d_x
  * thread-instructions/s. */
 int sph_pipe_peak(int device, int which, double* instr_per_s);
 
+/* Diagnostics (no reference counterpart): the FP64 arithmetic the pair passes
+ * form on the integer pipes, applied on `device` to n host values, for tests
+ * against the IEEE operations.  op 0: a[i] - b[i] through fixed-point copies
+ * at scale 2^k (the FP64 subtraction when a value has no exact copy);
+ * 1: sqrt(a[i]); 2: 1 / a[i]; 3: 2 / a[i].  out[i] receives the result. */
+int sph_arith_check(int device, int op, int k, int n, const double* a, const double* b,
+                    double* out);
+
 #ifdef __cplusplus
 }
 #endif

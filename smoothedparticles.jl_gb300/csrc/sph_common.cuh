@@ -194,11 +194,105 @@ __device__ __forceinline__ bool lt0(double v) {
   return b < 0 && m != 0 && m <= 0x7FF0000000000000LL;
 }
 
+// ---- FP64 square root and reciprocal on the integer pipes ----------------
+// GB300's FP64 pipe issues 2 operations per SM per clock and a correctly
+// rounded square root or reciprocal takes ~7.5 / ~4.6 of them; the same
+// results are formed here with integer instructions (the pipes the FP64
+// passes leave idle), for positive normal inputs with normal results
+// (anything else takes the FP64 operation out of line):
+//   sqrt: s = M 2^e (M of 53 bits), e made even, sqrt(s) = sqrt(N) 2^(e/2 - 26)
+//     with N = M' 2^52 in [2^104, 2^106), so Q = floor(sqrt N) has 53 bits;
+//   1/y = (2^105 / M) 2^(-e-105), Q = floor(2^105 / M) of 53 bits.
+// Q comes from an FP32 seed (rsqrt / rcp approximations) and two Newton
+// corrections in 128-bit integers, is adjusted to the exact floor (one step
+// at most; the floor condition is then verified exactly) and rounded to
+// nearest with the exact remainder (even on a tie).
+static __device__ __noinline__ double isqrt_fallback(double s) { return sqrt(s); }
+static __device__ __noinline__ double ircp_fallback(double y) { return __drcp_rn(y); }
+
+// f 2^scale as an integer (f positive and normal, the result below 2^63)
+__device__ __forceinline__ unsigned long long f32_fix(float f, int scale) {
+  const unsigned b = __float_as_uint(f);
+  const int sh = (int)(b >> 23) - 150 + scale;
+  const unsigned long long m = (unsigned long long)((b & 0x7fffffu) | 0x800000u);
+  return sh >= 0 ? m << sh : m >> -sh;
+}
+
+// RN(sqrt(s))
+__device__ __forceinline__ double isqrt_rn(double s) {
+  const unsigned long long b = (unsigned long long)__double_as_longlong(s);
+  const int E = (int)(b >> 52);  // the sign bit makes a negative input's E >= 0x800
+  if (E <= 0 || E >= 0x7ff) return isqrt_fallback(s);
+  const unsigned long long M = (b & 0xfffffffffffffull) | (1ull << 52);
+  const int e = E - 1075;
+  const int odd = e & 1;
+  const unsigned long long M2 = M << odd;  // [2^52, 2^54)
+  const int e2 = e - odd;
+  const unsigned __int128 N = (unsigned __int128)M2 << 52;
+  // the seed: u = M2 / 2^52 in [1, 4) from the leading bits
+  const float u = __uint_as_float((M2 >> 53) ? (128u << 23) | (unsigned)((M2 >> 30) & 0x7fffffu)
+                                             : (127u << 23) | (unsigned)((M2 >> 29) & 0x7fffffu));
+  float y0;
+  asm("rsqrt.approx.ftz.f32 %0, %1;" : "=f"(y0) : "f"(u));
+  unsigned long long q = f32_fix(u * y0, 52);  // ~ sqrt(N)
+  const long long Y = (long long)f32_fix(y0, 31);
+#pragma unroll
+  for (int it = 0; it < 2; ++it) {
+    // q += (N - q^2) / (2 q), with 1/(2q) ~ y0 2^-53
+    const __int128 D = (__int128)(N - (unsigned __int128)q * q);
+    q = (unsigned long long)((long long)q + (long long)(((D >> 22) * Y) >> 62));
+  }
+  unsigned __int128 q2 = (unsigned __int128)q * q;
+  if (q2 > N) {
+    --q;
+    q2 = (unsigned __int128)q * q;
+  } else if (N - q2 > 2 * (unsigned __int128)q) {
+    ++q;
+    q2 = (unsigned __int128)q * q;
+  }
+  if (q2 > N || N - q2 > 2 * (unsigned __int128)q) return isqrt_fallback(s);
+  if (N - q2 > q) ++q;  // sqrt(N) >= q + 1/2  <=>  N - q^2 > q (never a tie)
+  return __longlong_as_double((long long)(((unsigned long long)(e2 / 2 - 26 + 1074) << 52) + q));
+}
+
+// RN(1/y)
+__device__ __forceinline__ double ircp_rn(double y) {
+  const unsigned long long b = (unsigned long long)__double_as_longlong(y);
+  const int E = (int)(b >> 52);
+  if (E <= 1 || E >= 2045) return ircp_fallback(y);  // keeps 1/y normal
+  const unsigned long long M = (b & 0xfffffffffffffull) | (1ull << 52);
+  const int e = E - 1075;
+  const unsigned __int128 T = (unsigned __int128)1 << 105;
+  const float u = __uint_as_float((127u << 23) | (unsigned)((M >> 29) & 0x7fffffu));  // [1, 2)
+  float y0;
+  asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(y0) : "f"(u));
+  unsigned long long q = f32_fix(y0, 53);  // ~ 2^105 / M
+  const long long Y = (long long)f32_fix(y0, 31);
+#pragma unroll
+  for (int it = 0; it < 2; ++it) {
+    // q += (2^105 - q M) / M, with 1/M ~ y0 2^-52
+    const __int128 D = (__int128)(T - (unsigned __int128)q * M);
+    q = (unsigned long long)((long long)q + (long long)(((D >> 22) * Y) >> 61));
+  }
+  unsigned __int128 qm = (unsigned __int128)q * M;
+  if (qm > T) {
+    --q;
+    qm -= M;
+  } else if (T - qm >= M) {
+    ++q;
+    qm += M;
+  }
+  if (qm > T || T - qm >= M) return ircp_fallback(y);
+  const unsigned __int128 R2 = 2 * (T - qm);
+  if (R2 > M || (R2 == M && (q & 1ull))) ++q;
+  return __longlong_as_double((long long)(((unsigned long long)(-e - 105 + 1074) << 52) + q));
+}
+
 // 2.0 / y, correctly rounded: 2 RN(1/y) with the factor 2 applied to the
 // exponent field, which is exact while RN(1/y) and its double are normal;
 // otherwise the division itself
 __device__ __forceinline__ double two_over(double y) {
-  const double r = __drcp_rn(y);
+  const double r = ircp_rn(y);
   const long long b = __double_as_longlong(r);
   const long long e = (b >> 52) & 0x7FF;
   return (e >= 1 && e <= 0x7FD) ? __longlong_as_double(b + (1LL << 52)) : __ddiv_rn(2.0, y);

@@ -403,7 +403,7 @@ __global__ void __launch_bounds__(256) pair_list_kernel(State s, Geometry g, Con
         const double d2 = fx_sep(s, b.xfix, k.fx_k, 2, p, q);
         ss = __fma_rn(d2, d2, ss);
       }
-      const double r = sqrt(ss);
+      const double r = isqrt_rn(ss);
       const double t = ker_t(k, r);
       const double t2 = t * t;
       const double w = (k.mcw * (t2 * t2)) * __fma_rn(-4.0, t, 5.0);  // m W
@@ -434,7 +434,7 @@ __global__ void __launch_bounds__(256) pair_list_kernel(State s, Geometry g, Con
         double pi = 0.0;
         if (lt0(vdx)) {
           // mu = h v.x / (r^2 + eta^2) with r^2 as r r and the reciprocal
-          pi = ((k.ca * vdx) * __drcp_rn(r * r + k.eta2)) * inv_rb;
+          pi = ((k.ca * vdx) * ircp_rn(r * r + k.eta2)) * inv_rb;
           // one count per direction whose row is summed
           av += (wp ? 1 : 0) + (wq ? 1 : 0);
         }
@@ -473,6 +473,26 @@ void tiles_dim(cudaStream_t st, const State& s, const Geometry& g, const Consts&
   }
 }
 
+// sph_arith_check's kernel: one value per thread
+__global__ void arith_check_kernel(int op, int k, int n, const double* a, const double* b,
+                                   double* out) {
+  const int i = blockIdx.x * 256 + threadIdx.x;
+  if (i >= n) return;
+  const double x = a[i];
+  double r;
+  if (op == 0) {
+    const long long X = fx_fix(x, k), Y = fx_fix(b[i], k);
+    r = (X == kFxNone || Y == kFxNone) ? fx_fallback(x, &b[i]) : fx_diff(X, Y, k);
+  } else if (op == 1) {
+    r = isqrt_rn(x);
+  } else if (op == 2) {
+    r = ircp_rn(x);
+  } else {
+    r = two_over(x);
+  }
+  out[i] = r;
+}
+
 }  // namespace
 
 cudaError_t launch_tiles_fp64(const LaunchCtx& c, const State& s, const Geometry& g,
@@ -484,3 +504,33 @@ cudaError_t launch_tiles_fp64(const LaunchCtx& c, const State& s, const Geometry
 }
 
 }  // namespace sphgpu
+
+extern "C" int sph_arith_check(int device, int op, int k, int n, const double* a, const double* b,
+                               double* out) {
+  if (n < 0 || op < 0 || op > 3) return SPH_ERR_ARG;
+  if (n == 0) return SPH_OK;
+  if (!a || !out || (op == 0 && !b)) return SPH_ERR_ARG;
+  int prev = 0;
+  if (cudaGetDevice(&prev) != cudaSuccess || cudaSetDevice(device) != cudaSuccess) {
+    cudaGetLastError();
+    return SPH_ERR_CUDA;
+  }
+  const size_t bytes = sizeof(double) * (size_t)n;
+  double* d = nullptr;
+  int rc = SPH_OK;
+  if (cudaMalloc(&d, 3 * bytes) != cudaSuccess) {
+    rc = SPH_ERR_NOMEM;
+  } else if (cudaMemcpy(d, a, bytes, cudaMemcpyHostToDevice) != cudaSuccess ||
+             (op == 0 && cudaMemcpy(d + n, b, bytes, cudaMemcpyHostToDevice) != cudaSuccess)) {
+    rc = SPH_ERR_CUDA;
+  } else {
+    sphgpu::arith_check_kernel<<<(n + 255) / 256, 256>>>(op, k, n, d, d + n, d + 2 * (size_t)n);
+    if (cudaGetLastError() != cudaSuccess || cudaDeviceSynchronize() != cudaSuccess ||
+        cudaMemcpy(out, d + 2 * (size_t)n, bytes, cudaMemcpyDeviceToHost) != cudaSuccess)
+      rc = SPH_ERR_CUDA;
+  }
+  if (d) cudaFree(d);
+  cudaGetLastError();
+  cudaSetDevice(prev);
+  return rc;
+}

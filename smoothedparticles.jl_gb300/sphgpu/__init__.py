@@ -24,7 +24,7 @@ __all__ = ["ParticleSystem", "ParticleField", "create_cell_list", "apply", "appl
            "apply_binary", "sum", "SphError", "Operator", "SumFunction", "FLUID", "WALL",
            "FP64", "MIXED", "find_rho", "find_rho0", "internal_force", "find_pressure",
            "reset_rho", "reset_rho0", "reset_a", "accelerate", "move", "hydrostatic",
-           "DENSITY", "KERNEL", "PRESSURE", "SHEPARD", "wall_pressure", "Batch", "pipe_peak",
+           "DENSITY", "KERNEL", "PRESSURE", "SHEPARD", "wall_pressure", "Batch", "pipe_peak", "arith_check",
            "memory_estimate", "shape_count", "assemble_matrix", "assemble_vector", "CsrMatrix",
            "MAT_KERNEL", "MAT_PROJECTION", "VEC_PROJECTION"]
 
@@ -448,6 +448,24 @@ def memory_estimate(params: dict, n: int, precision: int = FP64) -> int:
     if rc != 0:
         raise SphError(rc, "sph_memory_estimate: invalid parameters")
     return b.value
+
+
+def arith_check(op: str, a, b=None, k: int = 59, device: int = 0):
+    """The FP64 arithmetic the pair passes form on the integer pipes, applied
+    on the device: op 'sub' (a - b through fixed-point copies at scale 2^k),
+    'sqrt', 'rcp' (1/a) or 'two_over' (2/a).  For tests against IEEE results."""
+    lib = L.load()
+    code = {"sub": 0, "sqrt": 1, "rcp": 2, "two_over": 3}[op]
+    a = np.ascontiguousarray(a, dtype=np.float64)
+    bb = np.ascontiguousarray(b if b is not None else a, dtype=np.float64)
+    if bb.shape != a.shape:
+        raise ValueError("a and b must have the same shape")
+    out = np.empty_like(a)
+    rc = lib.sph_arith_check(device, code, int(k), int(a.size), a.ctypes.data, bb.ctypes.data,
+                             out.ctypes.data)
+    if rc != 0:
+        raise SphError(rc, "sph_arith_check failed")
+    return out
 
 
 def pipe_peak(which: str, device: int = 0) -> float:

@@ -174,6 +174,8 @@ PROTOTYPES = {
     "sph_launch_count": (C.c_int, [_P, C.POINTER(_I64)]),
     "sph_pair_stats": (C.c_int, [_P, C.POINTER(C.c_uint64), C.c_int]),
     "sph_pipe_peak": (C.c_int, [C.c_int, C.c_int, C.POINTER(C.c_double)]),
+    "sph_arith_check": (C.c_int, [C.c_int, C.c_int, C.c_int, C.c_int, C.c_void_p, C.c_void_p,
+                                  C.c_void_p]),
     "sph_cell_list_noalloc": (C.c_int, [C.POINTER(sph_params), _I64, _P, _P, _P, _P]),
     "sph_set_tuning": (C.c_int, [_P, C.c_int]),
     "sph_get_tuning": (C.c_int, [_P, C.POINTER(C.c_int)]),
