@@ -306,7 +306,7 @@ __global__ void __launch_bounds__(32 * WARPS) pair64_kernel(State s, Geometry g,
 // wrote (sph_tile64.cu): one thread per particle; targets whose rows
 // overflowed are left to pair64_kernel.
 template <int DIM, int OP>
-__global__ void __launch_bounds__(256) row_sum_kernel(State s, Consts k, BinScratch b, int self,
+__global__ void __launch_bounds__(256, 5) row_sum_kernel(State s, Consts k, BinScratch b, int self,
                                                       int reset, int fuse_eos) {
   const int n = *b.d_n;
   const int i = blockIdx.x * 256 + threadIdx.x;

@@ -248,21 +248,34 @@ __device__ __forceinline__ void tile_run(const State& s, const Geometry& g, cons
       sh.rmask[lane] = rm;
       sh.rcur[lane] = rc;
       __syncwarp();
-      // the block's pairs with their ranks in both segments; a pair neither
-      // of whose sides has a row entry is dropped.  A column takes its rows
-      // in ascending order, so its rank in the column's segment counts up
-      // from the cursor (in the diagonal block the bits below the lane are
-      // all of the column's bits below each row taken).
+      // the block's pairs with their ranks in both segments.  A column takes
+      // its rows in ascending order, so its rank in the column's segment
+      // counts up from the cursor (in the diagonal block the bits below the
+      // lane are all of the column's bits below each row taken).  A side
+      // without a row entry (a wall, or a rank beyond hit_cap) is marked
+      // kRankNone; the pair kernels skip a pair with neither.
       unsigned em = diag ? (cm & below) : cm;
-      int qrank = cc;
       const unsigned lbase = (unsigned)(32 * ia) | ((unsigned)(32 * jb + lane) << 16);
       const unsigned mbase = ((unsigned)c << 20) | (qfl ? 0u : kQWall);
-      for (;;) {
-        const bool has = em != 0u;
-        if (__ballot_sync(full, has) == 0u) break;
-        bool keep = false;
-        unsigned meta = 0u, loc = 0u;
-        if (has) {
+      const int cnt = __popc(em);
+      int incl = cnt;
+#pragma unroll
+      for (int o = 1; o < 32; o <<= 1) {
+        const int t = __shfl_up_sync(full, incl, o);
+        if (lane >= o) incl += t;
+      }
+      const int total = __shfl_sync(full, incl, 31);
+      if (ln + total > kTileList) {
+        __syncwarp();
+        tile_emit(b, sh, lane, ln, sa, sb);
+        ln = 0;
+        __syncwarp();
+      }
+      if (total <= kTileList) {
+        // each lane writes its column's pairs into its own slice of the list
+        int slot = ln + incl - cnt;
+        int qrank = cc;
+        while (em) {
           const int i = __ffs(em) - 1;
           em &= em - 1u;
           const bool pfl = (afl >> i) & 1u;
@@ -273,19 +286,42 @@ __device__ __forceinline__ void tile_run(const State& s, const Geometry& g, cons
           }
           const unsigned qr_ = (qfl && qrank < cap) ? (unsigned)qrank : kRankNone;
           ++qrank;
-          keep = (pr_ & qr_) != kRankNone;
-          meta = pr_ | (qr_ << 10) | mbase | (pfl ? 0u : kPWall);
-          loc = lbase + (unsigned)i;
+          sh.list[slot++] = make_uint2(lbase + (unsigned)i,
+                                       pr_ | (qr_ << 10) | mbase | (pfl ? 0u : kPWall));
         }
-        const unsigned kb = __ballot_sync(full, keep);
-        if (ln + __popc(kb) > kTileList) {
-          __syncwarp();
-          tile_emit(b, sh, lane, ln, sa, sb);
-          ln = 0;
-          __syncwarp();
+        ln += total;
+      } else {
+        // more pairs than the buffer holds (dense clusters): whole warps of
+        // pairs at a time, emitted as the buffer fills
+        int qrank = cc;
+        for (;;) {
+          const bool has = em != 0u;
+          if (__ballot_sync(full, has) == 0u) break;
+          unsigned meta = 0u, loc = 0u;
+          if (has) {
+            const int i = __ffs(em) - 1;
+            em &= em - 1u;
+            const bool pfl = (afl >> i) & 1u;
+            unsigned pr_ = kRankNone;
+            if (pfl) {
+              const int v = sh.rcur[i] + __popc(sh.rmask[i] & below);
+              if (v < cap) pr_ = (unsigned)v;
+            }
+            const unsigned qr_ = (qfl && qrank < cap) ? (unsigned)qrank : kRankNone;
+            ++qrank;
+            meta = pr_ | (qr_ << 10) | mbase | (pfl ? 0u : kPWall);
+            loc = lbase + (unsigned)i;
+          }
+          const unsigned hb = __ballot_sync(full, has);
+          if (ln + __popc(hb) > kTileList) {
+            __syncwarp();
+            tile_emit(b, sh, lane, ln, sa, sb);
+            ln = 0;
+            __syncwarp();
+          }
+          if (has) sh.list[ln + __popc(hb & below)] = make_uint2(loc, meta);
+          ln += __popc(hb);
         }
-        if (keep) sh.list[ln + __popc(kb & below)] = make_uint2(loc, meta);
-        ln += __popc(kb);
       }
       if (!diag && lane < mb) b.rcur[cj] = cc + __popc(cm);
       __syncwarp();

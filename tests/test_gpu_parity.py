@@ -206,6 +206,36 @@ def test_row_overflow_bitexact(gpu, oracle_mod):
     g.synchronize()
 
 
+def test_pair_list_overflow_bitexact(gpu, oracle_mod):
+    """1,000 fluid and 500 wall particles inside one cell, all within H of one
+    another: every fluid row (1,499 neighbours) overflows its 384 entries and
+    the step's pair list (~5e5 pairs listed) overflows its capacity (192 per
+    particle), so every target takes the traversal."""
+    rng = np.random.default_rng(3)
+    nf, nw = 1000, 500
+    n = nf + nw
+    H = 0.1
+    x = 0.52 + rng.uniform(0.0, 0.05, (n, 3))
+    typ = np.concatenate([np.full(nf, G.FLUID, np.int32), np.full(nw, G.WALL, np.int32)])
+    v = np.zeros((n, 3))
+    v[:nf] = rng.normal(0.0, 0.01, (nf, 3))
+    rho0, c0 = 1000.0, 20.0
+    params = dict(dim=3, h=H, domain_min=[0.0, 0.0, 0.0], domain_max=[1.0, 1.0, 1.0],
+                  mass=rho0 * 0.05 ** 3 / n, rho0=rho0, c0=c0, h_smooth=0.5 * H, alpha=0.05,
+                  eps_xsph=0.5, gravity=[0.0, 0.0, -9.81], dt=(0.05 * H) / c0,
+                  col_height=0.6, vertical_axis=2)
+    c = G.Case("cluster", 3, H / 4.0, x, typ, v, params)
+    g, o = make(c, oracle_mod)
+    g.init_state()
+    assert g.pair_count(reset=True) == o.init_state()
+    assert_same_state(g, o)
+    for _ in range(2):
+        g.step(1)
+        assert g.pair_count(reset=True) == o.step(1)
+    assert_same_state(g, o)
+    g.synchronize()
+
+
 def _narrow_case(dim, n, seed):
     """Random fluid and wall particles in a domain one cell wide along x
     (and two along y in 3D): key + key_diff wraps between rows of cells and
