@@ -406,7 +406,7 @@ __global__ void __launch_bounds__(256) row_scan_kernel(State s, Geometry g, Cons
 // when its target is fluid and has a row (walls and overflowed targets have
 // none); every entry is written whole.
 template <int DIM, int PH>
-__global__ void __launch_bounds__(256) pair_list_kernel(State s, Geometry g, Consts k,
+__global__ void __launch_bounds__(256, PH == 0 ? 8 : 5) pair_list_kernel(State s, Geometry g, Consts k,
                                                         BinScratch b, int threads_total) {
   if (*b.d_pover) return;  // every target traverses
   const long long np = (long long)*b.d_npairs;
