@@ -76,27 +76,6 @@ struct TileShared {
   uint2 list[kTileList];  // pairs: (p_local | q_local << 16, pair_m)
 };
 
-// Two FP32 lanes per 64-bit register (Blackwell's packed FP32 arithmetic).
-__device__ __forceinline__ unsigned long long f2_pack(float lo, float hi) {
-  return (unsigned long long)__float_as_uint(lo) | ((unsigned long long)__float_as_uint(hi) << 32);
-}
-__device__ __forceinline__ unsigned long long f2_sub(unsigned long long a, unsigned long long b) {
-  unsigned long long r;
-  asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(a), "l"(b));
-  return r;
-}
-__device__ __forceinline__ unsigned long long f2_mul(unsigned long long a, unsigned long long b) {
-  unsigned long long r;
-  asm("mul.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(a), "l"(b));
-  return r;
-}
-__device__ __forceinline__ unsigned long long f2_fma(unsigned long long a, unsigned long long b,
-                                                     unsigned long long c) {
-  unsigned long long r;
-  asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(r) : "l"(a), "l"(b), "l"(c));
-  return r;
-}
-
 // 32 x 32 bit transpose across the warp: lane u holds column u's mask (bit i
 // = row i) on entry and row u's mask (bit i = column i) on return.  Each
 // stage swaps the off-diagonal blocks of width j.
