@@ -23,12 +23,13 @@
 // (q in b, slot mirror(c)), where mirror(c) = n_diff - 1 - c is the slot from
 // b back to a; every segment has exactly one writer, so nothing is atomic
 // but the pair list's tail.  A tile classifies a x b in blocks of 32 x 32:
-// lane u tests column q_u against the 32 staged rows (bit i of its column
-// mask); the row masks are the transposes (ballots).  The rank of q in p's
-// segment is the number of p's hits in the earlier column blocks (a cursor)
-// plus the bits of p's row mask below q, and likewise for p in q's segment.
-// The tile of the cell itself (c = centre) takes each unordered pair once
-// (p < q); its diagonal blocks are symmetric.
+// lane u tests column q_u against the 32 staged rows with packed FP32x2
+// arithmetic (bit i of its column mask); the row masks are the transposes (a
+// butterfly bit transpose).  The rank of q in p's segment is the number of
+// p's hits in the earlier column blocks (a cursor) plus the bits of p's row
+// mask below q, and likewise for p in q's segment.  The tile of the cell
+// itself (c = centre) takes each unordered pair once (p < q); its diagonal
+// blocks are symmetric.
 //
 // Passes of a step (launch order):
 //   tiles    classify once: rcur := hits per (target, slot); the pair list
@@ -45,8 +46,11 @@
 // scan; its sum passes traverse instead.  A pair list longer than pair_cap
 // sends every target to the traversal.
 //
-// Built with --fmad=false like sph_pair64.cu: the expressions below round
-// where they are written, in the oracle's order.
+// The pair kernels form position differences, the kernel distance's square
+// root and the force's reciprocals on the integer pipes, correctly rounded
+// (sph_common.cuh: fx_diff, isqrt_rn, ircp_rn).  Built with --fmad=false like
+// sph_pair64.cu: the FP64 expressions below round where they are written, in
+// the oracle's order.
 #include <algorithm>
 
 #include "sph_cellwarp.cuh"
