@@ -47,7 +47,9 @@ UNIT = "pair-interactions/s"
 #                        + a += (6) + W + m* + *inv + XSPH (9)         = 56
 #   force wall hit     = distance + rDW + m* + P-sum + coefficient + a += (6) = 24
 #   viscosity active   = +5 (h*v.d, r^2+eta^2, division, -a c0 *, * 1/rho)
-FLOPS = dict(density=20, wall=29, force_fluid=56, force_wall=24, force_av=5)
+# 2D drops the z terms: distance 6, g.d 3, dv 2, v.d 3, a += 4, XSPH 6.
+FLOPS_BY_DIM = {3: dict(density=20, wall=29, force_fluid=56, force_wall=24, force_av=5),
+                2: dict(density=17, wall=24, force_fluid=45, force_wall=19, force_av=5)}
 
 
 def parse():
@@ -245,10 +247,11 @@ def timed_steps(g, torch, dev, steps, world):
     return out
 
 
-def kernel_table(kst, cats, steps):
+def kernel_table(kst, cats, steps, dim):
     """Per kernel family: total and per-launch time, per-step time and, for the
     pair passes, algorithmic flops per step (the FP64 density and force passes
     of a step are several kernels each: tiles, pair evaluation, row sums)."""
+    FLOPS = FLOPS_BY_DIM[dim]
     flops = {
         "force": cats["force_fluid"] * FLOPS["force_fluid"] + cats["force_wall"] * FLOPS["force_wall"]
         + cats["force_av"] * FLOPS["force_av"],
@@ -521,7 +524,7 @@ def run_ours(args):
                  {"steps": target, "fields": field_errors(long64, longmx),
                   "note": "both runs from their own initial state (init_state of the same lattice)"}
                  if long64 is not None else None),
-             "kernels": kernel_table(rmx["kernels"], rmx["cats"], args.steps),
+             "kernels": kernel_table(rmx["kernels"], rmx["cats"], args.steps, case.dim),
              "binning_hbm": None,
              "gpu_launches": rmx["launches"], "clocks": rmx["clocks"]}
     # one step from an identical FP64 state (reference density included): the
@@ -542,7 +545,7 @@ def run_ours(args):
     mixed["error_vs_fp64_one_step"] = field_errors(one_64, one_mx)
 
     # ---- roofline of the dominant kernel of the FP64 step (the force pass)
-    kt = kernel_table(r64["kernels"], r64["cats"], args.steps)
+    kt = kernel_table(r64["kernels"], r64["cats"], args.steps, case.dim)
     mixed["binning_hbm"] = binning_roofline(mixed["kernels"], case, True)
     dom = max((k for k in kt if "tflops" in kt[k]), key=lambda k: kt[k]["ms_total"])
     dfma = sphgpu.pipe_peak("dfma", dev)
