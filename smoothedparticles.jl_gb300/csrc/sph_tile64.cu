@@ -322,7 +322,7 @@ __device__ __forceinline__ void tile_run(const State& s, const Geometry& g, cons
 // Warps stride over the tile slots (work item, forward slot); a tile is
 // taken by its cell's first item.
 template <int DIM>
-__global__ void __launch_bounds__(32 * kTileWarps) tile_kernel(State s, Geometry g, Consts k,
+__global__ void __launch_bounds__(32 * kTileWarps, 10) tile_kernel(State s, Geometry g, Consts k,
                                                                BinScratch b, int warps_total) {
   __shared__ TileShared shared[kTileWarps];
   TileShared& sh = shared[threadIdx.x >> 5];
