@@ -125,13 +125,37 @@ struct Proc64 {
     }
   }
 
-  // Sums target i's row (sph_tile64.cu wrote each entry's m W, or its
-  // pressure and XSPH factors, once per pair): the same terms, accumulated
-  // in the same order, as process() over the traversal's list.
+  // Sums target i's row (sph_tile64.cu wrote each entry's m W and distance,
+  // or its pressure and XSPH factors, once per pair): the same terms,
+  // accumulated in the same order, as process() over the traversal's list.
   __device__ __forceinline__ void rows(const BinScratch& b, int i, int cnt) {
     const RowEntry* row = b.rows + (size_t)i * b.hit_cap;
     if (OP == SPH_OP_DENSITY) {
       for (int j = 0; j < cnt; ++j) acc = acc + __ldg(&row[j].a);
+      c0 += cnt;
+    } else if (OP == SPH_OP_WALL_PRESSURE) {
+      // a wall's row: its fluid neighbours with their kernel distances
+      const int n = *b.d_n;
+      const long long X0 = b.xfix[0][i], X1 = b.xfix[1][i];
+      const long long X2 = DIM == 3 ? b.xfix[2][i] : 0;
+      for (int j = 0; j < cnt; ++j) {
+        const RowEntry en = row_load(row + j);
+        const int q = (int)(en.q & 0x7fffffffu);
+        if (q >= n) {  // an entry the tile passes did not write: report, skip
+          atomicOr(b.d_err, kErrBounds);
+          continue;
+        }
+        const double t = ker_t(k, en.b);
+        const double t2 = t * t;
+        const double w = (k.cw * (t2 * t2)) * __fma_rn(-4.0, t, 5.0);
+        const double d0 = fx_sep1(X0, &s.x[0][i], s, b.xfix, k.fx_k, 0, q);
+        const double d1 = fx_sep1(X1, &s.x[1][i], s, b.xfix, k.fx_k, 1, q);
+        double gd = __fma_rn(k.g[1], d1, k.g[0] * d0);
+        if (DIM == 3) gd = __fma_rn(k.g[2], fx_sep1(X2, &s.x[2][i], s, b.xfix, k.fx_k, 2, q), gd);
+        wp = __fma_rn(__ldg(&s.P[q]), w, wp);
+        wg = __fma_rn(__ldg(&s.rho[q]) * gd, w, wg);
+        ws = ws + w;
+      }
       c0 += cnt;
     } else if (OP == SPH_OP_FORCE) {
       const int n = *b.d_n;
@@ -302,17 +326,19 @@ __global__ void __launch_bounds__(32 * WARPS) pair64_kernel(State s, Geometry g,
   }
 }
 
-// The density and force passes of a step over the rows the tile passes
-// wrote (sph_tile64.cu): one thread per particle; targets whose rows
-// overflowed are left to pair64_kernel.
+// The density, wall-pressure and force passes of a step over the rows the
+// tile passes wrote (sph_tile64.cu): one thread per particle; targets whose
+// rows overflowed are left to pair64_kernel.
 template <int DIM, int OP>
 __global__ void __launch_bounds__(256, 5) row_sum_kernel(State s, Consts k, BinScratch b, int self,
                                                       int reset, int fuse_eos) {
   const int n = *b.d_n;
   const int i = blockIdx.x * 256 + threadIdx.x;
+  // the wall pressure acts on wall targets, every other operator on fluid ones
+  const int want = OP == SPH_OP_WALL_PRESSURE ? kWall : kFluid;
   Proc64<DIM, OP> p(s, k);
   if (i < n) {
-    if (s.type[i] != kFluid) {
+    if (s.type[i] != want) {
       skipped_target<DIM, OP>(s, i, reset);
     } else {
       const int cnt = __ldg(&b.hit_count[i]);
@@ -461,13 +487,19 @@ cudaError_t launch_pair_dim(const LaunchCtx& c, const State& s, const Geometry& 
   // the rows (sph_tile64.cu), the rows summed, then the traversal of the
   // targets whose rows overflowed (its warps return at once otherwise)
   if (list_mode == 3) {
-    const cudaError_t e = launch_tiles_fp64(c, s, g, k, b, cap, op == SPH_OP_FORCE ? 1 : 0);
-    if (e != cudaSuccess) return e;
     const int rb = (cap + 255) / 256;
-    if (op == SPH_OP_FORCE)
-      row_sum_kernel<DIM, SPH_OP_FORCE><<<rb, 256, 0, c.stream>>>(s, k, b, self, reset, 0);
-    else
-      row_sum_kernel<DIM, SPH_OP_DENSITY><<<rb, 256, 0, c.stream>>>(s, k, b, self, reset, fuse_eos);
+    if (op == SPH_OP_WALL_PRESSURE) {
+      // the density pass's rows hold every wall's fluid neighbours
+      row_sum_kernel<DIM, SPH_OP_WALL_PRESSURE><<<rb, 256, 0, c.stream>>>(s, k, b, 0, 0, 0);
+    } else {
+      const cudaError_t e = launch_tiles_fp64(c, s, g, k, b, cap, op == SPH_OP_FORCE ? 1 : 0);
+      if (e != cudaSuccess) return e;
+      if (op == SPH_OP_FORCE)
+        row_sum_kernel<DIM, SPH_OP_FORCE><<<rb, 256, 0, c.stream>>>(s, k, b, self, reset, 0);
+      else
+        row_sum_kernel<DIM, SPH_OP_DENSITY><<<rb, 256, 0, c.stream>>>(s, k, b, self, reset,
+                                                                      fuse_eos);
+    }
   }
   switch (op) {
     case SPH_OP_DENSITY:
@@ -481,9 +513,9 @@ cudaError_t launch_pair_dim(const LaunchCtx& c, const State& s, const Geometry& 
       else pair64_launch<DIM, SPH_OP_DENSITY_REF, 4>(c.stream, b, 128, s, g, k, b, self, reset, 0, 0);
       break;
     case SPH_OP_WALL_PRESSURE:
-      if (W == 2) pair64_launch<DIM, SPH_OP_WALL_PRESSURE, 2>(c.stream, b, 64, s, g, k, b, 0, 0, 0, 0);
-      else if (W == 8) pair64_launch<DIM, SPH_OP_WALL_PRESSURE, 8>(c.stream, b, 256, s, g, k, b, 0, 0, 0, 0);
-      else pair64_launch<DIM, SPH_OP_WALL_PRESSURE, 4>(c.stream, b, 128, s, g, k, b, 0, 0, 0, 0);
+      if (W == 2) pair64_launch<DIM, SPH_OP_WALL_PRESSURE, 2>(c.stream, b, 64, s, g, k, b, 0, 0, 0, list_mode);
+      else if (W == 8) pair64_launch<DIM, SPH_OP_WALL_PRESSURE, 8>(c.stream, b, 256, s, g, k, b, 0, 0, 0, list_mode);
+      else pair64_launch<DIM, SPH_OP_WALL_PRESSURE, 4>(c.stream, b, 128, s, g, k, b, 0, 0, 0, list_mode);
       break;
     default:
       if (W == 2) pair64_launch<DIM, SPH_OP_FORCE, 2>(c.stream, b, 64, s, g, k, b, self, reset, 0, list_mode);
@@ -491,7 +523,10 @@ cudaError_t launch_pair_dim(const LaunchCtx& c, const State& s, const Geometry& 
       else pair64_launch<DIM, SPH_OP_FORCE, 4>(c.stream, b, 128, s, g, k, b, self, reset, 0, list_mode);
       break;
   }
-  mark(c, kid, 1, list_mode == 3 ? kRowPassLaunches[op == SPH_OP_FORCE ? 1 : 0] : 1);
+  mark(c, kid, 1,
+       list_mode != 3                 ? 1
+       : op == SPH_OP_WALL_PRESSURE ? 2
+                                    : kRowPassLaunches[op == SPH_OP_FORCE ? 1 : 0]);
   return cudaGetLastError();
 }
 
@@ -501,9 +536,13 @@ cudaError_t launch_pair_fp64(const LaunchCtx& c, const State& s, const Geometry&
                              const Consts& k, const BinScratch& b, int cap, int op, int self,
                              int reset, int fuse_eos, int lists_valid) {
   if (cap <= 0) return cudaSuccess;
-  // rows: the density pass always builds them; the force pass sums them when
-  // the density pass of this binning built them, else it traverses
-  const int lm = op == SPH_OP_DENSITY || (op == SPH_OP_FORCE && lists_valid) ? 3 : 0;
+  // rows: the density pass always builds them; the wall-pressure and force
+  // passes sum them when the density pass of this binning built them, else
+  // they traverse
+  const int lm =
+      op == SPH_OP_DENSITY || ((op == SPH_OP_FORCE || op == SPH_OP_WALL_PRESSURE) && lists_valid)
+          ? 3
+          : 0;
   return k.dim == 2 ? launch_pair_dim<2>(c, s, g, k, b, cap, op, self, reset, fuse_eos, lm)
                     : launch_pair_dim<3>(c, s, g, k, b, cap, op, self, reset, fuse_eos, lm);
 }

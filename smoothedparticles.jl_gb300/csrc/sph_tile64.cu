@@ -37,6 +37,8 @@
 //   scan     roff := exclusive prefix over the target's slots; hit_count
 //   density  per pair: r and m W into both rows (at roff + rank)
 //   [sum]    sph_pair64.cu: rho = the row's sum, self term, EOS
+//   [wall]   sph_pair64.cu: each wall's pressure over its row (fluid
+//            neighbours, the kernel value from the stored distance)
 //   force    per pair: cf and wx into both rows (a fluid-wall pair only into
 //            the fluid target's row: walls are not force targets)
 //   [sum]    sph_pair64.cu: a += cf d, xs += -wx dv over the row
@@ -66,7 +68,8 @@ constexpr int kTileList = 512;         // pairs buffered per warp before they ar
 constexpr float kTileFar = 1.0e18f;    // coordinate of an empty staging slot
 // pair_m: rank in p's segment (10 bits), rank in q's segment (10), slot (5),
 // p is a wall, q is a wall.  A rank of kRankNone (>= every hit_cap) marks a
-// side without a row entry.
+// side beyond its row.  Wall rows hold their fluid neighbours (pairs of two
+// walls are not listed) for the wall pressure.
 constexpr unsigned kRankNone = 1023u;
 constexpr unsigned kPWall = 1u << 25, kQWall = 1u << 26;
 constexpr int kNoRow = 1 << 24;  // segment offset of a target without a row
@@ -262,12 +265,9 @@ __device__ __forceinline__ void tile_run(const State& s, const Geometry& g, cons
           const int i = __ffs(em) - 1;
           em &= em - 1u;
           const bool pfl = (afl >> i) & 1u;
-          unsigned pr_ = kRankNone;
-          if (pfl) {
-            const int v = sh.rcur[i] + __popc(sh.rmask[i] & below);
-            if (v < cap) pr_ = (unsigned)v;
-          }
-          const unsigned qr_ = (qfl && qrank < cap) ? (unsigned)qrank : kRankNone;
+          const int v = sh.rcur[i] + __popc(sh.rmask[i] & below);
+          const unsigned pr_ = v < cap ? (unsigned)v : kRankNone;
+          const unsigned qr_ = qrank < cap ? (unsigned)qrank : kRankNone;
           ++qrank;
           sh.list[slot++] = make_uint2(lbase + (unsigned)i,
                                        pr_ | (qr_ << 10) | mbase | (pfl ? 0u : kPWall));
@@ -285,12 +285,9 @@ __device__ __forceinline__ void tile_run(const State& s, const Geometry& g, cons
             const int i = __ffs(em) - 1;
             em &= em - 1u;
             const bool pfl = (afl >> i) & 1u;
-            unsigned pr_ = kRankNone;
-            if (pfl) {
-              const int v = sh.rcur[i] + __popc(sh.rmask[i] & below);
-              if (v < cap) pr_ = (unsigned)v;
-            }
-            const unsigned qr_ = (qfl && qrank < cap) ? (unsigned)qrank : kRankNone;
+            const int v = sh.rcur[i] + __popc(sh.rmask[i] & below);
+            const unsigned pr_ = v < cap ? (unsigned)v : kRankNone;
+            const unsigned qr_ = qrank < cap ? (unsigned)qrank : kRankNone;
             ++qrank;
             meta = pr_ | (qr_ << 10) | mbase | (pfl ? 0u : kPWall);
             loc = lbase + (unsigned)i;
@@ -349,18 +346,19 @@ __global__ void __launch_bounds__(32 * kTileWarps, 10) tile_kernel(State s, Geom
   }
 }
 
-// Row offsets of every fluid target from its per-slot counts; the
-// positions' fixed-point copies of every particle for the pair kernels.
+// Row offsets of every particle from its per-slot counts (a wall's row
+// holds its fluid neighbours); the positions' fixed-point copies for the
+// pair kernels.
 __global__ void __launch_bounds__(256) row_scan_kernel(State s, Geometry g, Consts k,
                                                        BinScratch b) {
   const int n = *b.d_n;
   const int i = blockIdx.x * 256 + threadIdx.x;
   if (i >= n) return;
   for (int d = 0; d < k.dim; ++d) b.xfix[d][i] = fx_fix(s.x[d][i], k.fx_k);
-  if (s.type[i] != kFluid) return;
   const int key = s.cell[i];
   const int nd = g.n_diff;
   bool over = __ldg(&b.cell_start[key + 1]) - __ldg(&b.cell_start[key]) > 0xffff;
+  const bool own_fluid = __ldg(&b.cell_fluid[key]) != 0;
   int run = 0;
   for (int c = 0; c < nd; ++c) {
     const int nk = key + g.key_diff[c];
@@ -368,7 +366,10 @@ __global__ void __launch_bounds__(256) row_scan_kernel(State s, Geometry g, Cons
     if (nk >= 1 && nk <= g.key_max) {
       const int m = __ldg(&b.cell_start[nk + 1]) - __ldg(&b.cell_start[nk]);
       if (m > 0xffff) over = true;
-      else if (m > 0) cnt = b.rcur[(size_t)i * nd + c];
+      // a tile between two cells without fluid is skipped (no pair of it
+      // involves a fluid particle), so its counts are not written
+      else if (m > 0 && (own_fluid || __ldg(&b.cell_fluid[nk]) != 0))
+        cnt = b.rcur[(size_t)i * nd + c];
     }
     b.roff[(size_t)i * nd + c] = run;
     run += cnt;
@@ -403,10 +404,13 @@ __global__ void __launch_bounds__(256, PH == 0 ? 8 : 5) pair_list_kernel(State s
     const int c = (int)((m >> 20) & 31u);
     const bool fp = (m & kPWall) == 0u, fq = (m & kQWall) == 0u;
     // entry positions (a rank of kRankNone, or a target without a row, lands
-    // beyond hit_cap)
-    const int vp = fp ? __ldg(&b.roff[(size_t)p * nd + c]) + (int)(m & 1023u) : b.hit_cap;
-    const int vq = fq ? __ldg(&b.roff[(size_t)q * nd + (nd - 1 - c)]) + (int)((m >> 10) & 1023u)
-                      : b.hit_cap;
+    // beyond hit_cap); the density pass fills wall rows too (the wall
+    // pressure's neighbours), the force pass fluid rows only
+    const int vp = (PH == 0 || fp) ? __ldg(&b.roff[(size_t)p * nd + c]) + (int)(m & 1023u)
+                                   : b.hit_cap;
+    const int vq = (PH == 0 || fq)
+                       ? __ldg(&b.roff[(size_t)q * nd + (nd - 1 - c)]) + (int)((m >> 10) & 1023u)
+                       : b.hit_cap;
     const bool wp = vp < b.hit_cap, wq = vq < b.hit_cap;
     if (!wp && !wq) continue;
     RowEntry* const ep = b.rows + (size_t)p * cap + vp;
