@@ -247,16 +247,14 @@ int pair_pass(sph_system* s, int op, int self, int reset, int fuse_eos) {
   // walls' records
   if (op == SPH_OP_DENSITY) s->aux_fluid = fuse_eos != 0;
   if (op == SPH_OP_WALL_PRESSURE) s->aux_wall = true;
-  // the density passes keep the hit masks (mixed) or the rows (FP64, the
-  // density pass only) for the force pass; an FP64 force pass turns the
-  // rows' m W into its own factors, and a traversing pass uses its targets'
-  // rows as scratch
-  if (s->params.precision == SPH_PREC_MIXED) {
-    if (op == SPH_OP_DENSITY || op == SPH_OP_DENSITY_REF) s->lists_valid = true;
-  } else {
-    if (op == SPH_OP_DENSITY) s->lists_valid = true;
-    else if (op == SPH_OP_DENSITY_REF || op == SPH_OP_FORCE) s->lists_valid = false;
-  }
+  // the density passes keep the hit masks (mixed) or the rows (FP64) for the
+  // force pass of the same binning; an FP64 force pass turns the rows' m W
+  // into its own factors (a traversing pass only writes the rows of targets
+  // that have none: passes without valid rows, overflowed rows)
+  if (op == SPH_OP_DENSITY || op == SPH_OP_DENSITY_REF)
+    s->lists_valid = true;
+  else if (op == SPH_OP_FORCE && s->params.precision != SPH_PREC_MIXED)
+    s->lists_valid = false;
   return SPH_OK;
 }
 

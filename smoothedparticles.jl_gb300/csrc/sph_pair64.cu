@@ -130,7 +130,7 @@ struct Proc64 {
   // accumulated in the same order, as process() over the traversal's list.
   __device__ __forceinline__ void rows(const BinScratch& b, int i, int cnt) {
     const RowEntry* row = b.rows + (size_t)i * b.hit_cap;
-    if (OP == SPH_OP_DENSITY) {
+    if (OP == SPH_OP_DENSITY || OP == SPH_OP_DENSITY_REF) {
       for (int j = 0; j < cnt; ++j) acc = acc + __ldg(&row[j].a);
       c0 += cnt;
     } else if (OP == SPH_OP_WALL_PRESSURE) {
@@ -496,6 +496,8 @@ cudaError_t launch_pair_dim(const LaunchCtx& c, const State& s, const Geometry& 
       if (e != cudaSuccess) return e;
       if (op == SPH_OP_FORCE)
         row_sum_kernel<DIM, SPH_OP_FORCE><<<rb, 256, 0, c.stream>>>(s, k, b, self, reset, 0);
+      else if (op == SPH_OP_DENSITY_REF)
+        row_sum_kernel<DIM, SPH_OP_DENSITY_REF><<<rb, 256, 0, c.stream>>>(s, k, b, self, reset, 0);
       else
         row_sum_kernel<DIM, SPH_OP_DENSITY><<<rb, 256, 0, c.stream>>>(s, k, b, self, reset,
                                                                       fuse_eos);
@@ -508,9 +510,9 @@ cudaError_t launch_pair_dim(const LaunchCtx& c, const State& s, const Geometry& 
       else pair64_launch<DIM, SPH_OP_DENSITY, 4>(c.stream, b, 128, s, g, k, b, self, reset, fuse_eos, list_mode);
       break;
     case SPH_OP_DENSITY_REF:
-      if (W == 2) pair64_launch<DIM, SPH_OP_DENSITY_REF, 2>(c.stream, b, 64, s, g, k, b, self, reset, 0, 0);
-      else if (W == 8) pair64_launch<DIM, SPH_OP_DENSITY_REF, 8>(c.stream, b, 256, s, g, k, b, self, reset, 0, 0);
-      else pair64_launch<DIM, SPH_OP_DENSITY_REF, 4>(c.stream, b, 128, s, g, k, b, self, reset, 0, 0);
+      if (W == 2) pair64_launch<DIM, SPH_OP_DENSITY_REF, 2>(c.stream, b, 64, s, g, k, b, self, reset, 0, list_mode);
+      else if (W == 8) pair64_launch<DIM, SPH_OP_DENSITY_REF, 8>(c.stream, b, 256, s, g, k, b, self, reset, 0, list_mode);
+      else pair64_launch<DIM, SPH_OP_DENSITY_REF, 4>(c.stream, b, 128, s, g, k, b, self, reset, 0, list_mode);
       break;
     case SPH_OP_WALL_PRESSURE:
       if (W == 2) pair64_launch<DIM, SPH_OP_WALL_PRESSURE, 2>(c.stream, b, 64, s, g, k, b, 0, 0, 0, list_mode);
@@ -536,13 +538,13 @@ cudaError_t launch_pair_fp64(const LaunchCtx& c, const State& s, const Geometry&
                              const Consts& k, const BinScratch& b, int cap, int op, int self,
                              int reset, int fuse_eos, int lists_valid) {
   if (cap <= 0) return cudaSuccess;
-  // rows: the density pass always builds them; the wall-pressure and force
-  // passes sum them when the density pass of this binning built them, else
-  // they traverse
-  const int lm =
-      op == SPH_OP_DENSITY || ((op == SPH_OP_FORCE || op == SPH_OP_WALL_PRESSURE) && lists_valid)
-          ? 3
-          : 0;
+  // rows: the density passes (rho and the reference density) always build
+  // them; the wall-pressure and force passes sum them when a density pass of
+  // this binning built them, else they traverse
+  const int lm = op == SPH_OP_DENSITY || op == SPH_OP_DENSITY_REF ||
+                         ((op == SPH_OP_FORCE || op == SPH_OP_WALL_PRESSURE) && lists_valid)
+                     ? 3
+                     : 0;
   return k.dim == 2 ? launch_pair_dim<2>(c, s, g, k, b, cap, op, self, reset, fuse_eos, lm)
                     : launch_pair_dim<3>(c, s, g, k, b, cap, op, self, reset, fuse_eos, lm);
 }
