@@ -81,17 +81,19 @@ struct Consts {
 };
 
 // One entry of an FP64 target's row (32 bytes, one DRAM sector, written
-// whole): the neighbour index (bit 31 set for walls) and two values -- after
-// the density pass m W and the kernel distance, after the force pass the
-// pressure factor and the XSPH factor.
+// whole): the neighbour index (bit 31 set for walls) and three values --
+// after the density pass m W, the kernel distance and m rDW (the force
+// pass's kernel derivative, formed from the same distance), after the force
+// pass the pressure factor and the XSPH factor.
 struct __align__(32) RowEntry {
   unsigned long long q;
   double a, b, c;
 };
 
-__device__ __forceinline__ void row_store(RowEntry* e, unsigned long long q, double a, double b) {
+__device__ __forceinline__ void row_store(RowEntry* e, unsigned long long q, double a, double b,
+                                          double c = 0.0) {
   asm volatile("st.global.v4.b64 [%0], {%1, %2, %3, %4};" ::"l"(e), "l"(q), "d"(a), "d"(b),
-               "d"(0.0)
+               "d"(c)
                : "memory");
 }
 
