@@ -81,10 +81,10 @@ struct Consts {
 };
 
 // One entry of an FP64 target's row (32 bytes, one DRAM sector, written
-// whole): the neighbour index (bit 31 set for walls) and three values --
-// after the density pass m W, the kernel distance and m rDW (the force
-// pass's kernel derivative, formed from the same distance), after the force
-// pass the pressure factor and the XSPH factor.
+// whole): the neighbour index (bit 31 set for walls) and up to three values
+// -- after the density pass m W, the kernel distance r and t = 1 - r/H (the
+// force pass's kernel derivative starts from it), after the force pass the
+// pressure factor and the XSPH factor.
 struct __align__(32) RowEntry {
   unsigned long long q;
   double a, b, c;

@@ -134,7 +134,7 @@ struct Proc64 {
       for (int j = 0; j < cnt; ++j) acc = acc + __ldg(&row[j].a);
       c0 += cnt;
     } else if (OP == SPH_OP_WALL_PRESSURE) {
-      // a wall's row: its fluid neighbours with their kernel distances
+      // a wall's row: its fluid neighbours with their distances and t = 1 - r/H
       const int n = *b.d_n;
       const long long X0 = b.xfix[0][i], X1 = b.xfix[1][i];
       const long long X2 = DIM == 3 ? b.xfix[2][i] : 0;
@@ -145,7 +145,7 @@ struct Proc64 {
           atomicOr(b.d_err, kErrBounds);
           continue;
         }
-        const double t = ker_t(k, en.b);
+        const double t = en.c;  // ker_t of the stored distance
         const double t2 = t * t;
         const double w = (k.cw * (t2 * t2)) * __fma_rn(-4.0, t, 5.0);
         const double d0 = fx_sep1(X0, &s.x[0][i], s, b.xfix, k.fx_k, 0, q);

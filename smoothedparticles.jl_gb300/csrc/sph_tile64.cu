@@ -430,15 +430,16 @@ __global__ void __launch_bounds__(256, PH == 0 ? 8 : 5) pair_list_kernel(State s
       const double t = ker_t(k, r);
       const double t2 = t * t;
       const double w = (k.mcw * (t2 * t2)) * __fma_rn(-4.0, t, 5.0);  // m W
-      // m rDW for the force pass of this binning: the same expression of the
-      // same t as the traversal's, formed here where t is at hand
-      const double ker = k.mcr * (t2 * t);
-      if (wp) row_store(ep, qbits, w, r, ker);
-      if (wq) row_store(eq, pbits, w, r, ker);
+      // t = 1 - r/H rides in the entry's spare slot, so that the force pass
+      // of this binning starts its kernel derivative from it
+      if (wp) row_store(ep, qbits, w, r, t);
+      if (wq) row_store(eq, pbits, w, r, t);
     } else {
-      // m W, r and m rDW as the density pass of this binning stored them
+      // m W, r and t as the density pass of this binning stored them
       const RowEntry en = row_load(wp ? ep : eq);
-      const double w = en.a, r = en.b, ker = en.c;
+      const double w = en.a, r = en.b, t = en.c;
+      const double t2 = t * t;
+      const double ker = k.mcr * (t2 * t);  // m rDW
       const double sp = __ldg(&s.Pr[p]) + __ldg(&s.Pr[q]);
       if (fp && fq) {
         // pressure (collapse_symplectic.jl:114-118) + Monaghan viscosity +
