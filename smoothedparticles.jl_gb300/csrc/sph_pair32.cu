@@ -48,6 +48,12 @@ struct MxShared {
   // force and wall pressure stage the 32-byte neighbour record
   float4 c0[32];               // (x, y, z) cell-relative, .w = type / signed rho
   float4 c1[kRec ? 32 : 1];    // (vx, vy, vz, P/rho^2)
+  // the staged coordinates once more, one array per axis: step A reads two
+  // candidates' coordinates as one 64-bit word for the packed FP32x2 tests
+  alignas(16) float px[32];
+  alignas(16) float py[32];
+  alignas(16) float pz[32];
+  unsigned fluid;              // wall pressure: bit u = candidate u is fluid
   float4 offs[27];             // offset of each neighbour cell from the target cell
   int cb[kTab];                // first candidate of each chunk of the item
   unsigned char cc[kTab];      // neighbour-cell number of each chunk
@@ -199,48 +205,74 @@ struct Acc32 {
 };
 
 // Stages candidates [base, base + m) of one neighbour cell; empty slots get a
-// far-away position and the type of no operator's neighbour.
-template <int OP>
+// far-away position and the type of no operator's neighbour.  CLASSIFY: the
+// chunk goes through step A, which also wants the per-axis copies.
+template <int OP, bool CLASSIFY>
 __device__ __forceinline__ void mx_stage(const State& s, MxShared<OP>& sh, int lane, int base,
                                          int m) {
   __syncwarp();
+  float4 c;
   if (MxShared<OP>::kRec) {
     if (lane < m) {
-      ld_rec(s.rec + 2 * (base + lane), sh.c0[lane], sh.c1[lane]);
+      float4 v;
+      ld_rec(s.rec + 2 * (base + lane), c, v);
+      sh.c0[lane] = c;
+      sh.c1[lane] = v;
     } else {
-      sh.c0[lane] = make_float4(kFar, kFar, kFar, -1.f);
+      c = make_float4(kFar, kFar, kFar, -1.f);
+      sh.c0[lane] = c;
     }
   } else {
-    sh.c0[lane] = lane < m ? __ldg(&s.pl[base + lane])
-                           : make_float4(kFar, kFar, kFar, __int_as_float(-1));
+    c = lane < m ? __ldg(&s.pl[base + lane]) : make_float4(kFar, kFar, kFar, __int_as_float(-1));
+    sh.c0[lane] = c;
+  }
+  if (CLASSIFY) {
+    sh.px[lane] = c.x;
+    sh.py[lane] = c.y;
+    sh.pz[lane] = c.z;
+    if (OP == SPH_OP_WALL_PRESSURE) {
+      const unsigned f = __ballot_sync(0xffffffffu, !signbit(c.w));
+      if (lane == 0) sh.fluid = f;
+    }
   }
   __syncwarp();
 }
 
 // Step A: hit mask (inside or in the band) and band mask of the 32 staged
 // candidates for a target at (ax, ay, az) relative to their cell.  The wall
-// pressure takes fluid neighbours only.
+// pressure takes fluid neighbours only.  Two candidates per packed FP32x2
+// operation; the decisions are the signs of s_hi - ss (set: beyond the
+// support) and ss - s_lo (set: below the band), exact in FP32, funnel-shifted
+// into the masks from candidate 31 down to candidate 0.
 template <int DIM, int OP>
 __device__ __forceinline__ void mx_classify(const MxShared<OP>& sh, const Consts& k, float ax,
                                             float ay, float az, unsigned& hit, unsigned& band) {
-  unsigned h = 0u, bd = 0u;
+  const unsigned long long cx = f2_pack(ax, ax), cy = f2_pack(ay, ay), cz = f2_pack(az, az);
+  const unsigned long long shi = f2_pack(k.s_hi, k.s_hi), slo = f2_pack(k.s_lo, k.s_lo);
+  const unsigned long long* x2 = reinterpret_cast<const unsigned long long*>(sh.px);
+  const unsigned long long* y2 = reinterpret_cast<const unsigned long long*>(sh.py);
+  const unsigned long long* z2 = reinterpret_cast<const unsigned long long*>(sh.pz);
+  unsigned out = 0u, low = 0u;  // bit u: candidate u beyond the support / below the band
 #pragma unroll
-  for (int u = 0; u < 32; ++u) {
-    const float4 pq = sh.c0[u];
-    const float dx = ax - pq.x;
-    const float dy = ay - pq.y;
-    float ss = dx * dx + dy * dy;
+  for (int i2 = 15; i2 >= 0; --i2) {
+    const unsigned long long dx = f2_sub(cx, x2[i2]);
+    const unsigned long long dy = f2_sub(cy, y2[i2]);
+    unsigned long long ss = f2_fma(dy, dy, f2_mul(dx, dx));
     if (DIM == 3) {
-      const float dz = az - pq.z;
-      ss = ss + dz * dz;
+      const unsigned long long dz = f2_sub(cz, z2[i2]);
+      ss = f2_fma(dz, dz, ss);
     }
-    bool in = !(ss > k.s_hi);
-    if (OP == SPH_OP_WALL_PRESSURE) in = in && !signbit(pq.w);
-    if (in) h |= 1u << u;
-    if (!(ss < k.s_lo)) bd |= 1u << u;
+    const unsigned long long dh = f2_sub(shi, ss);
+    const unsigned long long dl = f2_sub(ss, slo);
+    out = __funnelshift_l((unsigned)(dh >> 32), out, 1);
+    out = __funnelshift_l((unsigned)dh, out, 1);
+    low = __funnelshift_l((unsigned)(dl >> 32), low, 1);
+    low = __funnelshift_l((unsigned)dl, low, 1);
   }
+  unsigned h = ~out;
+  if (OP == SPH_OP_WALL_PRESSURE) h &= sh.fluid;
   hit = h;
-  band = bd & h;
+  band = ~low & h;
 }
 
 // Step B: the reference's FP64 test for every band candidate, the lanes
@@ -397,9 +429,9 @@ __device__ __forceinline__ void mx_pass(const State& s, const Geometry& g, const
         mask = t.active ? __ldg(&b.ck_mask[((size_t)ck + gi) * 32 + lane]) : 0u;
         ++gi;
         if (!__any_sync(0xffffffffu, mask != 0u)) continue;
-        mx_stage<OP>(s, sh, lane, base, m);
+        mx_stage<OP, false>(s, sh, lane, base, m);
       } else {
-        mx_stage<OP>(s, sh, lane, base, m);
+        mx_stage<OP, true>(s, sh, lane, base, m);
         unsigned band;
         mx_classify<DIM, OP>(sh, k, ax, ay, az, mask, band);
         const int self_u = t.i - base;  // core.jl:105: p == q is skipped
