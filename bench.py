@@ -611,12 +611,12 @@ PASS_KERNELS: dict = {"force": "one force pass: pair_list_kernel (every pair onc
                                "overflow sweep of pair64_kernel"}
 
 # DRAM bytes (read + write) of one FP64 force pass from the ncu capture
-# summarised in profiles/fp64_tiles_3d_dr0.025.md: pair_list_kernel 1,012,946,000
-# + 1,031,685,000 B and row_sum_kernel 1,106,376,000 + 19,414,000 B for the
+# summarised in profiles/fp64_tiles_3d_dr0.025.md: pair_list_kernel 994,898,432
+# + 1,031,022,080 B and row_sum_kernel 1,106,325,248 + 19,198,720 B for the
 # 3D dam break at dr = 0.025 (69,489,136 pair-interactions per step), scaled by
-# pair-interactions to the 5,746,633-particle case (2,077,155,042 per step).
-NCU_TRAFFIC: dict = {"force": int((1012946000 + 1031685000 + 1106376000 + 19414000)
-                                  * 2077155042 / 69489136)}
+# pair-interactions to the 5,746,633-particle case (2,078,775,269 per step).
+NCU_TRAFFIC: dict = {"force": int((994898432 + 1031022080 + 1106325248 + 19198720)
+                                  * 2078775269 / 69489136)}
 
 
 def main():
