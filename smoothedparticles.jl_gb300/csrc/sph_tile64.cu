@@ -172,13 +172,18 @@ __device__ __forceinline__ void tile_run(const State& s, const Geometry& g, cons
       if (lane < mb) {
         // two rows per packed operation; empty row slots are far away.  Any
         // FP32 rounding of the squared distance is within the band's margin.
+        // The decisions are the signs of s_hi - ss (set: beyond the support)
+        // and ss - s_lo (set: below the band), exact in FP32, funnel-shifted
+        // into the masks from row 31 down to row 0.
         const unsigned long long cx = f2_pack(pc.x, pc.x), cy = f2_pack(pc.y, pc.y);
         const unsigned long long cz = f2_pack(pc.z, pc.z);
+        const unsigned long long shi = f2_pack(k.s_hi, k.s_hi), slo = f2_pack(k.s_lo, k.s_lo);
         const unsigned long long* rx2 = reinterpret_cast<const unsigned long long*>(sh.rx);
         const unsigned long long* ry2 = reinterpret_cast<const unsigned long long*>(sh.ry);
         const unsigned long long* rz2 = reinterpret_cast<const unsigned long long*>(sh.rz);
+        unsigned out = 0u, low = 0u;
 #pragma unroll
-        for (int i2 = 0; i2 < 16; ++i2) {
+        for (int i2 = 15; i2 >= 0; --i2) {
           const unsigned long long dx = f2_sub(rx2[i2], cx);
           const unsigned long long dy = f2_sub(ry2[i2], cy);
           unsigned long long ss = f2_fma(dy, dy, f2_mul(dx, dx));
@@ -186,17 +191,15 @@ __device__ __forceinline__ void tile_run(const State& s, const Geometry& g, cons
             const unsigned long long dz = f2_sub(rz2[i2], cz);
             ss = f2_fma(dz, dz, ss);
           }
-          const float s0 = __uint_as_float((unsigned)ss);
-          const float s1 = __uint_as_float((unsigned)(ss >> 32));
-          if (!(s0 > k.s_hi)) {
-            cm |= 1u << (2 * i2);
-            if (!(s0 < k.s_lo)) bm |= 1u << (2 * i2);
-          }
-          if (!(s1 > k.s_hi)) {
-            cm |= 2u << (2 * i2);
-            if (!(s1 < k.s_lo)) bm |= 2u << (2 * i2);
-          }
+          const unsigned long long dh = f2_sub(shi, ss);
+          const unsigned long long dl = f2_sub(ss, slo);
+          out = __funnelshift_l((unsigned)(dh >> 32), out, 1);
+          out = __funnelshift_l((unsigned)dh, out, 1);
+          low = __funnelshift_l((unsigned)(dl >> 32), low, 1);
+          low = __funnelshift_l((unsigned)dl, low, 1);
         }
+        cm = ~out;
+        bm = ~low & cm;
         // a particle is not its own neighbour (core.jl:105)
         const int di = q - (sa + 32 * ia);
         if (di >= 0 && di < 32) {
