@@ -168,6 +168,7 @@ size_t carve(sph_system* s, char* base, size_t C) {
     b.hit_count = nullptr;
     b.roff = b.rcur = nullptr;
     b.xfix[0] = b.xfix[1] = b.xfix[2] = nullptr;
+    b.frec = nullptr;
     b.pair_p = b.pair_q = nullptr;
     b.pair_m = nullptr;
     b.pair_cap = 0;
@@ -179,6 +180,7 @@ size_t carve(sph_system* s, char* base, size_t C) {
     b.rows = (RowEntry*)take(sizeof(RowEntry) * (size_t)b.hit_cap * C);
     b.hit_count = (int*)take(4 * C);
     for (int d = 0; d < 3; ++d) b.xfix[d] = d < D ? (long long*)take(8 * C) : nullptr;
+    b.frec = (FxRec*)take(sizeof(FxRec) * C);  // 256-byte aligned start
     b.roff = (int*)take(4 * (size_t)s->geo.n_diff * C);
     b.rcur = (int*)take(4 * (size_t)s->geo.n_diff * C);
     // unordered pairs: a fluid-fluid pair fills two row entries, so half the

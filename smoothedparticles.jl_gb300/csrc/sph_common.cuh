@@ -107,6 +107,17 @@ __device__ __forceinline__ RowEntry row_load(const RowEntry* e) {
 }
 
 // Scratch of the binning (counting sort by cell key).
+// The FP64 force pass's record of one particle (64 bytes, two DRAM sectors,
+// rebuilt before every force pass from the SoA state, sph_tile64.cu): what
+// the force kernels gather per neighbour -- the fixed-point position copies
+// (fx_fix; X[2] = 0 in 2D), the velocity, the density and P/rho^2 -- in two
+// 256-bit loads instead of eleven scalar ones.
+struct __align__(64) FxRec {
+  long long X[3];
+  double v0;
+  double v1, v2, rho, pr;
+};
+
 struct BinScratch {
   int* keys;        // per particle (storage order before the sort)
   int* slots;       // rank of the particle inside its cell's bucket (atomic)
@@ -143,6 +154,7 @@ struct BinScratch {
   RowEntry* rows;
   int* hit_count;
   long long* xfix[3];  // positions as exact fixed-point integers (fx_fix), per step
+  FxRec* frec;         // per particle, for the force pass (FxRec)
   int* roff;          // n_diff per particle: first entry of each slot's segment
   int* rcur;          // n_diff per particle: hits per slot
   int hit_cap;
@@ -409,6 +421,32 @@ __device__ __forceinline__ double fx_sep1(long long Xp, const double* xp, const 
   const long long Xq = __ldg(&xfix[d][q]);
   if (Xp == kFxNone || Xq == kFxNone) return fx_fallback(__ldg(xp), &s.x[d][q]);
   return fx_diff(Xp, Xq, k);
+}
+
+// x_p - x_q along axis d from both copies at hand (xp, xq: the positions,
+// read only when a copy is missing)
+__device__ __forceinline__ double fx_sep2(long long Xp, const double* xp, long long Xq,
+                                          const double* xq, int k) {
+  if (Xp == kFxNone || Xq == kFxNone) return fx_fallback(__ldg(xp), xq);
+  return fx_diff(Xp, Xq, k);
+}
+
+// The two halves of a force record (one 256-bit load each).
+__device__ __forceinline__ void frec_load_x(const FxRec* r, long long& X0, long long& X1,
+                                            long long& X2, double& v0) {
+  asm("ld.global.nc.v4.b64 {%0, %1, %2, %3}, [%4];"
+      : "=l"(X0), "=l"(X1), "=l"(X2), "=d"(v0)
+      : "l"(r));
+}
+__device__ __forceinline__ void frec_load_v(const FxRec* r, double& v1, double& v2, double& rho,
+                                            double& pr) {
+  asm("ld.global.nc.v4.b64 {%0, %1, %2, %3}, [%4];"
+      : "=d"(v1), "=d"(v2), "=d"(rho), "=d"(pr)
+      : "l"(&r->v1));
+}
+
+__device__ __forceinline__ void frec_load_v12(const FxRec* r, double& v1, double& v2) {
+  asm("ld.global.nc.v2.f64 {%0, %1}, [%2];" : "=d"(v1), "=d"(v2) : "l"(&r->v1));
 }
 
 // x_p - x_q along axis d: from the fixed-point copies when both are exact

@@ -106,9 +106,9 @@ cudaError_t launch_pair_fp64(const LaunchCtx& c, const State& s, const Geometry&
 // ---- FP64 pair evaluation once per pair (sph_tile64.cu)
 // phase 0 (density pass): counts, row offsets, m W and distances into the
 // rows; phase 1 (force pass, after the density pass of the same binning):
-// pressure and XSPH factors into the rows.  Launches kTilesLaunches[phase]
-// kernels.
-constexpr int kTilesLaunches[2] = {3, 1};
+// the force records, then pressure and XSPH factors into the rows.  Launches
+// kTilesLaunches[phase] kernels.
+constexpr int kTilesLaunches[2] = {3, 2};
 // launches of the density (0) and force (1) passes of a step: the tile
 // kernels, the row sums and the traversal of overflowed rows
 constexpr int kRowPassLaunches[2] = {kTilesLaunches[0] + 2, kTilesLaunches[1] + 2};

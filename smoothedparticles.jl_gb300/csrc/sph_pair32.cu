@@ -557,8 +557,13 @@ __device__ __forceinline__ void pair32_body(const State& s, const Geometry& g, c
   cw_count<OP>(b, p.c0, p.c1, p.c2);
 }
 
+// The force pass (latency bound on its record gathers) runs at 8 blocks of 4
+// warps per SM (64 registers); 0 leaves the other passes to the compiler.
+template <int OP, int WARPS>
+constexpr int kMinBlocks32 = (OP == SPH_OP_FORCE && WARPS == 4) ? 8 : 0;
+
 template <int DIM, int OP, int WARPS>
-__global__ void __launch_bounds__(32 * WARPS) pair32_kernel(State s, Geometry g, Consts k,
+__global__ void __launch_bounds__(32 * WARPS, kMinBlocks32<OP, WARPS>) pair32_kernel(State s, Geometry g, Consts k,
                                                             BinScratch b, int self, int reset,
                                                             int fuse_eos, int list_mode) {
   __shared__ MxShared<OP> shared[WARPS];

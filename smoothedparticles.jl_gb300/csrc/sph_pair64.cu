@@ -171,16 +171,22 @@ struct Proc64 {
           atomicOr(b.d_err, kErrBounds);
           continue;
         }
-        const double d0 = fx_sep1(X0, &s.x[0][i], s, b.xfix, k.fx_k, 0, q);
-        const double d1 = fx_sep1(X1, &s.x[1][i], s, b.xfix, k.fx_k, 1, q);
+        // q's force record (sph_tile64.cu built it before this pass)
+        long long QX0, QX1, QX2;
+        double qv0;
+        frec_load_x(b.frec + q, QX0, QX1, QX2, qv0);
+        const double d0 = fx_sep2(X0, &s.x[0][i], QX0, &s.x[0][q], k.fx_k);
+        const double d1 = fx_sep2(X1, &s.x[1][i], QX1, &s.x[1][q], k.fx_k);
         ax = __fma_rn(cf, d0, ax);
         ay = __fma_rn(cf, d1, ay);
-        if (DIM == 3) az = __fma_rn(cf, fx_sep1(X2, &s.x[2][i], s, b.xfix, k.fx_k, 2, q), az);
+        if (DIM == 3) az = __fma_rn(cf, fx_sep2(X2, &s.x[2][i], QX2, &s.x[2][q], k.fx_k), az);
         if ((e & 0x80000000u) == 0u) {
           // fluid neighbour: + wx (v_q - v_p)
-          sx = __fma_rn(-wx, vp[0] - __ldg(&s.v[0][q]), sx);
-          sy = __fma_rn(-wx, vp[1] - __ldg(&s.v[1][q]), sy);
-          if (DIM == 3) sz = __fma_rn(-wx, vp[2] - __ldg(&s.v[2][q]), sz);
+          double qv1, qv2;
+          frec_load_v12(b.frec + q, qv1, qv2);
+          sx = __fma_rn(-wx, vp[0] - qv0, sx);
+          sy = __fma_rn(-wx, vp[1] - qv1, sy);
+          if (DIM == 3) sz = __fma_rn(-wx, vp[2] - qv2, sz);
           ++c0;
         } else {
           ++c1;

@@ -388,6 +388,27 @@ __global__ void __launch_bounds__(256) row_scan_kernel(State s, Geometry g, Cons
   b.hit_count[i] = run;
 }
 
+// The force records (FxRec) of every particle from the SoA state: the
+// density pass's fixed-point copies, the velocities after the step's first
+// kick, the densities and P/rho^2 after the EOS and the wall pressure.
+template <int DIM>
+__global__ void __launch_bounds__(256) frec_build_kernel(State s, BinScratch b) {
+  const int n = *b.d_n;
+  const int i = blockIdx.x * 256 + threadIdx.x;
+  if (i >= n) return;
+  const long long X0 = b.xfix[0][i], X1 = b.xfix[1][i];
+  const long long X2 = DIM == 3 ? b.xfix[2][i] : 0;
+  const double v0 = s.v[0][i], v1 = s.v[1][i];
+  const double v2 = DIM == 3 ? s.v[2][i] : 0.0;
+  FxRec* r = b.frec + i;
+  asm volatile("st.global.v4.b64 [%0], {%1, %2, %3, %4};" ::"l"(r), "l"(X0), "l"(X1), "l"(X2),
+               "d"(v0)
+               : "memory");
+  asm volatile("st.global.v4.b64 [%0], {%1, %2, %3, %4};" ::"l"(&r->v1), "d"(v1), "d"(v2),
+               "d"(s.rho[i]), "d"(s.Pr[i])
+               : "memory");
+}
+
 // The FP64 evaluation of the listed pairs into the rows (PH 0: density,
 // 1: force).  Threads stride over the list.  A side writes its entry only
 // when its target is fluid and has a row (walls and overflowed targets have
@@ -443,21 +464,34 @@ __global__ void __launch_bounds__(256, PH == 0 ? 8 : 5) pair_list_kernel(State s
       const double w = en.a, r = en.b, t = en.c;
       const double t2 = t * t;
       const double ker = k.mcr * (t2 * t);  // m rDW
-      const double sp = __ldg(&s.Pr[p]) + __ldg(&s.Pr[q]);
       if (fp && fq) {
         // pressure (collapse_symplectic.jl:114-118) + Monaghan viscosity +
-        // XSPH, in p's direction (q's is the same factor)
-        const double d0 = fx_sep(s, b.xfix, k.fx_k, 0, p, q);
-        const double d1 = fx_sep(s, b.xfix, k.fx_k, 1, p, q);
-        const double dv0 = __ldg(&s.v[0][p]) - __ldg(&s.v[0][q]);
-        const double dv1 = __ldg(&s.v[1][p]) - __ldg(&s.v[1][q]);
+        // XSPH, in p's direction (q's is the same factor); both particles'
+        // force records (frec_build_kernel), the (v1, v2, rho, P/rho^2)
+        // halves first
+        double sp, rs, dv1, dv2;
+        {
+          double pv1, pv2, prho, ppr, qv1, qv2, qrho, qpr;
+          frec_load_v(b.frec + p, pv1, pv2, prho, ppr);
+          frec_load_v(b.frec + q, qv1, qv2, qrho, qpr);
+          sp = ppr + qpr;
+          rs = prho + qrho;
+          dv1 = pv1 - qv1;
+          dv2 = DIM == 3 ? pv2 - qv2 : 0.0;
+        }
+        long long PX0, PX1, PX2, QX0, QX1, QX2;
+        double pv0, qv0;
+        frec_load_x(b.frec + p, PX0, PX1, PX2, pv0);
+        frec_load_x(b.frec + q, QX0, QX1, QX2, qv0);
+        const double d0 = fx_sep2(PX0, &s.x[0][p], QX0, &s.x[0][q], k.fx_k);
+        const double d1 = fx_sep2(PX1, &s.x[1][p], QX1, &s.x[1][q], k.fx_k);
+        const double dv0 = pv0 - qv0;
         double vdx = __fma_rn(dv1, d1, dv0 * d0);
         if (DIM == 3) {
-          const double d2 = fx_sep(s, b.xfix, k.fx_k, 2, p, q);
-          const double dv2 = __ldg(&s.v[2][p]) - __ldg(&s.v[2][q]);
+          const double d2 = fx_sep2(PX2, &s.x[2][p], QX2, &s.x[2][q], k.fx_k);
           vdx = __fma_rn(dv2, d2, vdx);
         }
-        const double inv_rb = two_over(__ldg(&s.rho[p]) + __ldg(&s.rho[q]));
+        const double inv_rb = two_over(rs);
         double pi = 0.0;
         if (lt0(vdx)) {
           // mu = h v.x / (r^2 + eta^2) with r^2 as r r and the reciprocal
@@ -472,6 +506,7 @@ __global__ void __launch_bounds__(256, PH == 0 ? 8 : 5) pair_list_kernel(State s
       } else {
         // fluid-wall: the pressure term with the wall pressure, into the
         // fluid target's row (a wall has no row entry)
+        const double sp = __ldg(&s.Pr[p]) + __ldg(&s.Pr[q]);
         const double cf = -ker * sp;
         if (wp) row_store(ep, qbits, cf, 0.0);
         if (wq) row_store(eq, pbits, cf, 0.0);
@@ -496,6 +531,7 @@ void tiles_dim(cudaStream_t st, const State& s, const Geometry& g, const Consts&
     row_scan_kernel<<<(cap + 255) / 256, 256, 0, st>>>(s, g, k, b);
     pair_list_kernel<DIM, 0><<<dens_wave, 256, 0, st>>>(s, g, k, b, dens_wave * 256);
   } else {
+    frec_build_kernel<DIM><<<(cap + 255) / 256, 256, 0, st>>>(s, b);
     pair_list_kernel<DIM, 1><<<force_wave, 256, 0, st>>>(s, g, k, b, force_wave * 256);
   }
 }
