@@ -357,7 +357,15 @@ __global__ void __launch_bounds__(256) row_scan_kernel(State s, Geometry g, Cons
   const int n = *b.d_n;
   const int i = blockIdx.x * 256 + threadIdx.x;
   if (i >= n) return;
-  for (int d = 0; d < k.dim; ++d) b.xfix[d][i] = fx_fix(s.x[d][i], k.fx_k);
+  long long X[3] = {0, 0, 0};
+  for (int d = 0; d < k.dim; ++d) {
+    X[d] = fx_fix(s.x[d][i], k.fx_k);
+    b.xfix[d][i] = X[d];
+  }
+  // the position half of the particle's record, for the density pair kernel
+  asm volatile("st.global.v4.b64 [%0], {%1, %2, %3, %4};" ::"l"(b.frec + i), "l"(X[0]),
+               "l"(X[1]), "l"(X[2]), "d"(s.v[0][i])
+               : "memory");
   const int key = s.cell[i];
   const int nd = g.n_diff;
   bool over = __ldg(&b.cell_start[key + 1]) - __ldg(&b.cell_start[key]) > 0xffff;
@@ -414,7 +422,7 @@ __global__ void __launch_bounds__(256) frec_build_kernel(State s, BinScratch b) 
 // when its target is fluid and has a row (walls and overflowed targets have
 // none); every entry is written whole.
 template <int DIM, int PH>
-__global__ void __launch_bounds__(256, PH == 0 ? 8 : 5) pair_list_kernel(State s, Geometry g, Consts k,
+__global__ void __launch_bounds__(256, PH == 0 ? 6 : 5) pair_list_kernel(State s, Geometry g, Consts k,
                                                         BinScratch b, int threads_total) {
   if (*b.d_pover) return;  // every target traverses
   const long long np = (long long)*b.d_npairs;
@@ -443,11 +451,15 @@ __global__ void __launch_bounds__(256, PH == 0 ? 8 : 5) pair_list_kernel(State s
     const unsigned long long pbits = (unsigned)p | (fp ? 0u : 0x80000000u);
     if (PH == 0) {
       // kdist64's distance, the separations formed exactly on the integer pipes
-      const double d0 = fx_sep(s, b.xfix, k.fx_k, 0, p, q);
-      const double d1 = fx_sep(s, b.xfix, k.fx_k, 1, p, q);
+      long long PX0, PX1, PX2, QX0, QX1, QX2;
+      double pv0, qv0;
+      frec_load_x(b.frec + p, PX0, PX1, PX2, pv0);
+      frec_load_x(b.frec + q, QX0, QX1, QX2, qv0);
+      const double d0 = fx_sep2(PX0, &s.x[0][p], QX0, &s.x[0][q], k.fx_k);
+      const double d1 = fx_sep2(PX1, &s.x[1][p], QX1, &s.x[1][q], k.fx_k);
       double ss = __fma_rn(d1, d1, d0 * d0);
       if (DIM == 3) {
-        const double d2 = fx_sep(s, b.xfix, k.fx_k, 2, p, q);
+        const double d2 = fx_sep2(PX2, &s.x[2][p], QX2, &s.x[2][q], k.fx_k);
         ss = __fma_rn(d2, d2, ss);
       }
       const double r = isqrt_rn(ss);
