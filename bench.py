@@ -606,17 +606,18 @@ def l2_note(resident: int) -> str:
 
 
 # The kernels of one FP64 force pass of a step (the roofline's unit).
-PASS_KERNELS: dict = {"force": "one force pass: pair_list_kernel (every pair once) + "
-                               "row_sum_kernel (each target's row in order) + the "
-                               "overflow sweep of pair64_kernel"}
+PASS_KERNELS: dict = {"force": "one force pass: frec_build_kernel (particle records) + "
+                               "pair_list_kernel (every pair once) + row_sum_kernel (each "
+                               "target's row in order) + the overflow sweep of pair64_kernel"}
 
 # DRAM bytes (read + write) of one FP64 force pass from the ncu capture
-# summarised in profiles/fp64_tiles_3d_dr0.025.md: pair_list_kernel 994,898,432
-# + 1,031,022,080 B and row_sum_kernel 1,106,325,248 + 19,198,720 B for the
-# 3D dam break at dr = 0.025 (69,489,136 pair-interactions per step), scaled by
+# summarised in profiles/fp64_tiles_3d_dr0.025.md: frec_build_kernel
+# 19,521,280 + 256 B, pair_list_kernel 1,013,006,592 + 1,076,423,680 B and
+# row_sum_kernel 1,129,463,040 + 21,318,400 B for the 3D dam break at
+# dr = 0.025 (69,489,136 pair-interactions per step), scaled by
 # pair-interactions to the 5,746,633-particle case (2,078,775,269 per step).
-NCU_TRAFFIC: dict = {"force": int((994898432 + 1031022080 + 1106325248 + 19198720)
-                                  * 2078775269 / 69489136)}
+NCU_TRAFFIC: dict = {"force": int((19521280 + 256 + 1013006592 + 1076423680 + 1129463040
+                                   + 21318400) * 2078775269 / 69489136)}
 
 
 def main():
