@@ -34,11 +34,13 @@
 // Passes of a step (launch order):
 //   tiles    classify once: rcur := hits per (target, slot); the pair list
 //            (p, q, both ranks, slot, wall bits)
-//   scan     roff := exclusive prefix over the target's slots; hit_count
-//   density  per pair: r and m W into both rows (at roff + rank)
+//   scan     roff := exclusive prefix over the target's slots; hit_count;
+//            the fixed-point positions (xfix and the records' first halves)
+//   density  per pair: m W, r and t into both rows (at roff + rank)
 //   [sum]    sph_pair64.cu: rho = the row's sum, self term, EOS
 //   [wall]   sph_pair64.cu: each wall's pressure over its row (fluid
-//            neighbours, the kernel value from the stored distance)
+//            neighbours, the kernel value from the stored t)
+//   records  every particle's FxRec from the current fields
 //   force    per pair: cf and wx into both rows (a fluid-wall pair only into
 //            the fluid target's row: walls are not force targets)
 //   [sum]    sph_pair64.cu: a += cf d, xs += -wx dv over the row
