@@ -150,7 +150,10 @@ int sph_sum_particle(sph_system* sys, int func, int64_t nq, const int64_t* index
 /* One verlet_step! (examples/collapse_symplectic.jl:170-180) per step: kick,
  * drift, create_cell_list!, density sum with self term, Tait EOS, wall
  * pressure, force, kick; the kick + drift run inside the binning's key kernel
- * and the EOS inside the density pass. */
+ * and the EOS inside the density pass.  From four steps per call (and with
+ * per-kernel timing off) the steps replay a CUDA graph of two steps captured
+ * on first use and kept until the system's buffers, particle count or tuning
+ * change; the results are those of single steps. */
 int sph_step(sph_system* sys, int nsteps);
 /* Initial state of the dam break (collapse_symplectic.jl:186-191 plus the
  * hydrostatic reference density): bin, rho_ref sum, hydrostatic scaling,

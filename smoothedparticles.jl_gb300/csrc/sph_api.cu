@@ -22,6 +22,10 @@ using namespace sphgpu;
 struct sph_batch {
   std::vector<sph_system*> members;
   std::vector<long long> generations;
+  // each member's current particle set (x of its `cur` ping-pong half) when
+  // the graph was captured: a graph of two steps starts from that half, so
+  // after an odd number of steps taken outside it the graph is stale
+  std::vector<const double*> cur0;
   int device = 0;
   cudaStream_t origin = nullptr;
   cudaEvent_t fork = nullptr;
@@ -480,6 +484,7 @@ int sph_create(const sph_params* p, int device, sph_system** out) {
 int sph_destroy(sph_system* s) {
   if (!s) return SPH_ERR_ARG;
   DeviceGuard guard(s->device);
+  if (s->solo) sph_batch_destroy(s->solo);
   cudaStreamSynchronize(s->stream);
   for (auto& p : s->pending) {
     cudaEventDestroy(p.start);
@@ -546,6 +551,8 @@ int sph_upload(sph_system* s, int64_t n, const double* x, const double* v, const
   if (e != cudaSuccess) return fail(s, SPH_ERR_CUDA, "upload: %s", cudaGetErrorString(e));
   CK(cudaStreamSynchronize(s->stream));
   s->n_host = (int)n;
+  // a captured step sized its grids by the previous count: capture again
+  ++s->generation;
   s->cells_valid = false;
   s->aux_fluid = s->aux_wall = false;
   s->lists_valid = false;
@@ -672,6 +679,7 @@ int sph_generate(sph_system* s, const sph_shape* shapes, int count, int64_t* n_o
   if (e != cudaSuccess) return fail(s, SPH_ERR_CUDA, "generate: %s", cudaGetErrorString(e));
   CK(cudaStreamSynchronize(s->stream));
   s->n_host = (int)total;
+  ++s->generation;  // as in sph_upload
   s->cells_valid = false;
   s->aux_fluid = s->aux_wall = false;
   s->lists_valid = false;
@@ -826,9 +834,38 @@ static int step_once(sph_system* s) {
   return unary(s, SPH_OP_KICK);
 }
 
+// Steps per call from which sph_step replays a captured CUDA graph.
+constexpr int kGraphSteps = 4;
+
 int sph_step(sph_system* s, int nsteps) {
   if (!s || nsteps < 0) return SPH_ERR_ARG;
   DeviceGuard guard(s->device);
+  // Many steps at once, without per-kernel timing: replay a captured
+  // two-step CUDA graph of this system alone (a batch of one, kept until the
+  // system's buffers, count or tuning change) instead of launching every
+  // kernel from the host -- small systems are bound by those launches.  The
+  // graph holds the kernels of step_once, so the results are the same.
+  if (nsteps >= kGraphSteps && !s->profiling && s->n_host > 0 && s->arena) {
+    if (!s->solo) {
+      sph_system* self = s;
+      const int rc = sph_batch_create(&self, 1, &s->solo);
+      if (rc) return fail(s, rc, "cannot set up the step graph");
+    }
+    sph_batch* b = s->solo;
+    if (b->fused_warps != s->k.warps) sph_batch_set_tuning(b, s->k.warps);
+    if (b->exec && (nsteps & 1) && b->cur0[0] != s->cur.x[0]) {
+      // an odd count on the other ping-pong half than the graph's: the
+      // single step first brings it back, and the graph serves the rest
+      const int rc = step_once(s);
+      if (rc) return rc;
+      --nsteps;
+    }
+    const long long l0 = b->launches;
+    const int rc = sph_batch_step(b, nsteps);
+    s->total_launches += b->launches - l0;
+    if (rc) return fail(s, rc, "step graph: %s", b->err.c_str());
+    return SPH_OK;
+  }
   for (int it = 0; it < nsteps; ++it) {
     const int rc = step_once(s);
     if (rc) return rc;
@@ -1128,6 +1165,7 @@ static int batch_capture_fused(sph_batch* b) {
     m->aux_fluid = m->aux_wall = true;
     m->lists_valid = true;
     b->generations[j] = m->generation;
+    b->cur0[j] = m->cur.x[0];
   }
   return SPH_OK;
 }
@@ -1163,6 +1201,7 @@ static int batch_capture(sph_batch* b) {
     b->members[j]->total_launches = before[j];  // captured, not yet executed
     b->members[j]->profiling = prof[j];
     b->generations[j] = b->members[j]->generation;
+    b->cur0[j] = b->members[j]->cur.x[0];
   }
   if (rc) {
     if (g) cudaGraphDestroy(g);
@@ -1198,6 +1237,7 @@ int sph_batch_create(sph_system* const* members, int count, sph_batch** out) {
       b->fusable = false;
   b->fused = b->fusable;
   b->generations.assign(count, -1);
+  b->cur0.assign(count, nullptr);
   b->device = members[0]->device;
   DeviceGuard guard(b->device);
   bool ok = cudaStreamCreateWithFlags(&b->origin, cudaStreamNonBlocking) == cudaSuccess &&
@@ -1237,7 +1277,9 @@ int sph_batch_step(sph_batch* b, int nsteps) {
   DeviceGuard guard(b->device);
   bool stale = !b->exec;
   for (size_t j = 0; j < b->members.size(); ++j)
-    if (b->generations[j] != b->members[j]->generation) stale = true;
+    if (b->generations[j] != b->members[j]->generation ||
+        b->cur0[j] != b->members[j]->cur.x[0])
+      stale = true;
   if (nsteps >= 2 && stale) {
     // the members' own streams may still run earlier work: order after it
     for (auto* m : b->members) {

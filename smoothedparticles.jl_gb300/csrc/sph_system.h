@@ -51,6 +51,8 @@ struct sph_system {
   // bumped whenever device buffers are reallocated or the launch shape
   // changes, so a batch knows its captured graph is stale
   long long generation = 0;
+  // sph_step's captured two-step graph (a batch of this system alone)
+  sph_batch* solo = nullptr;
 };
 
 namespace sphgpu {

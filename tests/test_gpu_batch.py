@@ -36,7 +36,9 @@ def test_batch_equals_alone(gpu, precision):
     mem = [make(c, precision) for c in cases]
     ref = [make(c, precision) for c in cases]
     b = sphgpu.Batch(mem)
-    for nsteps in (4, 3, 1, 6):
+    # an odd count leaves the members on the other ping-pong half than the
+    # captured graph's: the next graph launch must capture again
+    for nsteps in (4, 3, 4, 1, 6):
         b.step(nsteps)
         for r in ref:
             r.step(nsteps)
@@ -44,7 +46,7 @@ def test_batch_equals_alone(gpu, precision):
         for m, r in zip(mem, ref):
             assert_equal(m, r)
     st = b.stats()
-    assert st["graph_launches"] == 2 + 1 + 0 + 3
+    assert st["graph_launches"] == 2 + 1 + 2 + 0 + 3
     assert st["kernels_per_graph"] > 0
     # members keep their own accounting of pairs: same totals as alone
     for m, r in zip(mem, ref):
@@ -70,6 +72,56 @@ def test_batch_recapture_after_upload(gpu):
     b.synchronize()
     assert_equal(mem[1], ref)
     assert b.stats()["graph_launches"] == 3
+
+
+@pytest.mark.parametrize("precision", [sphgpu.FP64, sphgpu.MIXED])
+def test_step_graph_equals_single_steps(gpu, precision):
+    """sph_step of four or more steps replays a captured graph of the system;
+    its fields equal those of the same steps taken one call at a time, for
+    even and odd counts in any order (an odd count moves the system to the
+    other ping-pong half) and after the system is re-uploaded."""
+    c = G.dam_break(2, 0.03)
+    g, r = make(c, precision), make(c, precision)
+    for nsteps in (6, 5, 4, 5, 5, 1, 7):
+        g.step(nsteps)
+        for _ in range(nsteps):
+            r.step(1)
+        assert_equal(g, r)
+    assert g.pair_count() == r.pair_count()
+    c2 = G.dam_break(2, 0.035)
+    for s_ in (g, r):
+        s_.upload(c2.x, c2.v, type=c2.type)
+        s_.init_state()
+    g.step(8)
+    for _ in range(8):
+        r.step(1)
+    assert_equal(g, r)
+    if precision == sphgpu.FP64:
+        assert g.launch_count() == r.launch_count()
+
+
+@pytest.mark.parametrize("precision", [sphgpu.FP64, sphgpu.MIXED])
+def test_batch_recapture_after_upload_within_capacity(gpu, precision):
+    """A member re-uploaded with more particles than when the batch captured
+    its steps, but within the buffers it already holds: the captured graph's
+    launch sizes are stale, so the batch captures again."""
+    big = G.dam_break(2, 0.025, col_height=1.5)
+    half = G.Case("half", 2, big.dr, big.x[::2].copy(), big.type[::2].copy(),
+                  big.v[::2].copy(), big.params)
+    m = make(big, precision)          # buffers for the full set
+    m.upload(half.x, half.v, type=half.type)
+    m.init_state()
+    b = sphgpu.Batch([m])
+    b.step(2)                         # captured with the half set's count
+    m.upload(big.x, big.v, type=big.type)
+    m.init_state()
+    ref = make(big, precision)
+    b.step(4)
+    ref.step(4)
+    b.synchronize()
+    assert_equal(m, ref)
+    assert b.stats()["graph_launches"] == 3
+    b.close()
 
 
 @pytest.mark.parametrize("precision", [sphgpu.FP64, sphgpu.MIXED])
