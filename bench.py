@@ -377,7 +377,8 @@ def run_ensemble(args, torch, dev):
     ms = e0.elapsed_time(e1)
     pairs = sum(g.pair_count(reset=True) for g in mem)
     bst = b.stats()
-    # the same members stepped by sph_step on their own streams (no graph)
+    # the same members stepped by sph_step on their own streams (each member
+    # replays its own two-step graph: one graph launch per member and step pair)
     torch.cuda.synchronize(dev)
     t0 = time.perf_counter()
     for g in mem:
@@ -404,7 +405,8 @@ def run_ensemble(args, torch, dev):
                   "note": ("fused steps: each kernel of the step is one launch over all members"
                            if b.fused else "one graph branch per member")},
         "unbatched": {"value": pairs_plain / t_plain, "ms_per_step": 1e3 * t_plain / S,
-                      "note": "same members, sph_step per member on its own stream, host timer"},
+                      "note": "same members, sph_step per member on its own stream (a two-step "
+                              "graph of that member alone), host timer"},
         "autotune": {str(k): {"warps_per_block": v[0],
                               "ms_per_step": {str(w): round(t, 4) for w, t in v[1].items()}}
                      for k, v in sorted(table.items())},
