@@ -300,9 +300,11 @@ int sph_query(sph_system* sys, int* idle);
  * member an independent branch; every further pair of steps is one graph
  * launch, and the branches overlap on the device.  An odd last step runs on
  * the members' own streams.  Each member's results are bit-identical to
- * stepping it alone.  The graph is captured again when a member's buffers or
- * tuning changed; members must outlive the batch and must not be stepped by
- * other calls while a batch step is in flight. */
+ * stepping it alone.  The graph is captured again when a member's buffers,
+ * particle set (sph_upload, sph_generate) or tuning changed, or when an odd
+ * number of steps taken outside the graph left a member on the other half of
+ * its ping-pong buffers; members must outlive the batch and must not be
+ * stepped by other calls while a batch step is in flight. */
 typedef struct sph_batch sph_batch;
 int sph_batch_create(sph_system* const* members, int count, sph_batch** out);
 int sph_batch_destroy(sph_batch* batch);
