@@ -215,7 +215,9 @@ class ParticleSystem:
         return out
 
     def step(self, nsteps: int = 1):
-        """verlet_step! (collapse_symplectic.jl:170-180), nsteps times."""
+        """verlet_step! (collapse_symplectic.jl:170-180), nsteps times; four or more
+        steps per call (with per-kernel timing off) replay a captured two-step
+        CUDA graph of this system, with the same results."""
         self._check(self._lib.sph_step(self._h, int(nsteps)))
 
     def init_state(self):
