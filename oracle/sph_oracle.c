@@ -360,8 +360,9 @@ static int64_t binary_one(orc_system* s, int op, int64_t p) {
         double pi = 0.0;
         if (vdx < 0.0) {
           /* Monaghan: -alpha c0 mu / rho_bar, mu = h v.x / (r^2 + eta^2),
-           * r^2 as r r, the quotient as a product with the reciprocal */
-          pi = ((s->ca * vdx) * (1.0 / (rk * rk + s->eta2))) * inv_rb;
+           * r^2 + eta^2 as one fused multiply-add, the quotient as a product
+           * with the reciprocal */
+          pi = ((s->ca * vdx) * (1.0 / fma(rk, rk, s->eta2))) * inv_rb;
         }
         const double cf = -ker * ((prp + s->Pr[q]) + pi);
         ax = fma(cf, d[0], ax);

@@ -102,8 +102,9 @@ struct Proc64 {
         const double inv_rb = two_over(rhop + rhoq);
         double pi = 0.0;
         if (lt0(vdx)) {
-          // mu = h v.x / (r^2 + eta^2) with r^2 as r r and the reciprocal
-          pi = ((k.ca * vdx) * __drcp_rn(r * r + k.eta2)) * inv_rb;
+          // mu = h v.x / (r^2 + eta^2), r^2 + eta^2 as one fused multiply-add,
+          // the quotient as a product with the reciprocal
+          pi = ((k.ca * vdx) * __drcp_rn(__fma_rn(r, r, k.eta2))) * inv_rb;
           ++c2;
         }
         const double cf = -ker * ((prp + __ldg(&s.Pr[q])) + pi);

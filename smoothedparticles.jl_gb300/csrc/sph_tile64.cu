@@ -508,8 +508,9 @@ __global__ void __launch_bounds__(256, PH == 0 ? 6 : 5) pair_list_kernel(State s
         const double inv_rb = two_over(rs);
         double pi = 0.0;
         if (lt0(vdx)) {
-          // mu = h v.x / (r^2 + eta^2) with r^2 as r r and the reciprocal
-          pi = ((k.ca * vdx) * ircp_rn(r * r + k.eta2)) * inv_rb;
+          // mu = h v.x / (r^2 + eta^2), r^2 + eta^2 as one fused multiply-add,
+          // the quotient as a product with the reciprocal
+          pi = ((k.ca * vdx) * ircp_rn(__fma_rn(r, r, k.eta2))) * inv_rb;
           // one count per direction whose row is summed
           av += (wp ? 1 : 0) + (wq ? 1 : 0);
         }
