@@ -147,21 +147,26 @@ struct Acc32 {
   // a hit on the neighbour with position / record (pq, vq) in a cell at
   // offset `off` from the target's cell
   __device__ __forceinline__ void hit(const float4& pq, const float4& vq, const float4& off) {
-    const float hx = (pi4.x - pq.x) - off.x;
-    const float hy = (pi4.y - pq.y) - off.y;
-    const float hz = DIM == 3 ? (pi4.z - pq.z) - off.z : 0.f;
+    hit_rel(pq, vq, pi4.x - off.x, pi4.y - off.y, pi4.z - off.z);
+  }
+  // the same with the target's position relative to the neighbour's cell
+  // (ax, ay, az) at hand, as step A forms the separations
+  __device__ __forceinline__ void hit_rel(const float4& pq, const float4& vq, float ax, float ay,
+                                          float az) {
+    const float hx = ax - pq.x;
+    const float hy = ay - pq.y;
+    const float hz = DIM == 3 ? az - pq.z : 0.f;
     float ss = hx * hx + hy * hy;
     if (DIM == 3) ss = ss + hz * hz;
     const float r = fsqrt(ss);
     const float kt = kt32(k, r);
-    ++nh;
+    // the density and wall-pressure passes count their hits per chunk
+    if (OP == SPH_OP_FORCE) ++nh;
     if (OP == SPH_OP_DENSITY || OP == SPH_OP_DENSITY_REF) {
-      ++c0;
       // the shape t^4 (1 + 4x) only; m * C_w is applied per batch
       const float t2 = kt * kt;
       f0 += (t2 * t2) * (5.f - 4.f * kt);
     } else if (OP == SPH_OP_WALL_PRESSURE) {
-      ++c0;
       // Adami, Hu & Adams (2012) wall pressure, g . (x_w - x_f)
       const float w = kw32(k, r, kt);
       float gd = k.gf[0] * hx + k.gf[1] * hy;
@@ -446,12 +451,17 @@ __device__ __forceinline__ void mx_pass(const State& s, const Geometry& g, const
       }
       // keep every lane's FP32 batch at <= 32 hits (one decision per warp)
       if (__any_sync(0xffffffffu, a.nh + __popc(mask) > 32)) a.fold();
+      if (OP != SPH_OP_FORCE) {
+        const int hits = __popc(mask);
+        a.nh += hits;
+        a.c0 += hits;
+      }
       while (mask) {
         const int u = __ffs(mask) - 1;
         mask &= mask - 1u;
         float4 vq = make_float4(0.f, 0.f, 0.f, 0.f);
         if constexpr (MxShared<OP>::kRec) vq = sh.c1[u];
-        a.hit(sh.c0[u], vq, off);
+        a.hit_rel(sh.c0[u], vq, ax, ay, az);
       }
     }
   }

@@ -149,10 +149,14 @@ struct Proc64 {
         const double t = en.c;  // ker_t of the stored distance
         const double t2 = t * t;
         const double w = (k.cw * (t2 * t2)) * __fma_rn(-4.0, t, 5.0);
-        const double d0 = fx_sep1(X0, &s.x[0][i], s, b.xfix, k.fx_k, 0, q);
-        const double d1 = fx_sep1(X1, &s.x[1][i], s, b.xfix, k.fx_k, 1, q);
+        // q's position half of its record (the density pass's row scan)
+        long long QX0, QX1, QX2;
+        double qv0;
+        frec_load_x(b.frec + q, QX0, QX1, QX2, qv0);
+        const double d0 = fx_sep2(X0, &s.x[0][i], QX0, &s.x[0][q], k.fx_k);
+        const double d1 = fx_sep2(X1, &s.x[1][i], QX1, &s.x[1][q], k.fx_k);
         double gd = __fma_rn(k.g[1], d1, k.g[0] * d0);
-        if (DIM == 3) gd = __fma_rn(k.g[2], fx_sep1(X2, &s.x[2][i], s, b.xfix, k.fx_k, 2, q), gd);
+        if (DIM == 3) gd = __fma_rn(k.g[2], fx_sep2(X2, &s.x[2][i], QX2, &s.x[2][q], k.fx_k), gd);
         wp = __fma_rn(__ldg(&s.P[q]), w, wp);
         wg = __fma_rn(__ldg(&s.rho[q]) * gd, w, wg);
         ws = ws + w;
