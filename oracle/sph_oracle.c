@@ -10,12 +10,14 @@
  *
  * Evaluation order shared with the GPU library (the definition of the FP64
  * path; kernels.jl is @fastmath, so this is one admissible reading of it):
- *   x   = r * (1/H)                      (1/H computed once)
- *   W   = (Cw * t4) * (1 + 4x),  t = 1 - x, t2 = t*t, t4 = t2*t2
+ *   r   = sqrt(fma(d2, d2, fma(d1, d1, d0 * d0)))   the kernel distance (the
+ *         support test keeps the reference's unfused dist, core.jl:8-10)
+ *   t   = fma(-r, 1/H, 1) (= 1 - x, x = r/H; 1/H computed once), 0 when < 0
+ *   W   = (Cw * (t2 * t2)) * fma(-4, t, 5),  t2 = t*t  (5 - 4t = 1 + 4x)
  *         Cw = 7/pi / H^2 (2D), 21/(2 pi) / H^3 (3D), H^2 = H*H, H^3 = H^2*H
  *   rDW = Cr * (t2 * t)
  *         Cr = -140/pi / H^4 (2D), -210/pi / H^5 (3D), H^4 = H^2*H^2, H^5 = H^4*H
- *   W = rDW = 0 when x > 1
+ *   the mass is folded into the constants (m Cw, m Cr) in the pair operators
  */
 #include "sph_oracle.h"
 
