@@ -37,20 +37,53 @@ METRIC = "pair-interactions/s, 3D WCSPH 4M ptcl"
 UNIT = "pair-interactions/s"
 L2_BYTES = 129 * 2**20
 
-# Algorithmic FP64 flops per evaluated hit (add/sub/mul/compare = 1,
-# sqrt = 1, division = 1), counted from the operator formulas in
-# csrc/sph_pair64.cu, 3D:
-#   distance 9 (3 sub, 3 mul, 2 add, sqrt); W 9; rDW 6
-#   density hit        = distance + W + m*W + add                       = 20
-#   wall-pressure hit  = distance + W + g.d (5) + 6 accumulate ops      = 29
-#   force fluid hit    = distance + rDW + m* + dv (3) + v.d (5) + rho sum
-#                        + 2/(..) + compare + P-sum (2) + coefficient
-#                        + a += (6) + W + m* + *inv + XSPH (9)         = 56
-#   force wall hit     = distance + rDW + m* + P-sum + coefficient + a += (6) = 24
-#   viscosity active   = +5 (h*v.d, r^2+eta^2, division, -a c0 *, * 1/rho)
-# 2D drops the z terms: distance 6, g.d 3, dv 2, v.d 3, a += 4, XSPH 6.
-FLOPS_BY_DIM = {3: dict(density=20, wall=29, force_fluid=56, force_wall=24, force_av=5),
-                2: dict(density=17, wall=24, force_fluid=45, force_wall=19, force_av=5)}
+# Algorithmic flops of the pair passes (add/sub/mul/compare = 1, a fused
+# multiply-add = 2, sqrt = 1, division or reciprocal = 1).  The FP64 path
+# evaluates every unordered pair ONCE for both of its targets (sph_tile64.cu)
+# and then accumulates each target's row, so its count is per unordered pair
+# (the shared work) plus per directed hit (each target's accumulation); the
+# mixed path evaluates every directed hit in full (sph_pair32.cu), so its count
+# is per directed hit.  3D (2D drops the z terms):
+#   FP64 density, per unordered pair (fluid-fluid and fluid-wall):
+#       d 3 + squares 5 + sqrt 1 + t = 1 - r/H 2 + clamp 1 + m W 6       = 18
+#     per directed entry of a fluid target: the row sum 1
+#   FP64 wall pressure, per wall entry: W from the stored t 6 + d 3
+#       + g.d 5 + the three sums 6                                        = 20
+#   FP64 force, per unordered fluid-fluid pair: m rDW 3 + P-sum 1
+#       + rho-sum 1 + dv 3 + d 3 + v.d 5 + 2/rho-sum 1 + compare 1
+#       + coefficient 2 + m W/rho-bar 1                                   = 21
+#     + viscosity where active: r^2 + eta^2 2, reciprocal 1, 3 products  = 6
+#     per unordered fluid-wall pair: m rDW 3 + P-sum 1 + coefficient 1
+#       + d 3                                                             = 8
+#     per directed entry: a += cf d 6 (+ xsph += -wx dv 6, fluid q)
+#   mixed, per directed hit: density 18, wall pressure 31, force with a
+#     fluid q 55 (wall q 24); the candidate classification is overhead.
+FP64_FLOPS = {3: dict(dens_pair=18, dens_entry=1, wall=20, ff_pair=21, av_pair=6, fw_pair=8,
+                      acc_a=6, acc_x=6),
+              2: dict(dens_pair=15, dens_entry=1, wall=17, ff_pair=17, av_pair=6, fw_pair=7,
+                      acc_a=4, acc_x=4)}
+MIXED_FLOPS = {3: dict(density=18, wall=31, force_fluid=55, force_wall=24),
+               2: dict(density=15, wall=26, force_fluid=45, force_wall=19)}
+
+
+def pass_flops(cats, dim, mixed):
+    """Algorithmic flops of the density, wall-pressure and force passes from
+    the hit counts per category (sph_pair_stats: directed hits of the
+    operators' targets; the viscosity count is per summed direction)."""
+    if mixed:
+        F = MIXED_FLOPS[dim]
+        return {"density": cats["density"] * F["density"],
+                "wall_pressure": cats["wall"] * F["wall"],
+                "force": cats["force_fluid"] * F["force_fluid"]
+                + cats["force_wall"] * F["force_wall"]}
+    F = FP64_FLOPS[dim]
+    u_ff = cats["force_fluid"] / 2.0   # both directions of a fluid pair are summed
+    u_fw = cats["force_wall"]          # walls are not force targets
+    u_av = cats["force_av"] / 2.0
+    return {"density": (u_ff + u_fw) * F["dens_pair"] + cats["density"] * F["dens_entry"],
+            "wall_pressure": cats["wall"] * F["wall"],
+            "force": u_ff * F["ff_pair"] + u_av * F["av_pair"] + u_fw * F["fw_pair"]
+            + cats["force_fluid"] * (F["acc_a"] + F["acc_x"]) + cats["force_wall"] * F["acc_a"]}
 
 
 def parse():
@@ -61,7 +94,8 @@ def parse():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--dr", type=float, default=0.0079)
     ap.add_argument("--dim", type=int, default=3)
-    ap.add_argument("--e2e-steps", type=int, default=3)
+    ap.add_argument("--e2e-steps", type=int, default=0,
+                    help="steps of the end-to-end leg (0: the same as --steps)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--error-steps", type=int, default=300,
                     help="steps after which the mixed run is compared with the FP64 run (0: off)")
@@ -248,17 +282,11 @@ def timed_steps(g, torch, dev, steps, world):
     return out
 
 
-def kernel_table(kst, cats, steps, dim):
+def kernel_table(kst, cats, steps, dim, mixed=False):
     """Per kernel family: total and per-launch time, per-step time and, for the
     pair passes, algorithmic flops per step (the FP64 density and force passes
     of a step are several kernels each: tiles, pair evaluation, row sums)."""
-    FLOPS = FLOPS_BY_DIM[dim]
-    flops = {
-        "force": cats["force_fluid"] * FLOPS["force_fluid"] + cats["force_wall"] * FLOPS["force_wall"]
-        + cats["force_av"] * FLOPS["force_av"],
-        "density": cats["density"] * FLOPS["density"],
-        "wall_pressure": cats["wall"] * FLOPS["wall"],
-    }
+    flops = pass_flops(cats, dim, mixed)
     tot = sum(v[0] for v in kst.values())
     rows = {}
     for k, (tms, nl) in kst.items():
@@ -488,9 +516,10 @@ def run_ours(args):
     for f in ("x", "v", "a", "xsph"):
         g.get(f, out=h[f])
     g.pair_count(reset=True)
+    e2e_steps = args.e2e_steps if args.e2e_steps > 0 else args.steps
     torch.cuda.synchronize(dev)
     t0 = time.perf_counter()
-    for _ in range(args.e2e_steps):
+    for _ in range(e2e_steps):
         for f in ("x", "v", "a", "xsph"):
             g.set(f, h[f])
         g.step(1)
@@ -499,11 +528,11 @@ def run_ours(args):
     t_e2e = time.perf_counter() - t0
     e2e = {"value": g.pair_count(reset=True) / t_e2e, "unit": UNIT,
            "h2d_bytes_per_step": int(n * 4 * 24), "d2h_bytes_per_step": int(n * (4 * 24 + 2 * 8)),
-           "steps": args.e2e_steps,
+           "steps": e2e_steps, "ms_per_step": 1e3 * t_e2e / e2e_steps,
            "note": "per step: set x, v, a, xsph from pinned host arrays; sph_step; get x, v, a, "
                    "xsph, rho, P into pinned host arrays (reference particle order)"}
     # the FP64 run continues (untimed) to the comparison step
-    done64 = args.warmup + args.steps + args.e2e_steps
+    done64 = args.warmup + args.steps + e2e_steps
     target = max(args.error_steps, done64)
     if args.error_steps > 0 and target > done64:
         g.step(target - done64)
@@ -528,7 +557,7 @@ def run_ours(args):
                  {"steps": target, "fields": field_errors(long64, longmx),
                   "note": "both runs from their own initial state (init_state of the same lattice)"}
                  if long64 is not None else None),
-             "kernels": kernel_table(rmx["kernels"], rmx["cats"], args.steps, case.dim),
+             "kernels": kernel_table(rmx["kernels"], rmx["cats"], args.steps, case.dim, True),
              "binning_hbm": None,
              "gpu_launches": rmx["launches"], "clocks": rmx["clocks"]}
     # one step from an identical FP64 state (reference density included): the
@@ -566,8 +595,19 @@ def run_ours(args):
                 "fp32_peak_tflops": round(2.0 * ffma / 1e12, 3),
                 "flops_per_pass": kt[dom]["flops_per_step"],
                 "ms_per_pass": kt[dom]["ms_per_step"],
-                "note": "algorithmic flops count sqrt and division as 1 each; on GB300 each costs "
-                        "~10 FP64 pipe slots, and the FP64 parity path cannot fuse mul+add"}
+                "note": "algorithmic flops of the pair-once algorithm: the shared work of an "
+                        "unordered pair once, each target's accumulation once per direction "
+                        "(bench.py FP64_FLOPS); sqrt and division count 1 each"}
+    # the mixed step's dominant pass against the measured FP32 FMA rate
+    kmx = mixed["kernels"]
+    mdom = max((k for k in kmx if "tflops" in kmx[k]), key=lambda k: kmx[k]["ms_total"])
+    peak32 = 2.0 * ffma / 1e12
+    ach32 = kmx[mdom]["flops_per_step"] / (kmx[mdom]["ms_per_step"] * 1e-3) / 1e12
+    mixed["roofline"] = {"bound": "fp32", "kernel": mdom, "achieved": round(ach32, 3),
+                         "peak": round(peak32, 3), "unit": "TFLOP/s",
+                         "frac": round(ach32 / peak32, 4),
+                         "note": "per directed hit (the mixed passes evaluate every hit "
+                                 "in full; bench.py MIXED_FLOPS)"}
 
     ensemble = run_ensemble(args, torch, dev) if args.ens_members > 0 else None
     served = run_served(args, torch, dev) if args.serve_requests > 0 else None
@@ -593,10 +633,52 @@ def run_ours(args):
             "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": r64["launches"],
             "clocks": r64["clocks"],
         }
+        # a compact digest of the legs, last on the line so that a reader of
+        # the output's tail sees it
+        line["summary"] = summary(line, resident)
         print(json.dumps(line), flush=True)
     if world > 1:
         torch.distributed.destroy_process_group()
     return 0
+
+
+def _r(v, k=4):
+    return None if v is None else float(f"{v:.{k}g}")
+
+
+def summary(line, resident):
+    """The headline figures of every leg in a few hundred bytes."""
+    mx, rf = line["mixed"], line["roofline"]
+    out = {"fp64": {"ms_per_step": _r(line["ms_per_step"]), "pairs_per_s": _r(line["value"]),
+                    "roofline_frac": rf["frac"], "roofline_kernel": rf["kernel"],
+                    "e2e_pairs_per_s": _r(line["e2e"]["value"]),
+                    "resident_gb": _r(resident / 1e9, 3)},
+           "mixed": {"ms_per_step": _r(mx["ms_per_step"]), "pairs_per_s": _r(mx["value"]),
+                     "speedup_vs_fp64": _r(mx["speedup_vs_fp64"], 3),
+                     "roofline_frac": mx["roofline"]["frac"],
+                     "roofline_kernel": mx["roofline"]["kernel"]}}
+    one = mx.get("error_vs_fp64_one_step") or {}
+    out["mixed"]["err_one_step_rel"] = {f: _r(one[f]["rel_norm"], 2) for f in ("rho", "P", "a", "x")
+                                        if f in one}
+    run = (mx.get("error_vs_fp64_after_run") or {}).get("fields") or {}
+    out["mixed"]["err_after_run_rel"] = {f: _r(run[f]["rel_norm"], 2) for f in ("rho", "P", "a", "x")
+                                         if f in run}
+    ens = line.get("ensemble")
+    if ens:
+        out["ensemble"] = {"ms_per_step": _r(ens["ms_per_step"]), "pairs_per_s": _r(ens["value"]),
+                           "member_steps_per_s": _r(ens["member_steps_per_s"])}
+        if "tuned" in ens:
+            out["ensemble"]["tuned"] = ens["tuned"]
+    srv = line.get("served")
+    if srv:
+        out["served"] = {k: _r(srv[k]) if isinstance(srv[k], float) else srv[k]
+                         for k in ("requests", "p50_latency_s", "p99_latency_s",
+                                   "pair_interactions_per_s", "peak_admitted_frac",
+                                   "peak_concurrent") if k in srv}
+    cpu = line.get("cpu_baseline")
+    if cpu:
+        out["cpu_pairs_per_s"] = _r(cpu["value"])
+    return out
 
 
 def l2_note(resident: int) -> str:

@@ -59,7 +59,9 @@ extern "C" {
 #define SPH_OP_RESET_RHO 10
 #define SPH_OP_RESET_RHO_REF 11
 #define SPH_OP_RESET_A 12     /* a = 0 and xsph = 0                            */
-#define SPH_OP_EOS 13         /* Tait: P = B((rho/rho_ref)^7 - 1)              */
+#define SPH_OP_EOS 13         /* the system's EOS (sph_params.eos), fluid p:
+                                 Tait P = B((rho/rho_ref)^7 - 1), P/rho^2; or
+                                 linear P = c0^2 (rho - rho_ref), P/rho0^2     */
 #define SPH_OP_KICK 14        /* v += dt/2 (a + g)  (fluid)                    */
 #define SPH_OP_DRIFT 15       /* x += dt (v + eps xsph)  (fluid)               */
 #define SPH_OP_HYDROSTATIC 16 /* rho_ref /= (1 + rho0 g (H_col - y) / B)^(1/7) */
@@ -99,8 +101,17 @@ typedef struct sph_params {
   double dt;
   double col_height;     /* free-surface height for SPH_OP_HYDROSTATIC           */
   int32_t vertical_axis; /* 0-based axis along gravity                           */
-  int32_t reserved;
+  int32_t eos;           /* SPH_EOS_TAIT (0) or SPH_EOS_LINEAR (1), below         */
 } sph_params;
+
+/* Equation of state of SPH_OP_EOS and of the step's fused EOS, and the
+ * pressure term P/rho^2 the force pass uses:
+ *   SPH_EOS_TAIT    P = B((rho/rho_ref)^7 - 1), B = c0^2 rho0 / 7; P/rho^2
+ *                   (the weakly compressible dam-break scheme)
+ *   SPH_EOS_LINEAR  P = c0^2 (rho - rho_ref); P/rho0^2 -- find_pressure! and
+ *                   internal_force! of tests/test_collision_2d.jl:71-78 */
+#define SPH_EOS_TAIT 0
+#define SPH_EOS_LINEAR 1
 
 typedef struct sph_system sph_system;
 
@@ -184,6 +195,15 @@ int sph_stream(sph_system* sys, void** stream);
  * descending neighbour index), as (p, q) reference indices.  Writes up to cap
  * pairs and the total count to *count. */
 int sph_debug_pairs(sph_system* sys, int64_t* pairs, int64_t cap, int64_t* count);
+/* The ordered pairs (p, q) the last density pass (SPH_OP_DENSITY or
+ * SPH_OP_DENSITY_REF) acted on, read back from what that pass stored for the
+ * force pass of the same cells -- the FP64 path's rows or the mixed path's
+ * hit masks -- as reference indices, fluid targets only, each target's
+ * neighbours in the reference's traversal order (targets ascending).  The
+ * mixed path's pair set is checked through this against the oracle.
+ * SPH_ERR_STATE when no density pass ran since the last binning or a
+ * target's hits were not stored (an overflow sent it to the traversal). */
+int sph_debug_hits(sph_system* sys, int64_t* pairs, int64_t cap, int64_t* count);
 /* Per-kernel timing with CUDA events on the handle's stream, enabled by
  * sph_set_profiling(sys, 1).  kernel ids are SPH_KERNEL_*. */
 #define SPH_KERNEL_BIN_KEYS 0
@@ -336,10 +356,14 @@ int sph_batch_stream(sph_batch* batch, void** stream);
  * static device array of about 21 MB that every GPU which loads the library
  * holds until the process exits; every call shares it, so calls that overlap
  * on the GPU (different streams, or concurrent host threads) race.  The first
- * call on a device looks up the array's device address (cudaGetSymbolAddress)
- * with that device current; make that first call before any stream capture.
+ * call in a CUDA context looks up the array's device address
+ * (cudaGetSymbolAddress) with that context current and caches it under the
+ * context's id; make that first call before any stream capture.  A context
+ * destroyed and created again (cudaDeviceReset) is a new context: its first
+ * call looks the address up again, so it too must come before any capture.
  *
- * Inputs: params (h and domain_min/max are used), n particles, d_x = device
+ * Inputs: params (dim, h and domain_min/max are used; the same checks as
+ * sph_create), n particles, d_x = device
  * array of n x 3 doubles.  Outputs (device memory owned by the caller):
  * d_cell_start[key_max + 2] and d_order[n].  Cell k (1-based key as in
  * find_key) holds d_order[d_cell_start[k] .. d_cell_start[k+1]), particle

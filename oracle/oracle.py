@@ -32,7 +32,7 @@ class orc_params(C.Structure):
         ("h_smooth", C.c_double), ("alpha", C.c_double), ("eps_xsph", C.c_double),
         ("gravity", C.c_double * 3), ("dt", C.c_double), ("col_height", C.c_double),
         ("vertical_axis", C.c_int32),
-        ("reserved", C.c_int32),
+        ("eos", C.c_int32),
     ]
 
 
@@ -124,9 +124,11 @@ class OracleSystem:
         for name in ("mass", "rho0", "c0", "h_smooth", "alpha", "eps_xsph", "dt", "col_height"):
             setattr(p, name, float(params[name]))
         p.vertical_axis = int(params["vertical_axis"])
+        p.eos = int(params.get("eos", 0))
         self._h = self._lib.orc_create(C.byref(p))
         if not self._h:
-            raise ValueError("invalid ParticleSystem declaration (h must be positive)")
+            raise ValueError("invalid ParticleSystem declaration (h must be positive, "
+                             "eos 0 or 1)")
         self.params = dict(params)
 
     def close(self):

@@ -37,6 +37,7 @@ struct orc_system {
   /* derived constants, computed once */
   double inv_h, cw, cr, B, hdt, eta2, alpha_c0, gmag;
   double mcw, mcr, ca; /* m C_w, m C_r, -(alpha c0) h_smooth */
+  double c2, rho0sq;   /* c0^2, rho0^2 (ORC_EOS_LINEAR) */
   /* particles in the reference's order (0-based index = position in
    * sys.particles minus one) */
   int64_t n, cap;
@@ -81,6 +82,7 @@ static inline double ker_r(const double d[3]) {
 /* structs.jl:57-92 */
 orc_system* orc_create(const orc_params* p) {
   if (!(p->h > 0.0)) return NULL; /* structs.jl:59 */
+  if (p->eos != ORC_EOS_TAIT && p->eos != ORC_EOS_LINEAR) return NULL;
   orc_system* s = (orc_system*)calloc(1, sizeof(orc_system));
   s->p = *p;
   s->kdim = p->dim;
@@ -110,6 +112,8 @@ orc_system* orc_create(const orc_params* p) {
     s->cr = -66.84507609859604 / ((h2 * h2) * H);
   }
   s->B = ((p->c0 * p->c0) * p->rho0) / 7.0;
+  s->c2 = p->c0 * p->c0;          /* test_collision_2d.jl:72 c^2 */
+  s->rho0sq = p->rho0 * p->rho0;  /* test_collision_2d.jl:77 rho0^2 */
   s->hdt = 0.5 * p->dt;
   s->eta2 = 0.01 * (p->h_smooth * p->h_smooth);
   s->alpha_c0 = p->alpha * p->c0;
@@ -214,7 +218,9 @@ void orc_set_state(orc_system* s, const double* x, const double* v, const double
     if (rho_ref) s->rho_ref[i] = rho_ref[i];
     if (P) {
       s->P[i] = P[i];
-      s->Pr[i] = s->type[i] == ORC_FLUID ? P[i] / (s->rho[i] * s->rho[i]) : 0.0;
+      s->Pr[i] = s->type[i] != ORC_FLUID      ? 0.0
+                 : s->p.eos == ORC_EOS_LINEAR ? P[i] / s->rho0sq
+                                              : P[i] / (s->rho[i] * s->rho[i]);
     }
   }
   if (x) s->cells_valid = 0;
@@ -447,7 +453,12 @@ void orc_apply_unary(orc_system* s, int op) {
         for (int d = 0; d < 3; ++d) { s->a[i][d] = 0.0; s->xs[i][d] = 0.0; }
         break;
       case ORC_OP_EOS:
-        if (fluid) {
+        if (fluid && P->eos == ORC_EOS_LINEAR) {
+          /* test_collision_2d.jl:71-73 find_pressure!: P = c^2 (rho - rho0);
+           * :77 uses P / rho0^2 */
+          s->P[i] = s->c2 * (s->rho[i] - s->rho_ref[i]);
+          s->Pr[i] = s->P[i] / s->rho0sq;
+        } else if (fluid) {
           const double ratio = s->rho[i] / s->rho_ref[i];
           const double r2 = ratio * ratio;
           const double r4 = r2 * r2;

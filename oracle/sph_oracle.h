@@ -19,6 +19,8 @@
  *   src/kernels.jl:108-195 wendland2/rDwendland2/wendland3/rDwendland3
  *   examples/collapse_symplectic.jl:98-143,170-191  operator templates and the
  *                          kick-drift-kick step order
+ *   tests/test_collision_2d.jl:63-116  the linear EOS and the P/rho0^2
+ *                          pressure force (ORC_EOS_LINEAR), the same step
  *
  * The reference has no Tait EOS, artificial viscosity, XSPH or wall-pressure
  * operator; those are written from the published formulas (Tait/Monaghan
@@ -59,7 +61,7 @@ enum {
   ORC_OP_RESET_RHO = 10,
   ORC_OP_RESET_RHO_REF = 11,
   ORC_OP_RESET_A = 12,    /* a = 0, xsph = 0                                */
-  ORC_OP_EOS = 13,        /* Tait: P, P/rho^2                               */
+  ORC_OP_EOS = 13,        /* P and the force's P/rho^2 (orc_params.eos)      */
   ORC_OP_KICK = 14,       /* v += dt/2 (a + g)                              */
   ORC_OP_DRIFT = 15,      /* x += dt (v + eps xsph)                         */
   ORC_OP_HYDROSTATIC = 16 /* rho_ref /= (1 + rho0 g (H_col - y)/B)^(1/7)   */
@@ -88,8 +90,15 @@ typedef struct orc_params {
   double dt;
   double col_height;     /* free-surface height for hydrostatic init        */
   int32_t vertical_axis; /* 0-based axis of gravity                         */
-  int32_t reserved;
+  int32_t eos;           /* ORC_EOS_TAIT or ORC_EOS_LINEAR                  */
 } orc_params;
+
+/* equation of state (orc_params.eos) and the force's pressure term */
+enum {
+  ORC_EOS_TAIT = 0,  /* P = B((rho/rho_ref)^7 - 1), B = c0^2 rho0 / 7; P/rho^2 */
+  ORC_EOS_LINEAR = 1 /* P = c0^2 (rho - rho_ref); P/rho0^2 -- find_pressure!
+                        and internal_force! of tests/test_collision_2d.jl:71-78 */
+};
 
 typedef struct orc_system orc_system;
 

@@ -197,7 +197,10 @@ size_t carve(sph_system* s, char* base, size_t C) {
     b.ck_cap = 0;
     b.ck_mask = nullptr;
   }
-  s->staging = take(72 * C + 64);
+  // host-transfer staging: 72 bytes per particle (x, v, rho, rho_ref,
+  // type of an upload); the debug listings put 4 + 8 bytes per particle at a
+  // 256-byte boundary, which the 512 bytes of slack cover for any C
+  s->staging = take(72 * C + 512);
   return off;
 }
 
@@ -257,8 +260,10 @@ int pair_pass(sph_system* s, int op, int self, int reset, int fuse_eos) {
   // force pass of the same binning; an FP64 force pass turns the rows' m W
   // into its own factors (a traversing pass only writes the rows of targets
   // that have none: passes without valid rows, overflowed rows)
-  if (op == SPH_OP_DENSITY || op == SPH_OP_DENSITY_REF)
+  if (op == SPH_OP_DENSITY || op == SPH_OP_DENSITY_REF) {
     s->lists_valid = true;
+    s->hits_valid = true;
+  }
   else if (op == SPH_OP_FORCE && s->params.precision != SPH_PREC_MIXED)
     s->lists_valid = false;
   return SPH_OK;
@@ -272,6 +277,7 @@ int binning(sph_system* s, int step_mode, int gather_mode) {
   s->cells_valid = true;
   s->aux_fluid = s->aux_wall = false;
   s->lists_valid = false;
+  s->hits_valid = false;
   return SPH_OK;
 }
 
@@ -281,6 +287,7 @@ int unary(sph_system* s, int op) {
   if (op == SPH_OP_DRIFT) {
     s->cells_valid = false;
     s->lists_valid = false;
+    s->hits_valid = false;
   }
   s->aux_fluid = s->aux_wall = false;
   return SPH_OK;
@@ -321,6 +328,7 @@ static int setup_host(const sph_params* p, sph_system* s) {
   for (int d = 0; d < 3; ++d)
     if (!(p->domain_min[d] <= p->domain_max[d])) return SPH_ERR_ARG;
   if (p->dim == 2 && (p->domain_min[2] > 0.0 || p->domain_max[2] < 0.0)) return SPH_ERR_ARG;
+  if (p->eos != SPH_EOS_TAIT && p->eos != SPH_EOS_LINEAR) return SPH_ERR_ARG;
   s->params = *p;
   // structs.jl:64-82
   const double H = p->h;
@@ -361,6 +369,9 @@ static int setup_host(const sph_params* p, sph_system* s) {
   k.mass = p->mass;
   k.rho0 = p->rho0;
   k.B = ((p->c0 * p->c0) * p->rho0) / 7.0;
+  k.eos = p->eos;
+  k.c2 = p->c0 * p->c0;
+  k.rho0sq = p->rho0 * p->rho0;
   k.hdt = 0.5 * p->dt;
   k.dt = p->dt;
   k.eta2 = 0.01 * (p->h_smooth * p->h_smooth);
@@ -469,6 +480,7 @@ int sph_create(const sph_params* p, int device, sph_system** out) {
   s->b.d_npairs = (unsigned long long*)(c + 1280);
   s->b.d_pover = (int*)(c + 1288);
   s->b.d_rover = (int*)(c + 1292);
+  s->d_debug = (int*)(c + 1536);
   if (cudaMemsetAsync(cells, 0, bytes, s->stream) != cudaSuccess ||
       cudaStreamSynchronize(s->stream) != cudaSuccess) {
     cudaGetLastError();
@@ -556,6 +568,7 @@ int sph_upload(sph_system* s, int64_t n, const double* x, const double* v, const
   s->cells_valid = false;
   s->aux_fluid = s->aux_wall = false;
   s->lists_valid = false;
+  s->hits_valid = false;
   return SPH_OK;
 }
 
@@ -683,6 +696,7 @@ int sph_generate(sph_system* s, const sph_shape* shapes, int count, int64_t* n_o
   s->cells_valid = false;
   s->aux_fluid = s->aux_wall = false;
   s->lists_valid = false;
+  s->hits_valid = false;
   if (n_out) *n_out = total;
   return SPH_OK;
 }
@@ -738,7 +752,7 @@ int sph_set_field(sph_system* s, int field, const void* in) {
   if (e != cudaSuccess) return fail(s, SPH_ERR_CUDA, "field: %s", cudaGetErrorString(e));
   CK(cudaStreamSynchronize(s->stream));
   if (field == SPH_FIELD_X) s->cells_valid = false;
-  if (field == SPH_FIELD_X || field == SPH_FIELD_TYPE) s->lists_valid = false;
+  if (field == SPH_FIELD_X || field == SPH_FIELD_TYPE) s->lists_valid = s->hits_valid = false;
   s->aux_fluid = s->aux_wall = false;
   return SPH_OK;
 }
@@ -973,6 +987,55 @@ int sph_debug_pairs(sph_system* s, int64_t* pairs, int64_t cap, int64_t* count) 
   return SPH_OK;
 }
 
+int sph_debug_hits(sph_system* s, int64_t* pairs, int64_t cap, int64_t* count) {
+  if (!s || !count || cap < 0 || (cap > 0 && !pairs)) return SPH_ERR_ARG;
+  if (!s->cells_valid || !s->hits_valid)
+    return fail(s, SPH_ERR_STATE, "no density pass since the last create_cell_list!");
+  DeviceGuard guard(s->device);
+  int n = 0;
+  int rc = read_count(s, &n);
+  if (rc) return rc;
+  *count = 0;
+  if (n == 0) return SPH_OK;
+  const int mixed = s->params.precision == SPH_PREC_MIXED ? 1 : 0;
+  int* dcounts = (int*)s->staging;
+  long long* doff = (long long*)((char*)s->staging + align_up(4 * (size_t)n));
+  CK(cudaMemsetAsync(s->d_debug, 0, sizeof(int), s->stream));
+  cudaError_t e = launch_debug_hits(ctx(s), s->cur, s->geo, s->b, s->n_host, mixed, 0, dcounts,
+                                    nullptr, nullptr, 0, s->d_debug);
+  if (e != cudaSuccess) return fail(s, SPH_ERR_CUDA, "hits: %s", cudaGetErrorString(e));
+  std::vector<int> hc(n);
+  std::vector<long long> ho(n);
+  int bad = 0;
+  CK(cudaMemcpyAsync(hc.data(), dcounts, 4 * (size_t)n, cudaMemcpyDeviceToHost, s->stream));
+  CK(cudaMemcpyAsync(&bad, s->d_debug, sizeof(int), cudaMemcpyDeviceToHost, s->stream));
+  CK(cudaStreamSynchronize(s->stream));
+  if (bad)
+    return fail(s, SPH_ERR_STATE, "some targets' hits were not stored (overflow bits 0x%x)", bad);
+  long long total = 0;
+  for (int i = 0; i < n; ++i) {
+    ho[i] = total;
+    total += hc[i];
+  }
+  *count = total;
+  if (cap == 0) return SPH_OK;
+  CK(cudaMemcpyAsync(doff, ho.data(), 8 * (size_t)n, cudaMemcpyHostToDevice, s->stream));
+  const long long m = total < cap ? total : cap;
+  long long* dpairs = nullptr;
+  if (cudaMalloc(&dpairs, 16 * (size_t)(m > 0 ? m : 1)) != cudaSuccess) {
+    cudaGetLastError();
+    return fail(s, SPH_ERR_NOMEM, "cannot allocate the pair list");
+  }
+  e = launch_debug_hits(ctx(s), s->cur, s->geo, s->b, s->n_host, mixed, 1, dcounts, doff, dpairs,
+                        m, s->d_debug);
+  cudaError_t e2 = cudaMemcpyAsync(pairs, dpairs, 16 * (size_t)m, cudaMemcpyDeviceToHost, s->stream);
+  cudaError_t e3 = cudaStreamSynchronize(s->stream);
+  cudaFree(dpairs);
+  if (e != cudaSuccess || e2 != cudaSuccess || e3 != cudaSuccess)
+    return fail(s, SPH_ERR_CUDA, "pair list transfer failed");
+  return SPH_OK;
+}
+
 int sph_set_profiling(sph_system* s, int on) {
   if (!s) return SPH_ERR_ARG;
   s->profiling = on != 0;
@@ -1164,6 +1227,7 @@ static int batch_capture_fused(sph_batch* b) {
     m->cells_valid = true;
     m->aux_fluid = m->aux_wall = true;
     m->lists_valid = true;
+    m->hits_valid = true;
     b->generations[j] = m->generation;
     b->cur0[j] = m->cur.x[0];
   }

@@ -78,6 +78,9 @@ struct Consts {
   // FP32 copies for the mixed-precision pair arithmetic
   float inv_hf, cwf, crf, massf, eta2f, alpha_c0f, h_smoothf, rho0f;
   float gf[3];
+  // equation of state (SPH_EOS_*) and the linear one's constants c0^2, rho0^2
+  int eos;
+  double c2, rho0sq;
 };
 
 // One entry of an FP64 target's row (32 bytes, one DRAM sector, written
@@ -220,7 +223,14 @@ __device__ __forceinline__ bool lt0(double v) {
 // Q comes from an FP32 seed (rsqrt / rcp approximations) and two Newton
 // corrections in 128-bit integers, is adjusted to the exact floor (one step
 // at most; the floor condition is then verified exactly) and rounded to
-// nearest with the exact remainder (even on a tie).
+// nearest with the exact remainder (even on a tie).  The method is the
+// textbook one: Newton-Raphson iteration for the reciprocal and the
+// reciprocal square root (Markstein, IBM J. Res. Dev. 34(1), 1990), carried
+// out in integer arithmetic, followed by correct rounding decided from the
+// exact remainder N - Q^2 or 2^105 - Q M (Muller et al., Handbook of
+// Floating-Point Arithmetic, 2nd ed. 2018, the chapters on division and
+// square root by iteration).  No library routine's constants or steps are
+// reproduced; tests compare every result with the IEEE operation.
 static __device__ __noinline__ double isqrt_fallback(double s) { return sqrt(s); }
 static __device__ __noinline__ double ircp_fallback(double y) { return __drcp_rn(y); }
 
@@ -328,6 +338,25 @@ __device__ __forceinline__ double ker_w(const Consts& k, double r) {
 __device__ __forceinline__ double ker_rdw(const Consts& k, double r) {
   const double t = ker_t(k, r);
   return k.cr * ((t * t) * t);
+}
+
+// The equation of state of a fluid particle and the pressure term of the
+// force, P/rho^2 (Tait, the dam-break scheme; B = c0^2 rho0 / 7, ^7 as a
+// product chain) or P/rho0^2 (the linear P = c^2 (rho - rho0) of
+// tests/test_collision_2d.jl:71-78), in the oracle's evaluation order.
+__device__ __forceinline__ void eos_eval(const Consts& k, double rho, double rho_ref, double& P,
+                                         double& Pr) {
+  if (k.eos == 1) {
+    P = k.c2 * (rho - rho_ref);
+    Pr = P / k.rho0sq;
+  } else {
+    const double ratio = rho / rho_ref;
+    const double r2 = ratio * ratio;
+    const double r4 = r2 * r2;
+    const double r7 = (r4 * r2) * ratio;
+    P = k.B * (r7 - 1.0);
+    Pr = P / (rho * rho);
+  }
 }
 
 // structs.jl:97-106 for an arbitrary point: -1 when a coordinate is NaN,

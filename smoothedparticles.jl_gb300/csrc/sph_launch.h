@@ -133,6 +133,14 @@ cudaError_t launch_debug_pairs(const LaunchCtx& c, const State& s, const Geometr
                                int* counts, const long long* offsets, long long* pairs,
                                long long cap_pairs);
 
+// The pairs the last density pass stored (FP64 rows or mixed hit masks) in
+// the reference order: pass 0 counts per reference index, pass 1 writes;
+// *bad (device) gets a bit when some target's hits were not stored.
+cudaError_t launch_debug_hits(const LaunchCtx& c, const State& s, const Geometry& g,
+                              const BinScratch& b, int cap, int mixed, int pass, int* counts,
+                              const long long* offsets, long long* pairs, long long cap_pairs,
+                              int* bad);
+
 // ---- device-side particle generation (sph_lattice.cu)
 struct LatticeShape {
   int kind, type, dim, keep_axis;

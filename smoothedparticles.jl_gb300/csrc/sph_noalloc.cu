@@ -17,6 +17,9 @@
 // order (core.jl:26-41).  Particles outside the domain's bounding box (NaN
 // included) are not binned: they follow in order[cell_start[key_max+1] .. n),
 // also in descending index order, for the caller to remove.
+#include <cuda.h>
+
+#include <cmath>
 #include <mutex>
 
 #include "sph_launch.h"
@@ -121,27 +124,79 @@ __global__ void na_copy_starts(int len, const int* starts, int* out) {
   if (i < len) out[i] = starts[i];
 }
 
-// Device address of the scratch, looked up once per device.
-std::mutex g_mu;
-int* g_addr[64] = {};
+// Device address of the scratch, looked up once per CUDA context.  A context
+// that is destroyed and created again (cudaDeviceReset, CUDA.jl's
+// device_reset!) loads the module again, possibly at another address, so the
+// cache is keyed by the context's process-unique id (cuCtxGetId), not by the
+// device number.  The two driver functions are fetched through the runtime's
+// entry-point query, so the library does not link libcuda directly.
+using CtxGetCurrent = CUresult (*)(CUcontext*);
+using CtxGetId = CUresult (*)(CUcontext, unsigned long long*);
 
-int scratch_on_current_device(int** out) {
-  int dev = 0;
-  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) {
+struct ScratchSlot {
+  unsigned long long ctx_id;
+  int* addr;
+};
+
+std::mutex g_mu;
+CtxGetCurrent g_get_current = nullptr;
+CtxGetId g_get_id = nullptr;
+bool g_driver_ready = false;
+constexpr int kSlots = 64;
+ScratchSlot g_slots[kSlots] = {};
+int g_next_slot = 0;
+
+int driver_functions() {
+  if (g_driver_ready) return SPH_OK;
+  void* f1 = nullptr;
+  void* f2 = nullptr;
+  cudaDriverEntryPointQueryResult q1 = cudaDriverEntryPointSymbolNotFound, q2 = q1;
+  if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &f1, 12000, cudaEnableDefault, &q1) !=
+          cudaSuccess ||
+      cudaGetDriverEntryPointByVersion("cuCtxGetId", &f2, 12000, cudaEnableDefault, &q2) !=
+          cudaSuccess ||
+      q1 != cudaDriverEntryPointSuccess || q2 != cudaDriverEntryPointSuccess || !f1 || !f2) {
     cudaGetLastError();
     return SPH_ERR_CUDA;
   }
+  g_get_current = (CtxGetCurrent)f1;
+  g_get_id = (CtxGetId)f2;
+  g_driver_ready = true;
+  return SPH_OK;
+}
+
+int scratch_on_current_device(int** out) {
   std::lock_guard<std::mutex> lock(g_mu);
-  if (!g_addr[dev]) {
-    void* p = nullptr;
-    const cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
-    if (e != cudaSuccess || !p) {
+  if (driver_functions() != SPH_OK) return SPH_ERR_CUDA;
+  CUcontext ctx = nullptr;
+  if (g_get_current(&ctx) != CUDA_SUCCESS) return SPH_ERR_CUDA;
+  if (!ctx) {
+    // no context current on this thread yet: the runtime's own choice, the
+    // current device's primary context (cudaSetDevice initialises it)
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || cudaSetDevice(dev) != cudaSuccess) {
       cudaGetLastError();
       return SPH_ERR_CUDA;
     }
-    g_addr[dev] = (int*)p;
+    if (g_get_current(&ctx) != CUDA_SUCCESS || !ctx) return SPH_ERR_CUDA;
   }
-  *out = g_addr[dev];
+  unsigned long long id = 0;
+  if (g_get_id(ctx, &id) != CUDA_SUCCESS) return SPH_ERR_CUDA;
+  for (const ScratchSlot& sl : g_slots)
+    if (sl.addr && sl.ctx_id == id) {
+      *out = sl.addr;
+      return SPH_OK;
+    }
+  void* p = nullptr;
+  const cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+  if (e != cudaSuccess || !p) {
+    cudaGetLastError();
+    return SPH_ERR_CUDA;
+  }
+  // contexts beyond kSlots reuse the oldest slot (a lookup again costs little)
+  g_slots[g_next_slot] = ScratchSlot{id, (int*)p};
+  g_next_slot = (g_next_slot + 1) % kSlots;
+  *out = (int*)p;
   return SPH_OK;
 }
 
@@ -153,8 +208,12 @@ using namespace sphgpu;
 extern "C" int sph_cell_list_noalloc(const sph_params* params, int64_t n, const double* d_x,
                                      int32_t* d_cell_start, int32_t* d_order, void* stream) {
   if (!params || n < 0 || (n > 0 && (!d_x || !d_order)) || !d_cell_start) return SPH_ERR_ARG;
+  // the same checks as sph_create (structs.jl:59 asserts h > 0)
+  if (params->dim != 2 && params->dim != 3) return SPH_ERR_ARG;
   if (!(params->h > 0.0)) return SPH_ERR_ARG;
   if (n > kMaxN) return SPH_ERR_BUDGET;  // more particles than the static scratch holds
+  if (params->dim == 2 && (params->domain_min[2] > 0.0 || params->domain_max[2] < 0.0))
+    return SPH_ERR_ARG;  // a 2D domain contains the plane z = 0
   Geo g{};
   g.h = params->h;
   long long key_max = 1;
@@ -162,11 +221,17 @@ extern "C" int sph_cell_list_noalloc(const sph_params* params, int64_t n, const 
     if (!(params->domain_min[d] <= params->domain_max[d])) return SPH_ERR_ARG;
     g.dmin[d] = params->domain_min[d];
     g.dmax[d] = params->domain_max[d];
-    g.key_phase[d] = (long long)std::floor(params->domain_min[d] / g.h);
-    g.key_lim[d] = (long long)std::floor(params->domain_max[d] / g.h) - g.key_phase[d] + 1;
+    // floor(domain / h) must be a representable cell index before any
+    // product is formed: a tiny h against the domain is a table too large
+    const double lo = std::floor(params->domain_min[d] / g.h);
+    const double hi = std::floor(params->domain_max[d] / g.h);
+    if (!(lo >= -4.0e15 && hi <= 4.0e15)) return SPH_ERR_BUDGET;
+    g.key_phase[d] = (long long)lo;
+    g.key_lim[d] = (long long)hi - g.key_phase[d] + 1;
+    if (g.key_lim[d] < 1 || g.key_lim[d] > kMaxCells) return SPH_ERR_BUDGET;
     key_max *= g.key_lim[d];
+    if (key_max > kMaxCells) return SPH_ERR_BUDGET;  // cell table too large
   }
-  if (key_max <= 0 || key_max > kMaxCells) return SPH_ERR_BUDGET;  // cell table too large
   g.key_max = (int)key_max;
   int* base = nullptr;
   int rc = scratch_on_current_device(&base);

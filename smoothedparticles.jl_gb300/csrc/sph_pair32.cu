@@ -172,7 +172,9 @@ struct Acc32 {
       float gd = k.gf[0] * hx + k.gf[1] * hy;
       if (DIM == 3) gd += k.gf[2] * hz;
       const float rq = fabsf(pq.w);
-      const float Pq = vq.w * rq * rq;
+      // P from the record's pressure term (P/rho^2, or P/rho0^2 under the
+      // linear EOS)
+      const float Pq = k.eos == 1 ? vq.w * (k.rho0f * k.rho0f) : vq.w * rq * rq;
       f0 += Pq * w;
       f1 += (rq * gd) * w;
       f2 += w;
@@ -530,12 +532,8 @@ __device__ __forceinline__ void pair32_body(const State& s, const Geometry& g, c
         s.rho[i] = acc;
         double Pr = s.Pr[i];
         if (fuse_eos) {
-          const double ratio = acc / s.rho_ref[i];
-          const double r2 = ratio * ratio;
-          const double r4 = r2 * r2;
-          const double r7 = (r4 * r2) * ratio;
-          const double P = k.B * (r7 - 1.0);
-          Pr = P / (acc * acc);
+          double P;
+          eos_eval(k, acc, s.rho_ref[i], P, Pr);
           s.P[i] = P;
           s.Pr[i] = Pr;
         }

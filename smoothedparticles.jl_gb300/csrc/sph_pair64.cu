@@ -248,13 +248,10 @@ __device__ __forceinline__ void target_epilogue(const State& s, const Consts& k,
     if (OP == SPH_OP_DENSITY) {
       s.rho[i] = acc;
       if (fuse_eos) {
-        const double ratio = acc / s.rho_ref[i];
-        const double r2 = ratio * ratio;
-        const double r4 = r2 * r2;
-        const double r7 = (r4 * r2) * ratio;
-        const double P = k.B * (r7 - 1.0);
+        double P, Pr;
+        eos_eval(k, acc, s.rho_ref[i], P, Pr);
         s.P[i] = P;
-        s.Pr[i] = P / (acc * acc);
+        s.Pr[i] = Pr;
       }
     } else {
       s.rho_ref[i] = acc;
@@ -471,6 +468,79 @@ __global__ void __launch_bounds__(128) debug_pairs_kernel(State s, Geometry g, C
   }
   if (!pass) counts[rid] = cnt;
 }
+// The pairs the last density pass acted on, read back from what it stored
+// for the pass after it: an FP64 fluid target's row (its neighbours' indices
+// in the reference's order) or a mixed-precision target's hit masks, decoded
+// chunk by chunk in the traversal order (key_diff order, 32 candidates per
+// chunk, bit u = candidate u).  Pass 0 counts per reference index, pass 1
+// writes (rid_p, rid_q) at offsets[rid_p].  A fluid target whose hits were not
+// stored (an overflowed row, mask slots beyond the capacity) sets *bad.
+__global__ void __launch_bounds__(128) debug_hits_kernel(State s, Geometry g, BinScratch b,
+                                                         int mixed, int pass, int* counts,
+                                                         const long long* offsets,
+                                                         long long* pairs, long long cap_pairs,
+                                                         int* bad) {
+  const int n = *b.d_n;
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const int rid = s.rid[i];
+  long long pos = pass ? offsets[rid] : 0;
+  int cnt = 0;
+  if (s.type[i] == kFluid) {
+    if (!mixed) {
+      const int hc = b.hit_count[i];
+      if (hc > b.hit_cap || *b.d_pover != 0) {
+        atomicOr(bad, 1);
+      } else {
+        const RowEntry* row = b.rows + (size_t)i * b.hit_cap;
+        for (int j = 0; j < hc; ++j, ++pos, ++cnt)
+          if (pass && pos < cap_pairs) {
+            pairs[2 * pos] = rid;
+            pairs[2 * pos + 1] = s.rid[(int)(row[j].q & 0x7fffffffu)];
+          }
+      }
+    } else {
+      // the target's work item and lane, and the item's mask slots (the
+      // binning counted them per cell: items of a cell x chunks per item)
+      const int key = s.cell[i];
+      const int local = i - b.cell_start[key];
+      const int i0 = b.item_off[key], ni = b.item_off[key + 1] - i0;
+      const int item = i0 + (local >> 5), lane = local & 31;
+      const int co = b.chunk_off[key];
+      const int nc = ni > 0 ? (b.chunk_off[key + 1] - co) / ni : 0;
+      const long long start = (long long)co + (long long)(item - i0) * nc;
+      if (start + nc > (long long)b.ck_cap) {
+        atomicOr(bad, 2);
+      } else {
+        int gi = 0;
+        for (int c = 0; c < g.n_diff; ++c) {
+          const int nk = key + g.key_diff[c];
+          if (nk < 1 || nk > g.key_max) continue;  // core.jl:98
+          const int en = b.cell_start[nk + 1];
+          for (int base = b.cell_start[nk]; base < en; base += 32, ++gi) {
+            if (gi >= nc) {
+              atomicOr(bad, 4);
+              break;
+            }
+            unsigned mask = b.ck_mask[((size_t)start + gi) * 32 + lane];
+            while (mask) {
+              const int u = __ffs(mask) - 1;
+              mask &= mask - 1u;
+              if (pass && pos < cap_pairs) {
+                pairs[2 * pos] = rid;
+                pairs[2 * pos + 1] = s.rid[base + u];
+              }
+              ++pos;
+              ++cnt;
+            }
+          }
+        }
+      }
+    }
+  }
+  if (!pass) counts[rid] = cnt;
+}
+
 // pair64_kernel with one warp per work item (the block scheduler balances
 // the uneven items), or, for the sweep over overflowed rows (list_mode 3,
 // usually nothing to do), one resident wave of blocks striding over them
@@ -570,6 +640,18 @@ cudaError_t launch_sum(const LaunchCtx& c, const State& s, const Geometry& g, co
     sum_kernel<2><<<blocks, 128, 0, c.stream>>>(s, g, k, b, func, nq, x, rid_query, out);
   else
     sum_kernel<3><<<blocks, 128, 0, c.stream>>>(s, g, k, b, func, nq, x, rid_query, out);
+  mark(c, SPH_KERNEL_SUM, 1);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_debug_hits(const LaunchCtx& c, const State& s, const Geometry& g,
+                              const BinScratch& b, int cap, int mixed, int pass, int* counts,
+                              const long long* offsets, long long* pairs, long long cap_pairs,
+                              int* bad) {
+  if (cap <= 0) return cudaSuccess;
+  mark(c, SPH_KERNEL_SUM, 0);
+  debug_hits_kernel<<<(cap + 127) / 128, 128, 0, c.stream>>>(s, g, b, mixed, pass, counts, offsets,
+                                                              pairs, cap_pairs, bad);
   mark(c, SPH_KERNEL_SUM, 1);
   return cudaGetLastError();
 }

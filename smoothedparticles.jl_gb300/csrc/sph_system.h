@@ -35,6 +35,10 @@ struct sph_system {
   bool aux_fluid = false;
   bool aux_wall = false;
   bool lists_valid = false;  // hit lists of the last density pass match cells and positions
+  // the neighbour indices the last density pass stored (FP64 rows, mixed hit
+  // masks) belong to the current cells: sph_debug_hits may read them
+  bool hits_valid = false;
+  int* d_debug = nullptr;    // a device word of the debug listings (in the cell tables)
   std::string err;
   // launch accounting and optional per-kernel CUDA-event timing
   bool profiling = false;

@@ -34,16 +34,12 @@ __device__ __forceinline__ void unary_body(const State& s, const Consts& k, cons
         s.xs[d][i] = 0.0;
       }
       break;
-    case SPH_OP_EOS:  // Tait equation of state, ^7 as a product chain
+    case SPH_OP_EOS:  // the system's equation of state (eos_eval)
       if (fluid) {
-        const double rho = s.rho[i];
-        const double ratio = rho / s.rho_ref[i];
-        const double r2 = ratio * ratio;
-        const double r4 = r2 * r2;
-        const double r7 = (r4 * r2) * ratio;
-        const double P = k.B * (r7 - 1.0);
+        double P, Pr;
+        eos_eval(k, s.rho[i], s.rho_ref[i], P, Pr);
         s.P[i] = P;
-        s.Pr[i] = P / (rho * rho);
+        s.Pr[i] = Pr;
       } else {
         s.P[i] = 0.0;
         s.Pr[i] = 0.0;
@@ -131,7 +127,8 @@ __global__ void __launch_bounds__(kThreads) upload_kernel(State s, BinScratch b,
 // dir 0: state (cell order) -> staging (reference order); dir 1: the reverse.
 template <int DIM>
 __global__ void __launch_bounds__(kThreads) field_kernel(State s, BinScratch b, int field,
-                                                         int dir, void* staging) {
+                                                         int dir, void* staging, int eos,
+                                                         double rho0sq) {
   const int n = *b.d_n;
   const int i = blockIdx.x * kThreads + threadIdx.x;
   if (i >= n) return;
@@ -164,7 +161,9 @@ __global__ void __launch_bounds__(kThreads) field_kernel(State s, BinScratch b, 
     } else {
       sc[i] = st[r];
       if (field == SPH_FIELD_P)
-        s.Pr[i] = s.type[i] == kFluid ? st[r] / (s.rho[i] * s.rho[i]) : 0.0;
+        s.Pr[i] = s.type[i] != kFluid ? 0.0
+                  : eos == 1         ? st[r] / rho0sq
+                                     : st[r] / (s.rho[i] * s.rho[i]);
     }
   } else if (field == SPH_FIELD_TYPE) {
     int* st = (int*)staging;
@@ -226,9 +225,9 @@ cudaError_t launch_field(const LaunchCtx& c, const State& s, const Consts& k,
   const int blocks = (cap + kThreads - 1) / kThreads;
   mark(c, SPH_KERNEL_IO, 0);
   if (k.dim == 2)
-    field_kernel<2><<<blocks, kThreads, 0, c.stream>>>(s, b, field, dir, staging);
+    field_kernel<2><<<blocks, kThreads, 0, c.stream>>>(s, b, field, dir, staging, k.eos, k.rho0sq);
   else
-    field_kernel<3><<<blocks, kThreads, 0, c.stream>>>(s, b, field, dir, staging);
+    field_kernel<3><<<blocks, kThreads, 0, c.stream>>>(s, b, field, dir, staging, k.eos, k.rho0sq);
   mark(c, SPH_KERNEL_IO, 1);
   return cudaGetLastError();
 }

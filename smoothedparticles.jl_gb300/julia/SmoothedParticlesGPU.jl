@@ -42,7 +42,7 @@ struct SphParams
     dt::Float64
     col_height::Float64
     vertical_axis::Int32
-    reserved::Int32
+    eos::Int32           # 0: Tait (P/rho^2 in the force), 1: linear c0^2 (rho - rho0) (P/rho0^2)
 end
 
 abstract type BuiltinOperator end
@@ -53,7 +53,7 @@ struct WallPressure <: BuiltinOperator end        # SPH_OP_WALL_PRESSURE
 struct ResetRho <: BuiltinOperator end            # reset_rho!     -> SPH_OP_RESET_RHO
 struct ResetRho0 <: BuiltinOperator end
 struct ResetA <: BuiltinOperator end              # reset_a!
-struct FindPressure <: BuiltinOperator end        # find_pressure! -> SPH_OP_EOS (Tait)
+struct FindPressure <: BuiltinOperator end        # find_pressure! -> SPH_OP_EOS (the params' eos)
 struct Accelerate <: BuiltinOperator end          # accelerate!    -> SPH_OP_KICK
 struct Move <: BuiltinOperator end                # move!          -> SPH_OP_DRIFT
 struct Hydrostatic <: BuiltinOperator end
@@ -166,8 +166,12 @@ apply_unary!(sys::GPUParticleSystem, op::BuiltinOperator) =
     check(sys, ccall((:sph_apply_unary, libsphgpu), Cint, (Ptr{Cvoid}, Cint),
                      sys.handle, opcode(op)))
 
-"sum(sys, func, x) at the columns of a 3 x m matrix; func: 1 density, 2 kernel, 3 pressure, 4 Shepard."
+"""sum(sys, func, x) at the columns of a 3 x m matrix (2D points as well: z = 0);
+func: 1 density, 2 kernel, 3 pressure, 4 Shepard."""
 function SmoothedParticles.sum(sys::GPUParticleSystem, func::Integer, x::Matrix{Float64})
+    # the library reads m points of 3 doubles each
+    size(x, 1) == 3 || throw(DimensionMismatch(
+        "query points must be a 3 x m matrix (got $(size(x, 1)) x $(size(x, 2)))"))
     out = Vector{Float64}(undef, size(x, 2))
     check(sys, ccall((:sph_sum_point, libsphgpu), Cint,
                      (Ptr{Cvoid}, Cint, Int64, Ptr{Float64}, Ptr{Float64}),

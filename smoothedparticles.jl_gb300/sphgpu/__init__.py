@@ -62,6 +62,15 @@ reset_a = Operator("reset_a!", L.SPH_OP_RESET_A, False)
 accelerate = Operator("accelerate!", L.SPH_OP_KICK, False)
 move = Operator("move!", L.SPH_OP_DRIFT, False)
 hydrostatic = Operator("hydrostatic!", L.SPH_OP_HYDROSTATIC, False)
+_BY_ID = {o.op: o for o in (find_rho, find_rho0, internal_force, wall_pressure, find_pressure,
+                            reset_rho, reset_rho0, reset_a, accelerate, move, hydrostatic)}
+
+
+def op_by_id(op: int) -> Operator:
+    """The built-in operator with the C ABI's id ``op`` (SPH_OP_*)."""
+    return _BY_ID[int(op)]
+
+
 # functions for sum()
 DENSITY = SumFunction("density", L.SPH_SUM_DENSITY)
 KERNEL = SumFunction("kernel", L.SPH_SUM_KERNEL)
@@ -244,6 +253,16 @@ class ParticleSystem:
         out = np.empty((cnt.value, 2), np.int64)
         if cnt.value:
             self._check(self._lib.sph_debug_pairs(self._h, _ptr(out), cnt.value, C.byref(cnt)))
+        return out
+
+    def debug_hits(self) -> np.ndarray:
+        """The (p, q) pairs the last density pass stored for the force pass
+        (FP64 rows or mixed hit masks), fluid targets, reference order."""
+        cnt = C.c_int64()
+        self._check(self._lib.sph_debug_hits(self._h, None, 0, C.byref(cnt)))
+        out = np.empty((cnt.value, 2), np.int64)
+        if cnt.value:
+            self._check(self._lib.sph_debug_hits(self._h, _ptr(out), cnt.value, C.byref(cnt)))
         return out
 
     def set_profiling(self, on: bool = True):

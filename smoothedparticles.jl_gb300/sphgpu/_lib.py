@@ -79,9 +79,12 @@ class sph_params(C.Structure):
         ("dt", C.c_double),
         ("col_height", C.c_double),
         ("vertical_axis", C.c_int32),
-        ("reserved", C.c_int32),
+        ("eos", C.c_int32),
     ]
 
+
+SPH_EOS_TAIT = 0
+SPH_EOS_LINEAR = 1
 
 SPH_MAT_KERNEL = 1
 SPH_MAT_PROJECTION = 2
@@ -136,7 +139,7 @@ def make_params(cls, p: dict, precision: int = 0):
     for name in ("mass", "rho0", "c0", "h_smooth", "alpha", "eps_xsph", "dt", "col_height"):
         setattr(s, name, float(p[name]))
     s.vertical_axis = int(p["vertical_axis"])
-    s.reserved = 0
+    s.eos = int(p.get("eos", SPH_EOS_TAIT))
     return s
 
 
@@ -168,6 +171,7 @@ PROTOTYPES = {
     "sph_synchronize": (C.c_int, [_P]),
     "sph_stream": (C.c_int, [_P, C.POINTER(_P)]),
     "sph_debug_pairs": (C.c_int, [_P, _P, _I64, C.POINTER(_I64)]),
+    "sph_debug_hits": (C.c_int, [_P, _P, _I64, C.POINTER(_I64)]),
     "sph_set_profiling": (C.c_int, [_P, C.c_int]),
     "sph_kernel_stats": (C.c_int, [_P, C.c_int, C.POINTER(C.c_double), C.POINTER(_I64)]),
     "sph_reset_kernel_stats": (C.c_int, [_P]),

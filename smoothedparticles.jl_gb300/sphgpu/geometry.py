@@ -262,7 +262,9 @@ def collision_2d(dr: float = 0.02, c0: float = 20.0) -> Case:
     Circles of radius 0.4 centred at (-0.5, -0.1) and (0.5, 0.1) moving at
     +1 and -1 m/s along x, domain [-10, 10]^2, kernel support ``2.4*dr``
     (the test uses h as the support), no walls, no gravity, no viscosity and
-    no XSPH, so the scheme is conservative.
+    no XSPH.  The equation of state is the test's linear one,
+    P = c^2 (rho - rho0) with P/rho0^2 in the pressure force
+    (test_collision_2d.jl:71-78), c = 20.
     """
     H = 2.4 * dr
     x1 = circle(2, dr, -0.5 * 1.0, -0.5 * 0.2, 0.4)
@@ -276,5 +278,5 @@ def collision_2d(dr: float = 0.02, c0: float = 20.0) -> Case:
     params = dict(dim=2, h=H, domain_min=[-10.0, -10.0, 0.0], domain_max=[10.0, 10.0, 0.0],
                   mass=rho0 * (dr * dr), rho0=rho0, c0=c0, h_smooth=0.5 * H, alpha=0.0,
                   eps_xsph=0.0, gravity=[0.0, 0.0, 0.0], dt=(0.1 * H) / c0, col_height=0.0,
-                  vertical_axis=1)
+                  vertical_axis=1, eos=1)
     return Case("collision_2d", 2, dr, x, typ, v, params)

@@ -33,3 +33,20 @@ def test_reference_arm_line():
 
 def test_reference_arm_other_ranks_silent():
     assert _run({"RANK": "1", "WORLD_SIZE": "2"}) == []
+
+
+def test_pair_once_flops_below_per_hit_count():
+    """The FP64 count is per unordered pair plus per-target accumulation, so
+    one fluid-fluid pair (two directed hits) costs less than two mixed hits,
+    each of which is evaluated in full."""
+    sys.path.insert(0, ROOT)
+    import bench
+    cats = dict(density=200, wall=10, force_fluid=180, force_wall=10, force_av=60)
+    for dim in (2, 3):
+        f64 = bench.pass_flops(cats, dim, False)
+        f32 = bench.pass_flops(cats, dim, True)
+        assert 0 < f64["force"] < f32["force"]
+        assert 0 < f64["density"] < f32["density"]
+        F = bench.FP64_FLOPS[dim]
+        assert f64["force"] == (90 * F["ff_pair"] + 30 * F["av_pair"] + 10 * F["fw_pair"]
+                                + 180 * (F["acc_a"] + F["acc_x"]) + 10 * F["acc_a"])

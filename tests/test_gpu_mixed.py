@@ -2,7 +2,7 @@
 
 The mixed path classifies candidates exactly like the FP64 path, so its pair
 set (and pair counts per category) must be identical for the same positions.
-Its arithmetic is FP32 with FP64 accumulation per batch of <= 16 hits, so the
+Its arithmetic is FP32 with FP64 accumulation per batch of <= 32 hits, so the
 fields differ from FP64 by the FP32 rounding of each term; the tolerances
 below are the stated per-field accuracy of the mixed path, about 5x the
 errors measured on GB300 (after the initialisation: rho 2.0e-7, P 3.0e-7,
@@ -104,3 +104,75 @@ def test_mixed_reference_style_operators(gpu):
         sphgpu.apply(g, sphgpu.internal_force)
     e = errors(g64, g32)
     assert e["rho"] <= 1e-6 and e["a"] <= 5e-6
+
+
+def _oracle_state_after(oracle_mod, case, steps):
+    o = oracle_mod.from_case(case)
+    if steps:
+        o.init_state()
+        o.step(steps)
+    o.create_cell_list()
+    return o, o.state()
+
+
+@pytest.mark.parametrize("dim,dr,steps", [(2, 0.02, 0), (3, 0.05, 0), (2, 0.02, 20), (3, 0.05, 4)])
+def test_pair_set_of_both_paths_equals_oracle(gpu, oracle_mod, dim, dr, steps):
+    """The set of neighbour pairs the density pass acts on and stores for the
+    force pass -- the mixed path's hit masks and the FP64 path's rows, read
+    back with sph_debug_hits -- equals the oracle's pair list (core.jl:94-112:
+    every q with r <= h, q != p, in key_diff order) for every fluid target,
+    order included.  Both on the initial lattice (many pairs exactly at
+    r = h) and on the oracle's particles after some steps (off-lattice)."""
+    c = G.dam_break(dim, dr)
+    o, st = _oracle_state_after(oracle_mod, c, steps)
+    ref = o.pairs()
+    ref = ref[st["type"][ref[:, 0]] == G.FLUID]
+    assert len(ref) > 0
+    for prec in (sphgpu.MIXED, sphgpu.FP64):
+        g = sphgpu.ParticleSystem(c.params, prec)
+        g.upload(st["x"], st["v"], type=st["type"])
+        g.create_cell_list()
+        sphgpu.apply(g, sphgpu.find_rho, self=True)
+        hits = g.debug_hits()
+        assert hits.shape == ref.shape, (prec, hits.shape, ref.shape)
+        assert np.array_equal(hits, ref), prec
+        g.close()
+
+
+@pytest.mark.parametrize("dim,dr", [(2, 0.02), (3, 0.05)])
+def test_mixed_error_against_oracle(gpu, oracle_mod, dim, dr):
+    """The mixed path's per-field error measured against the oracle itself
+    (the FP64 path equals the oracle bit for bit, so these are the errors of
+    the mixed arithmetic), after the initial state and after 10 steps, with
+    the bounds stated at the top of this file."""
+    c = G.dam_break(dim, dr)
+    g = sphgpu.ParticleSystem(c.params, sphgpu.MIXED)
+    g.upload(c.x, c.v, type=c.type)
+    o = oracle_mod.from_case(c)
+    g.init_state()
+    o.init_state()
+
+    def err():
+        st = o.state()
+        fl = st["type"] == G.FLUID
+        d = {}
+        for f in ("rho", "P", "a"):
+            x, y = st[f], g.get(f)
+            if x.ndim == 2:
+                d[f] = np.linalg.norm(x - y) / max(np.linalg.norm(x), 1e-300)
+            elif f == "P":
+                d[f] = np.abs(x - y).max() / max(np.abs(x).max(), 1e-300)
+            else:
+                d[f] = (np.abs(x - y)[fl] / np.abs(x)[fl]).max()
+        d["x_over_dr"] = np.abs(st["x"] - g.get("x")).max() / dr
+        return d
+    e0 = err()
+    print(f"\nmixed vs oracle after init ({dim}D dr={dr}): {e0}")
+    assert e0["rho"] <= 1e-6 and e0["P"] <= 2e-6 and e0["a"] <= 5e-6 and e0["x_over_dr"] == 0.0
+    g.step(10)
+    o.step(10)
+    e1 = err()
+    print(f"mixed vs oracle after 10 steps: {e1}")
+    assert g.n == o.n
+    assert e1["x_over_dr"] <= 1e-6
+    g.close()

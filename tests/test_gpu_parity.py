@@ -208,20 +208,37 @@ def test_sums_bitexact(gpu, oracle_mod):
         assert np.array_equal(a, b)
 
 
-def test_collision_energy_gpu(gpu):
-    """tests/test_collision_2d.jl:106-147 on the GPU to t = 1.0: constant
-    particle count, relative energy drift < 1e-2."""
-    from test_oracle_collision import run_collision
+def test_collision_2d_as_written_gpu(gpu, oracle_mod):
+    """tests/test_collision_2d.jl run as written (its scenario, linear EOS,
+    P/rho0^2 pressure force, no gravity, its initialisation and time loop to
+    t = 1.0, 4,168 steps) on the GPU and on the oracle: every field equal to
+    the oracle's bit for bit at each of the test's ten records and at the
+    end, and the test's own assertions on the GPU's records -- a constant
+    particle count and a relative energy increase below 1e-2."""
+    from test_oracle_collision import initialise, run_collision
     c = G.collision_2d()
-    g = sphgpu.ParticleSystem(c.params)
-    g.upload(c.x, c.v, type=c.type)
+    g, o = make(c, oracle_mod)
+    initialise(g.create_cell_list, lambda op, s: sphgpu.apply(g, sphgpu.op_by_id(op), self=s),
+               lambda op: sphgpu.apply(g, sphgpu.op_by_id(op)))
+    initialise(o.create_cell_list, o.apply, o.apply_unary)
+    assert_same_state(g, o)
+    records = []
 
-    def state(s):
-        return {k: s.get(k) for k in ("v", "rho", "rho_ref")}
-    N, E = run_collision(g, 1.0, lambda s: s.init_state(), lambda s, k: s.step(k), state,
-                         lambda s: s.n)
-    assert (N == N[0]).all()
+    def step_both(k):
+        g.step(k)
+        o.step(k)
+
+    def check(k, st):
+        records.append(k)
+        assert_same_state(g, o)
+
+    N, E = run_collision(step_both, lambda: {f: g.get(f) for f in ("v", "rho", "rho_ref")},
+                         lambda: g.n, c.params, on_record=check)
+    assert records == [417 * j for j in range(10)]
+    assert_same_state(g, o)
+    assert np.all(N == N[0])
     assert np.max(E / E[0] - 1.0) < 1e-2
+    g.synchronize()
 
 
 def test_large_2d_first_steps_bitexact(gpu, oracle_mod):
