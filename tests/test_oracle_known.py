@@ -162,7 +162,8 @@ def test_result_independent_of_threads(oracle_mod):
         "st = s.state(); np.save(sys.argv[1], np.concatenate([st['x'].ravel(), st['rho']]))\n")
     import os
     import tempfile
-    paths = [p for p in sys.path[:3]]
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    paths = [root, os.path.join(root, "smoothedparticles.jl_gb300"), os.path.join(root, "oracle")]
     outs = []
     with tempfile.TemporaryDirectory() as td:
         for nt in (1, 3):
