@@ -167,33 +167,31 @@ size_t carve(sph_system* s, char* base, size_t C) {
     const long long cap = 2LL * (long long)C + 64;
     b.ck_cap = (int)(cap < 0x3ffffffLL * 16 ? cap : 0x3ffffffLL * 16);
     b.ck_mask = (unsigned*)take(4 * 32 * (size_t)b.ck_cap);
-    b.hit_cap = 0;
-    b.rows = nullptr;
     b.hit_count = nullptr;
-    b.roff = b.rcur = nullptr;
+    b.row_base = nullptr;
+    b.c4 = nullptr;
+    b.rseg = nullptr;
+    b.pscan_tmp = nullptr;
     b.xfix[0] = b.xfix[1] = b.xfix[2] = nullptr;
     b.frec = nullptr;
-    b.pair_p = b.pair_q = nullptr;
-    b.pair_m = nullptr;
-    b.pair_cap = 0;
+    b.trav = nullptr;
+    b.trav_slots = 0;
   } else {
-    // rows: hits per target ~256 in the 3D lattice interior (H = 4 dr), ~68
-    // in 2D (H = 4.8 dr); the capacity leaves room for compression, and an
-    // overflowed row only sends its target back to a traversal
-    b.hit_cap = D == 3 ? 384 : 160;
-    b.rows = (RowEntry*)take(sizeof(RowEntry) * (size_t)b.hit_cap * C);
+    // the rows themselves and the pair list are sized from the counts and
+    // live in their own allocation (ensure_rows); per particle here: the
+    // row length and start, the per-slot segment offsets, the positions'
+    // fixed-point copies and the force records
     b.hit_count = (int*)take(4 * C);
+    b.row_base = (unsigned*)take(4 * (C + 1));
+    b.c4 = (int*)take(4 * (C + 1));
+    b.pscan_tmp = (int*)take(4 * (scan_tmp_ints((int)C + 1) + 64));
     for (int d = 0; d < 3; ++d) b.xfix[d] = d < D ? (long long*)take(8 * C) : nullptr;
     b.frec = (FxRec*)take(sizeof(FxRec) * C);  // 256-byte aligned start
-    b.roff = (int*)take(4 * (size_t)s->geo.n_diff * C);
-    b.rcur = (int*)take(4 * (size_t)s->geo.n_diff * C);
-    // unordered pairs: a fluid-fluid pair fills two row entries, so half the
-    // rows' capacity is ample (a longer list sends every target to the
-    // traversal)
-    b.pair_cap = (long long)(b.hit_cap / 2) * (long long)C + 1024;
-    b.pair_p = (int*)take(4 * (size_t)b.pair_cap);
-    b.pair_q = (int*)take(4 * (size_t)b.pair_cap);
-    b.pair_m = (unsigned*)take(4 * (size_t)b.pair_cap);
+    b.rseg = (unsigned*)take(4 * (size_t)s->geo.n_diff * C);
+    // the traversal's hit lists: one slot per warp of its persistent grid,
+    // about one warp per 32 particles up to a full device (64 warps per SM)
+    b.trav_slots = (int)std::min<size_t>(C / 32 + 64, 64 * (size_t)s->sms);
+    b.trav = (int*)take(4 * (size_t)b.trav_slots * 32 * kTravCap);
     b.ck_cap = 0;
     b.ck_mask = nullptr;
   }
@@ -227,6 +225,85 @@ int ensure_capacity(sph_system* s, int n) {
   return SPH_OK;
 }
 
+// Rows beyond this many entries cannot be addressed by the 32-bit segment
+// offsets; such systems keep the traversal.
+constexpr unsigned long long kMaxRowEntries = 0xffffffffull - 8191ull;
+
+bool capturing(sph_system* s) {
+  cudaStreamCaptureStatus st = cudaStreamCaptureStatusNone;
+  if (cudaStreamIsCapturing(s->stream, &st) != cudaSuccess) {
+    cudaGetLastError();
+    return true;  // be safe: no allocation
+  }
+  return st != cudaStreamCaptureStatusNone;
+}
+
+// The rows and pair list for `need` row entries: reallocated (nothing to
+// keep: every density pass rewrites them) with 1/12 headroom, so that the
+// slow growth of a compressing flow does not overflow every few steps.
+// Changes the launch arguments, so captured graphs are recaptured.
+int ensure_rows(sph_system* s, unsigned long long need) {
+  BinScratch& b = s->b;
+  if ((long long)need <= b.row_cap || s->rows_impossible) return SPH_OK;
+  if (need > kMaxRowEntries) {
+    s->rows_impossible = true;
+    return SPH_OK;
+  }
+  CK(cudaStreamSynchronize(s->stream));
+  if (s->rowbuf) CK(cudaFree(s->rowbuf));
+  s->rowbuf = nullptr;
+  s->rowbuf_bytes = 0;
+  b.rows = nullptr;
+  b.row_cap = 0;
+  b.pair_p = b.pair_q = nullptr;
+  b.pair_m = nullptr;
+  b.pair_cap = 0;
+  ++s->generation;
+  unsigned long long cap = need + need / 12 + 4096;
+  cap = std::min(cap, kMaxRowEntries) & ~3ull;
+  // a listed pair fills two row entries (fluid-fluid: both targets;
+  // fluid-wall: the fluid target and the wall's row), so half the entries
+  // bound the pairs
+  const unsigned long long pcap = cap / 2 + 1024;
+  const size_t bytes = align_up(sizeof(RowEntry) * cap) + 3 * align_up(4 * pcap);
+  void* p = nullptr;
+  if (cudaMalloc(&p, bytes) != cudaSuccess) {
+    cudaGetLastError();
+    return fail(s, SPH_ERR_NOMEM, "cannot allocate %zu bytes for the FP64 rows (%llu entries)",
+                bytes, cap);
+  }
+  char* c = (char*)p;
+  b.rows = (RowEntry*)c;
+  c += align_up(sizeof(RowEntry) * cap);
+  b.pair_p = (int*)c;
+  c += align_up(4 * pcap);
+  b.pair_q = (int*)c;
+  c += align_up(4 * pcap);
+  b.pair_m = (unsigned*)c;
+  b.row_cap = (long long)cap;
+  b.pair_cap = (long long)pcap;
+  s->rowbuf = p;
+  s->rowbuf_bytes = bytes;
+  return SPH_OK;
+}
+
+// Grows the rows to what an earlier pass reported it needed (the host-mapped
+// word); never during a stream capture.  `wait`: first let the stream finish,
+// so that the report of passes just queued is seen.  Callers: before a
+// density pass or a step (which rebuild the rows), or right after a density
+// pass that had no rows (its wall-pressure and force passes traverse).
+int grow_rows(sph_system* s, bool wait) {
+  if (s->params.precision == SPH_PREC_MIXED || !s->need_host || s->rows_impossible) return SPH_OK;
+  if (capturing(s)) return SPH_OK;
+  if (wait) CK(cudaStreamSynchronize(s->stream));
+  volatile unsigned long long* need = s->need_host;
+  const unsigned long long v = *need;
+  if ((long long)v <= s->b.row_cap) return SPH_OK;
+  const int rc = ensure_rows(s, v);
+  *need = 0;
+  return rc;
+}
+
 int read_count(sph_system* s, int* n) {
   CK(cudaMemcpyAsync(n, s->b.d_n, sizeof(int), cudaMemcpyDeviceToHost, s->stream));
   CK(cudaStreamSynchronize(s->stream));
@@ -235,6 +312,13 @@ int read_count(sph_system* s, int* n) {
 }
 
 int pair_pass(sph_system* s, int op, int self, int reset, int fuse_eos) {
+  // the rows may be replaced only where a pass rebuilds them: before a
+  // density pass (the wall-pressure and force passes read what it wrote)
+  int rc = SPH_OK;
+  if (op == SPH_OP_DENSITY || op == SPH_OP_DENSITY_REF) {
+    rc = grow_rows(s, false);
+    if (rc) return rc;
+  }
   cudaError_t e;
   if (s->params.precision == SPH_PREC_MIXED) {
     // the wall pressure reads fluid records, the force every record
@@ -263,6 +347,12 @@ int pair_pass(sph_system* s, int op, int self, int reset, int fuse_eos) {
   if (op == SPH_OP_DENSITY || op == SPH_OP_DENSITY_REF) {
     s->lists_valid = true;
     s->hits_valid = true;
+    // the first density pass of an FP64 system finds the rows' size (it
+    // traverses, having none): allocate them before the next pass
+    if (s->params.precision != SPH_PREC_MIXED && s->b.row_cap == 0) {
+      rc = grow_rows(s, true);
+      if (rc) return rc;
+    }
   }
   else if (op == SPH_OP_FORCE && s->params.precision != SPH_PREC_MIXED)
     s->lists_valid = false;
@@ -443,10 +533,31 @@ int sph_create(const sph_params* p, int device, sph_system** out) {
   }
   s->device = device;
   DeviceGuard guard(device);
+  if (cudaDeviceGetAttribute(&s->sms, cudaDevAttrMultiProcessorCount, device) != cudaSuccess ||
+      s->sms < 1) {
+    cudaGetLastError();
+    s->sms = 1;
+  }
   if (cudaStreamCreateWithFlags(&s->stream, cudaStreamNonBlocking) != cudaSuccess) {
     cudaGetLastError();
     delete s;
     return SPH_ERR_CUDA;
+  }
+  if (p->precision == SPH_PREC_FP64) {
+    // the word the FP64 passes report a row shortfall in: host memory the
+    // device writes directly, so the host reads it without a copy
+    void* dev_alias = nullptr;
+    if (cudaHostAlloc((void**)&s->need_host, sizeof(unsigned long long), cudaHostAllocMapped) !=
+            cudaSuccess ||
+        cudaHostGetDevicePointer(&dev_alias, s->need_host, 0) != cudaSuccess) {
+      cudaGetLastError();
+      if (s->need_host) cudaFreeHost(s->need_host);
+      cudaStreamDestroy(s->stream);
+      delete s;
+      return SPH_ERR_CUDA;
+    }
+    *s->need_host = 0;
+    s->b.need_host = (unsigned long long*)dev_alias;
   }
   const size_t nb = (size_t)s->geo.key_max + 3;
   const size_t scan_ints = scan_tmp_ints((int)nb) + 64;
@@ -454,6 +565,7 @@ int sph_create(const sph_params* p, int device, sph_system** out) {
   void* cells = nullptr;
   if (cudaMalloc(&cells, bytes) != cudaSuccess) {
     cudaGetLastError();
+    if (s->need_host) cudaFreeHost(s->need_host);
     cudaStreamDestroy(s->stream);
     delete s;
     return SPH_ERR_NOMEM;
@@ -480,11 +592,14 @@ int sph_create(const sph_params* p, int device, sph_system** out) {
   s->b.d_npairs = (unsigned long long*)(c + 1280);
   s->b.d_pover = (int*)(c + 1288);
   s->b.d_rover = (int*)(c + 1292);
+  s->b.d_rowsum = (unsigned long long*)(c + 1296);
   s->d_debug = (int*)(c + 1536);
+  s->b.work_ctr = (int*)(c + 1600);
   if (cudaMemsetAsync(cells, 0, bytes, s->stream) != cudaSuccess ||
       cudaStreamSynchronize(s->stream) != cudaSuccess) {
     cudaGetLastError();
     cudaFree(cells);
+    if (s->need_host) cudaFreeHost(s->need_host);
     cudaStreamDestroy(s->stream);
     delete s;
     return SPH_ERR_CUDA;
@@ -505,6 +620,8 @@ int sph_destroy(sph_system* s) {
   for (auto e : s->pool) cudaEventDestroy(e);
   if (s->open_start) cudaEventDestroy(s->open_start);
   if (s->arena) cudaFree(s->arena);
+  if (s->rowbuf) cudaFree(s->rowbuf);
+  if (s->need_host) cudaFreeHost(s->need_host);
   if (s->cells) cudaFree(s->cells);
   if (s->query) cudaFree(s->query);
   cudaStreamDestroy(s->stream);
@@ -1079,12 +1196,44 @@ int sph_get_tuning(const sph_system* s, int* warps_per_block) {
   return SPH_OK;
 }
 
+// Multiprocessors assumed by sph_memory_estimate (no CUDA call there): at
+// least the count of any single GPU of this class, so the traversal scratch
+// it adds is an upper bound.
+constexpr int kEstimateSms = 160;
+
+// The FP64 rows and pair list of n particles on the lattice the parameters
+// imply (spacing dr = (m / rho0)^(1/dim)): every particle a full lattice
+// neighbourhood within h (an interior fluid target -- walls and surface
+// particles have fewer), rows padded to four entries, the headroom
+// ensure_rows adds.  Only an estimate: a flow that clusters its particles
+// needs more, and the rows then grow.
+static size_t rows_estimate(const sph_params* p, long long n) {
+  if (p->precision == SPH_PREC_MIXED || n <= 0) return 0;
+  double dr = 0.0;
+  if (p->mass > 0.0 && p->rho0 > 0.0) dr = std::pow(p->mass / p->rho0, 1.0 / p->dim);
+  double ratio = dr > 0.0 ? p->h / dr : 4.0;
+  if (!(ratio > 0.0) || ratio > 64.0) ratio = 4.0;
+  const int R = (int)std::ceil(ratio);
+  const double r2 = ratio * ratio * (1.0 + 1e-9);
+  long long nb = 0;
+  for (int i = -R; i <= R; ++i)
+    for (int j = -R; j <= R; ++j)
+      for (int k = (p->dim == 3 ? -R : 0); k <= (p->dim == 3 ? R : 0); ++k)
+        if ((i || j || k) && (double)(i * i + j * j + k * k) <= r2) ++nb;
+  const unsigned long long need = (unsigned long long)n * (unsigned long long)((nb + 3) & ~3LL);
+  unsigned long long cap = std::min(need + need / 12 + 4096, kMaxRowEntries) & ~3ull;
+  const unsigned long long pcap = cap / 2 + 1024;
+  return align_up(sizeof(RowEntry) * cap) + 3 * align_up(4 * pcap);
+}
+
 int sph_memory_estimate(const sph_params* p, int64_t n, uint64_t* bytes) {
   if (!p || !bytes || n < 0 || n > 0x7fffffffLL - 64) return SPH_ERR_ARG;
   sph_system tmp;
   const int rc = setup_host(p, &tmp);
   if (rc) return rc;
-  *bytes = (uint64_t)(cells_bytes(&tmp) + carve(&tmp, nullptr, (size_t)(n > 0 ? n : 1)));
+  tmp.sms = kEstimateSms;
+  *bytes = (uint64_t)(cells_bytes(&tmp) + carve(&tmp, nullptr, (size_t)(n > 0 ? n : 1)) +
+                      rows_estimate(p, n));
   return SPH_OK;
 }
 
@@ -1093,8 +1242,10 @@ int sph_memory_usage(const sph_system* s, uint64_t* bytes) {
   sph_system tmp;
   tmp.params = s->params;
   tmp.geo = s->geo;
+  tmp.sms = s->sms;
   size_t b = cells_bytes(s);
   if (s->arena) b += carve(&tmp, nullptr, (size_t)s->cap);
+  b += s->rowbuf_bytes;
   b += s->query_bytes;
   *bytes = (uint64_t)b;
   return SPH_OK;
@@ -1339,6 +1490,12 @@ const char* sph_batch_last_error(const sph_batch* b) { return b ? b->err.c_str()
 int sph_batch_step(sph_batch* b, int nsteps) {
   if (!b || nsteps < 0) return SPH_ERR_ARG;
   DeviceGuard guard(b->device);
+  // FP64 members whose rows fell short in earlier steps grow them now (a
+  // new generation: the graph is captured again)
+  for (auto* m : b->members) {
+    const int rc = grow_rows(m, false);
+    if (rc) return bfail(b, rc, "growing a member's rows failed");
+  }
   bool stale = !b->exec;
   for (size_t j = 0; j < b->members.size(); ++j)
     if (b->generations[j] != b->members[j]->generation ||

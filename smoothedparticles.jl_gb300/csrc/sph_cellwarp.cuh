@@ -15,12 +15,12 @@
 // A candidate is classified in FP32; only candidates within a thin band around
 // the support radius take the reference's FP64 test (proof in sph_pair64.cu).
 //
-// Hits are appended, in traversal order, to a list in the target's row of
-// global memory (see cw_list).  After the traversal every lane processes its
-// own list in order, so each target's sums are formed in exactly the
-// reference's order, and the lanes' lists have nearly equal lengths (the FP64
-// work runs with full warps).  A list that would exceed hit_cap is processed
-// early.
+// Hits are appended, in traversal order, to a per-lane list in global memory
+// (see cw_list; the warp's slot of the traversal scratch).  After the
+// traversal every lane processes its own list in order, so each target's
+// sums are formed in exactly the reference's order, and the lanes' lists
+// have nearly equal lengths (the FP64 work runs with full warps).  A list
+// that would exceed kTravCap entries is processed early.
 #pragma once
 
 #include "sph_common.cuh"
@@ -68,12 +68,14 @@ __device__ __forceinline__ void cw_offsets(const Geometry& g, const Consts& k, C
   __syncwarp();
 }
 
-// Target i's list is the contiguous segment hits[i * hit_cap ...].  Appends go
-// through an 8-entry ring per lane in shared memory and reach global memory
-// as whole 32-byte sectors (no partially written sectors for the L2 to fill
-// from DRAM); the process phase reads each list sequentially.
-__device__ __forceinline__ int* cw_list(const BinScratch& b, int i) {
-  return reinterpret_cast<int*>(b.rows + (size_t)i * b.hit_cap);
+// A lane's list is kTravCap contiguous entries of the warp's slot of the
+// traversal scratch (slot < trav_slots; the persistent traversal grid gives
+// each warp its own).  Appends go through an 8-entry ring per lane in shared
+// memory and reach global memory as whole 32-byte sectors (no partially
+// written sectors for the L2 to fill from DRAM); the process phase reads each
+// list sequentially.
+__device__ __forceinline__ int* cw_list(const BinScratch& b, int slot, int lane) {
+  return b.trav + ((size_t)slot * 32 + lane) * kTravCap;
 }
 constexpr int kCwRow = 1;  // elements between consecutive entries of one list
 
@@ -129,9 +131,9 @@ __device__ __forceinline__ void cw_resolve(const State& s, const Consts& k, CwSh
 template <int DIM, bool FLUID_CELLS_ONLY, class P>
 __device__ __forceinline__ void cw_traverse(const State& s, const Geometry& g, const Consts& k,
                                             const BinScratch& b, CwShared& sh, int lane,
-                                            const CwTarget& t, P& proc) {
-  int* const list = cw_list(b, t.i);  // dereferenced only by active lanes
-  const int cap = b.hit_cap;
+                                            const CwTarget& t, P& proc, int slot) {
+  int* const list = cw_list(b, slot, lane);  // dereferenced only by active lanes
+  const int cap = kTravCap;
   int cnt = 0;
   int nb = 0;  // deferred band candidates of this lane
   cw_offsets(g, k, sh, lane, t);
@@ -247,8 +249,8 @@ __device__ __forceinline__ void cw_count(const BinScratch& b, int c0, int c1, in
 template <int DIM, int OP, class P>
 __device__ __forceinline__ void cw_pass(const State& s, const Geometry& g, const Consts& k,
                                         const BinScratch& b, CwShared& sh, int lane,
-                                        const CwTarget& t, P& proc, int) {
-  cw_traverse<DIM, OP == SPH_OP_WALL_PRESSURE>(s, g, k, b, sh, lane, t, proc);
+                                        const CwTarget& t, P& proc, int slot) {
+  cw_traverse<DIM, OP == SPH_OP_WALL_PRESSURE>(s, g, k, b, sh, lane, t, proc, slot);
 }
 
 // d = x_p - x_q and the kernel distance sqrt((d0 d0 + d1 d1) + d2 d2) with the

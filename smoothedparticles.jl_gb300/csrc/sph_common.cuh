@@ -138,7 +138,8 @@ struct BinScratch {
   int* d_n;         // particle count (device-resident)
   int* d_nrem;      // particles removed by the last binning
   int* d_err;       // error bits
-  int* scan_tmp;    // block sums of the scans
+  int* scan_tmp;    // block sums of the scans over the cell tables
+  int* pscan_tmp;   // block sums of the scans over the particles (FP64 rows)
   unsigned long long* d_pairs;
   // hits per category: [0] density sums, [1] wall pressure (fluid q),
   // [2] force fluid-fluid, [3] force fluid-wall, [4] force with viscosity
@@ -147,20 +148,34 @@ struct BinScratch {
   int2* items;      // (first target, count)
   int* item_off;    // key_max + 3: exclusive prefix of items per cell
   int max_items;    // capacity of `items`
-  // FP64 passes (null in mixed-precision systems).  Every fluid target i
-  // owns a row of hit_cap entries at rows + i * hit_cap, its neighbours in
-  // the reference's order; hit_count[i] entries are used (> hit_cap: the
-  // row overflowed and the target traverses instead).  The row is split into
-  // one segment per neighbour-cell slot c (key_diff order), starting at
-  // roff[i * n_diff + c] (sph_tile64.cu).  A traversal (sph_cellwarp.cuh)
-  // uses the rows of its own targets as scratch.
+  // FP64 passes (null in mixed-precision systems).  Compact rows (CSR):
+  // particle i's row -- its neighbours in the reference's order; a wall's
+  // row holds its fluid neighbours -- is hit_count[i] entries starting at
+  // entry 4 * row_base[i] of `rows` (every row padded to a multiple of four
+  // entries, 128 bytes).  The row is split into one segment per
+  // neighbour-cell slot c (key_diff order): the tile kernel counts each
+  // segment's hits into rseg[i * n_diff + c], the row scan turns the counts
+  // into the segments' absolute first entries (sph_tile64.cu).  A row that
+  // cannot be used (a segment of more than kSegMax hits, a neighbour cell of
+  // more than 65535 particles) has hit_count kRowOver and its target
+  // traverses; so does every target when the rows do not fit row_cap (the
+  // host grows them before the next pass).
   RowEntry* rows;
+  long long row_cap;    // entries `rows` holds (< 2^32)
+  unsigned* row_base;   // cap + 1: exclusive prefix of c4 (row starts / 4)
+  int* c4;              // cap + 1: (hit_count + 3) / 4, 0 for rows not used
+  unsigned* rseg;       // n_diff per particle: hits per slot, then first entries
   int* hit_count;
+  // the largest row total a pass needed beyond row_cap (host-mapped memory,
+  // read by the host to grow the rows between passes)
+  unsigned long long* need_host;
   long long* xfix[3];  // positions as exact fixed-point integers (fx_fix), per step
   FxRec* frec;         // per particle, for the force pass (FxRec)
-  int* roff;          // n_diff per particle: first entry of each slot's segment
-  int* rcur;          // n_diff per particle: hits per slot
-  int hit_cap;
+  // the traversal's per-lane hit lists (sph_cellwarp.cuh): trav_slots warps,
+  // each 32 lists of kTravCap entries, claimed by a persistent grid's warps
+  int* trav;
+  int trav_slots;
+  int* work_ctr;       // the traversal's item counter (reset before each launch)
   // the step's unordered pairs (sph_tile64.cu), pair_cap at most: the two
   // particles and (rank in p's segment, rank in q's segment, slot, walls)
   int* pair_p;
@@ -168,8 +183,13 @@ struct BinScratch {
   unsigned* pair_m;
   long long pair_cap;
   unsigned long long* d_npairs;  // pairs listed (may exceed pair_cap)
-  int* d_pover;                  // the list overflowed: every target traverses
+  // the list (or the rows) overflowed: every target traverses
+  int* d_pover;
   int* d_rover;                  // some target's row overflowed (it traverses)
+  // the sum of c4 over the particles in 64 bits (follows d_rover: cleared
+  // with the pair count and the flags), so that an int32 scan that wrapped
+  // is never trusted
+  unsigned long long* d_rowsum;
   int* cell_fluid;    // key_max + 3: fluid particles per cell
   // mixed-precision passes: one 32-bit hit mask per lane and 32-candidate
   // chunk of the neighbour sequence (sph_pair32.cu); item j of cell k owns
@@ -179,6 +199,11 @@ struct BinScratch {
   int ck_cap;
   int* chunk_off;     // key_max + 3: exclusive prefix of the cells' slots
 };
+
+constexpr int kSegMax = 1022;        // hits of one row segment a rank can address
+constexpr int kRowOver = 0x7fffffff; // hit_count of a row that is not used
+constexpr unsigned kNoRow = 0xffffffffu;
+constexpr int kTravCap = 256;        // entries of a traversal hit list
 
 // Upper bound of the work-list length for n particles (every cell with
 // particles contributes ceil(c/32) <= c/32 + 1 items).

@@ -104,11 +104,11 @@ cudaError_t launch_pair_fp64(const LaunchCtx& c, const State& s, const Geometry&
                              const Consts& k, const BinScratch& b, int cap, int op, int self,
                              int reset, int fuse_eos, int lists_valid);
 // ---- FP64 pair evaluation once per pair (sph_tile64.cu)
-// phase 0 (density pass): counts, row offsets, m W and distances into the
-// rows; phase 1 (force pass, after the density pass of the same binning):
-// the force records, then pressure and XSPH factors into the rows.  Launches
-// kTilesLaunches[phase] kernels.
-constexpr int kTilesLaunches[2] = {3, 2};
+// phase 0 (density pass): counts, row lengths, the rows' scan and segment
+// offsets, m W and distances into the rows; phase 1 (force pass, after the
+// density pass of the same binning): the force records, then pressure and
+// XSPH factors into the rows.  Launches kTilesLaunches[phase] kernels.
+constexpr int kTilesLaunches[2] = {7, 2};
 // launches of the density (0) and force (1) passes of a step: the tile
 // kernels, the row sums and the traversal of overflowed rows
 constexpr int kRowPassLaunches[2] = {kTilesLaunches[0] + 2, kTilesLaunches[1] + 2};

@@ -130,7 +130,7 @@ struct Proc64 {
   // or its pressure and XSPH factors, once per pair): the same terms,
   // accumulated in the same order, as process() over the traversal's list.
   __device__ __forceinline__ void rows(const BinScratch& b, int i, int cnt) {
-    const RowEntry* row = b.rows + (size_t)i * b.hit_cap;
+    const RowEntry* row = b.rows + 4 * (size_t)__ldg(&b.row_base[i]);
     if (OP == SPH_OP_DENSITY || OP == SPH_OP_DENSITY_REF) {
       for (int j = 0; j < cnt; ++j) acc = acc + __ldg(&row[j].a);
       c0 += cnt;
@@ -286,23 +286,29 @@ __device__ __forceinline__ void target_epilogue(const State& s, const Consts& k,
   }
 }
 
-// One warp per work item; the warps stride over the items (one resident
-// wave of blocks, so that a launch with little to do costs little).
+// A persistent grid of at most trav_slots warps, each with its own slot of
+// the traversal scratch, taking work items from a counter (zeroed before the
+// launch) so that uneven items balance; one warp per item.
 template <int DIM, int OP, int WARPS>
 __global__ void __launch_bounds__(32 * WARPS) pair64_kernel(State s, Geometry g, Consts k,
                                                             BinScratch b, int self, int reset,
-                                                            int fuse_eos, int list_mode,
-                                                            int warps_total) {
+                                                            int fuse_eos, int list_mode) {
   __shared__ CwShared shared[WARPS];
   const int lane = threadIdx.x & 31;
   const int w = threadIdx.x >> 5;
-  // list_mode 3: row_sum_kernel took every target whose row is complete;
+  const int slot = blockIdx.x * WARPS + w;
+  if (slot >= b.trav_slots) return;  // warp-uniform
+  // list_mode 3: the row sums took every target whose row is complete;
   // only overflowed rows traverse here
   if (list_mode == 3 && *b.d_rover == 0 && *b.d_pover == 0) return;
   const int total = __ldg(&b.item_off[g.key_max + 1]);
   // the wall pressure acts on wall targets, every other operator on fluid ones
   const int want = OP == SPH_OP_WALL_PRESSURE ? kWall : kFluid;
-  for (int item = blockIdx.x * WARPS + w; item < total; item += warps_total) {
+  for (;;) {
+    int item = 0;
+    if (lane == 0) item = atomicAdd(b.work_ctr, 1);
+    item = __shfl_sync(0xffffffffu, item, 0);
+    if (item >= total) break;
     const int2 it = __ldg(&b.items[item]);
     const int first = it.x, count = it.y;
     const int i = first + lane;
@@ -311,7 +317,7 @@ __global__ void __launch_bounds__(32 * WARPS) pair64_kernel(State s, Geometry g,
     CwTarget t;
     t.active = valid && ti == want;
     if (list_mode == 3)
-      t.active = t.active && (__ldg(&b.hit_count[i]) > b.hit_cap || *b.d_pover != 0);
+      t.active = t.active && (__ldg(&b.hit_count[i]) == kRowOver || *b.d_pover != 0);
     else if (valid && ti != want)
       skipped_target<DIM, OP>(s, i, reset);
     // an item without targets of the operator has nothing to traverse
@@ -328,7 +334,7 @@ __global__ void __launch_bounds__(32 * WARPS) pair64_kernel(State s, Geometry g,
     p.xp[1] = t.xp[1];
     p.xp[2] = t.xp[2];
     if (t.active) target_prologue<DIM, OP>(s, i, reset, p);
-    cw_pass<DIM, OP>(s, g, k, b, shared[w], lane, t, p, 0);
+    cw_pass<DIM, OP>(s, g, k, b, shared[w], lane, t, p, slot);
     if (t.active) target_epilogue<DIM, OP>(s, k, i, p, self, fuse_eos);
     cw_count<OP>(b, p.c0, p.c1, p.c2);
   }
@@ -350,7 +356,7 @@ __global__ void __launch_bounds__(256, 5) row_sum_kernel(State s, Consts k, BinS
       skipped_target<DIM, OP>(s, i, reset);
     } else {
       const int cnt = __ldg(&b.hit_count[i]);
-      if (cnt <= b.hit_cap && *b.d_pover == 0) {
+      if (cnt != kRowOver && *b.d_pover == 0) {
         p.xp[0] = s.x[0][i];
         p.xp[1] = s.x[1][i];
         p.xp[2] = DIM == 3 ? s.x[2][i] : 0.0;
@@ -361,6 +367,99 @@ __global__ void __launch_bounds__(256, 5) row_sum_kernel(State s, Consts k, BinS
     }
   }
   cw_count<OP>(b, p.c0, p.c1, p.c2);
+}
+
+// The wall pressure of a step over the walls' rows (their fluid neighbours,
+// written by the density pass): one warp per 32 consecutive particles.  The
+// warp takes its walls that have fluid neighbours one after another; for
+// each, its lanes form the terms of 32 row entries at once (the entry, the
+// neighbour's record, the kernel value from the stored t, g . d), and lane 0
+// adds them up in the row's order -- the reference's summation order, as
+// Proc64::rows forms it.  A wall without fluid neighbours gets the empty sum
+// (P = 0).  Walls whose rows are not used (kRowOver, or every target after an
+// overflow) are left to pair64_kernel.
+template <int DIM>
+__global__ void __launch_bounds__(256) wall_rows_kernel(State s, Consts k, BinScratch b) {
+  __shared__ double terms[8][3][32];
+  const unsigned full = 0xffffffffu;
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  const int n = *b.d_n;
+  const int i0 = (blockIdx.x * 8 + w) * 32;
+  if (i0 >= n) return;  // warp-uniform
+  const int i = i0 + lane;
+  const bool pover = *b.d_pover != 0;
+  int cnt = 0;
+  bool use = false;
+  if (i < n && s.type[i] == kWall) {
+    cnt = __ldg(&b.hit_count[i]);
+    use = !pover && cnt != kRowOver;
+  }
+  if (use && cnt == 0) {
+    s.P[i] = 0.0;
+    s.Pr[i] = 0.0 / (k.rho0 * k.rho0);
+    s.rho[i] = k.rho0;
+  }
+  int c0 = use ? cnt : 0;
+  unsigned todo = __ballot_sync(full, use && cnt > 0);
+  while (todo) {
+    const int j = __ffs(todo) - 1;
+    todo &= todo - 1u;
+    const int t = i0 + j;
+    const int tc = __shfl_sync(full, cnt, j);
+    const RowEntry* row = b.rows + 4 * (size_t)__ldg(&b.row_base[t]);
+    const long long X0 = __ldg(&b.xfix[0][t]), X1 = __ldg(&b.xfix[1][t]);
+    const long long X2 = DIM == 3 ? __ldg(&b.xfix[2][t]) : 0;
+    double wp = 0.0, wg = 0.0, ws = 0.0;
+    for (int e0 = 0; e0 < tc; e0 += 32) {
+      const int m = min(32, tc - e0);
+      double tw = 0.0, ta = 0.0, tb = 0.0;
+      bool ok = false;
+      if (lane < m) {
+        const RowEntry en = row_load(row + e0 + lane);
+        const int q = (int)(en.q & 0x7fffffffu);
+        ok = q < n;
+        if (ok) {
+          const double tt = en.c;  // ker_t of the stored distance
+          const double t2 = tt * tt;
+          tw = (k.cw * (t2 * t2)) * __fma_rn(-4.0, tt, 5.0);
+          // q's position half of its record (written by the density pass)
+          long long QX0, QX1, QX2;
+          double qv0;
+          frec_load_x(b.frec + q, QX0, QX1, QX2, qv0);
+          const double d0 = fx_sep2(X0, &s.x[0][t], QX0, &s.x[0][q], k.fx_k);
+          const double d1 = fx_sep2(X1, &s.x[1][t], QX1, &s.x[1][q], k.fx_k);
+          double gd = __fma_rn(k.g[1], d1, k.g[0] * d0);
+          if (DIM == 3) gd = __fma_rn(k.g[2], fx_sep2(X2, &s.x[2][t], QX2, &s.x[2][q], k.fx_k), gd);
+          ta = __ldg(&s.P[q]);
+          tb = __ldg(&s.rho[q]) * gd;
+        }
+      }
+      // an entry the tile passes did not write: reported, skipped
+      const unsigned valid = __ballot_sync(full, ok);
+      if (lane == 0 && __popc(valid) != m) atomicOr(b.d_err, kErrBounds);
+      terms[w][0][lane] = tw;
+      terms[w][1][lane] = ta;
+      terms[w][2][lane] = tb;
+      __syncwarp();
+      if (lane == 0) {
+        for (int u = 0; u < m; ++u) {
+          if (!((valid >> u) & 1u)) continue;
+          const double ww = terms[w][0][u];
+          wp = __fma_rn(terms[w][1][u], ww, wp);
+          wg = __fma_rn(terms[w][2][u], ww, wg);
+          ws = ws + ww;
+        }
+      }
+      __syncwarp();
+    }
+    if (lane == 0) {
+      const double P = ws > 0.0 ? (wp + wg) / ws : 0.0;
+      s.P[t] = P;
+      s.Pr[t] = P / (k.rho0 * k.rho0);
+      s.rho[t] = k.rho0;
+    }
+  }
+  cw_count<SPH_OP_WALL_PRESSURE>(b, c0, 0, 0);
 }
 
 // sum(sys, func, x) (core.jl:240-260) / sum(sys, func, p) (core.jl:271-291):
@@ -489,10 +588,10 @@ __global__ void __launch_bounds__(128) debug_hits_kernel(State s, Geometry g, Bi
   if (s.type[i] == kFluid) {
     if (!mixed) {
       const int hc = b.hit_count[i];
-      if (hc > b.hit_cap || *b.d_pover != 0) {
+      if (hc == kRowOver || *b.d_pover != 0) {
         atomicOr(bad, 1);
       } else {
-        const RowEntry* row = b.rows + (size_t)i * b.hit_cap;
+        const RowEntry* row = b.rows + 4 * (size_t)b.row_base[i];
         for (int j = 0; j < hc; ++j, ++pos, ++cnt)
           if (pass && pos < cap_pairs) {
             pairs[2 * pos] = rid;
@@ -541,18 +640,18 @@ __global__ void __launch_bounds__(128) debug_hits_kernel(State s, Geometry g, Bi
   if (!pass) counts[rid] = cnt;
 }
 
-// pair64_kernel with one warp per work item (the block scheduler balances
-// the uneven items), or, for the sweep over overflowed rows (list_mode 3,
-// usually nothing to do), one resident wave of blocks striding over them
+// pair64_kernel: at most one resident wave of blocks and at most
+// trav_slots warps (each needs its own slot of the traversal scratch)
 template <int DIM, int OP, int WARPS>
 void pair64_launch(cudaStream_t st, const BinScratch& b, int threads, const State& s,
                    const Geometry& g, const Consts& k, const BinScratch& bb, int self, int reset,
                    int fuse_eos, int list_mode) {
   static const int wave = resident_blocks(pair64_kernel<DIM, OP, WARPS>, 32 * WARPS);
-  const int all = std::max(1, (b.max_items + WARPS - 1) / WARPS);
-  const int blocks = list_mode == 3 ? std::min(all, wave) : all;
+  const int need = std::max(1, std::min(b.max_items, b.trav_slots));
+  const int blocks = std::max(1, std::min((need + WARPS - 1) / WARPS, wave));
+  cudaMemsetAsync(b.work_ctr, 0, sizeof(int), st);
   pair64_kernel<DIM, OP, WARPS><<<blocks, threads, 0, st>>>(s, g, k, bb, self, reset, fuse_eos,
-                                                           list_mode, blocks * WARPS);
+                                                           list_mode);
 }
 
 template <int DIM>
@@ -571,7 +670,7 @@ cudaError_t launch_pair_dim(const LaunchCtx& c, const State& s, const Geometry& 
     const int rb = (cap + 255) / 256;
     if (op == SPH_OP_WALL_PRESSURE) {
       // the density pass's rows hold every wall's fluid neighbours
-      row_sum_kernel<DIM, SPH_OP_WALL_PRESSURE><<<rb, 256, 0, c.stream>>>(s, k, b, 0, 0, 0);
+      wall_rows_kernel<DIM><<<(cap + 255) / 256, 256, 0, c.stream>>>(s, k, b);
     } else {
       const cudaError_t e = launch_tiles_fp64(c, s, g, k, b, cap, op == SPH_OP_FORCE ? 1 : 0);
       if (e != cudaSuccess) return e;

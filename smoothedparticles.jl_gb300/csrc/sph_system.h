@@ -28,6 +28,14 @@ struct sph_system {
   double* query = nullptr;  // sum() query buffer
   size_t query_bytes = 0;
   int cap = 0;              // particles the arena holds
+  int sms = 1;              // multiprocessors of the device
+  // FP64 systems: the rows and the pair list (their own allocation, grown
+  // to a high-water mark of what the passes needed) and the host-mapped word
+  // the passes report a shortfall in
+  void* rowbuf = nullptr;
+  size_t rowbuf_bytes = 0;
+  unsigned long long* need_host = nullptr;
+  bool rows_impossible = false;  // more entries than 32-bit offsets address
   int n_host = 0;           // upper bound of the device-resident count
   bool cells_valid = false;
   // FP32 neighbour records current (mixed precision): of the fluid particles

@@ -12,8 +12,9 @@
 // the FP32 band the FP32 decision equals the exact test, inside the band it
 // is the exact test, which squares the differences.
 //
-// Rows: every fluid target owns hit_cap entries (neighbour index, distance,
-// two factors).  Its neighbours in the reference's order (core.jl:96-105) are
+// Rows (CSR, sized from the counts): every target's row holds its
+// neighbours (neighbour index, distance, two factors; a wall's row its fluid
+// neighbours).  The neighbours in the reference's order (core.jl:96-105) are
 // the slots of key_diff in turn, each slot's cell in stored order, so the row
 // is one segment per slot: the segment of (target i, slot c) holds i's hits
 // in cell key(i) + key_diff[c], in ascending index order.
@@ -32,11 +33,14 @@
 // blocks are symmetric.
 //
 // Passes of a step (launch order):
-//   tiles    classify once: rcur := hits per (target, slot); the pair list
+//   tiles    classify once: rseg := hits per (target, slot); the pair list
 //            (p, q, both ranks, slot, wall bits)
-//   scan     roff := exclusive prefix over the target's slots; hit_count;
+//   count    hit_count (the row length), c4 = the row in 128-byte units;
 //            the fixed-point positions (xfix and the records' first halves)
-//   density  per pair: m W, r and t into both rows (at roff + rank)
+//   scan     row_base := exclusive prefix of c4 over the particles
+//   offsets  rseg := each segment's absolute first entry; rows beyond
+//            row_cap send every target to the traversal (and tell the host)
+//   density  per pair: m W, r and t into both rows (at rseg + rank)
 //   [sum]    sph_pair64.cu: rho = the row's sum, self term, EOS
 //   [wall]   sph_pair64.cu: each wall's pressure over its row (fluid
 //            neighbours, the kernel value from the stored t)
@@ -45,10 +49,11 @@
 //            the fluid target's row: walls are not force targets)
 //   [sum]    sph_pair64.cu: a += cf d, xs += -wx dv over the row
 //
-// A row longer than hit_cap, or a target next to a cell of more than 65535
-// particles (the tiles' 16-bit local indices), is marked overflowed by the
-// scan; its sum passes traverse instead.  A pair list longer than pair_cap
-// sends every target to the traversal.
+// A row with a segment of more than kSegMax hits (the 10-bit ranks), or a
+// target next to a cell of more than 65535 particles (the tiles' 16-bit local
+// indices), is marked overflowed by the count; its sum passes traverse
+// instead.  A pair list longer than pair_cap, or rows beyond row_cap, send
+// every target to the traversal.
 //
 // The pair kernels form position differences, the kernel distance's square
 // root and the force's reciprocals on the integer pipes, correctly rounded
@@ -69,12 +74,13 @@ constexpr int kTileWarps = 4;
 constexpr int kTileList = 512;         // pairs buffered per warp before they are listed
 constexpr float kTileFar = 1.0e18f;    // coordinate of an empty staging slot
 // pair_m: rank in p's segment (10 bits), rank in q's segment (10), slot (5),
-// p is a wall, q is a wall.  A rank of kRankNone (>= every hit_cap) marks a
-// side beyond its row.  Wall rows hold their fluid neighbours (pairs of two
-// walls are not listed) for the wall pressure.
+// p is a wall, q is a wall.  A rank of kRankNone (> kSegMax) marks a side
+// beyond what a rank addresses (that target's row is not used).  Wall rows
+// hold their fluid neighbours (pairs of two walls are not listed) for the
+// wall pressure.
 constexpr unsigned kRankNone = 1023u;
+static_assert(kSegMax < (int)kRankNone, "ranks up to kSegMax must be encodable");
 constexpr unsigned kPWall = 1u << 25, kQWall = 1u << 26;
-constexpr int kNoRow = 1 << 24;  // segment offset of a target without a row
 
 struct TileShared {
   // rows: cell-relative positions minus b's offset (pairs of rows are read
@@ -127,7 +133,7 @@ __device__ __forceinline__ void tile_run(const State& s, const Geometry& g, cons
   const int nd = g.n_diff;
   const bool self = c == (nd >> 1);
   const int mc = nd - 1 - c;
-  const int cap = b.hit_cap;
+  const int cap = kSegMax + 1;  // ranks below this are addressable
   const unsigned below = lanemask_lt();
   // b's origin relative to a's (the traversal's cw_offset)
   int acx, acy, acz, bcx, bcy, bcz;
@@ -151,7 +157,7 @@ __device__ __forceinline__ void tile_run(const State& s, const Geometry& g, cons
       pr.y = pr.y - oy;
       pr.z = pr.z - oz;
       // in the own cell's tile, earlier blocks counted p's hits as a column
-      if (self && ia > 0) rc = b.rcur[(size_t)p * nd + c];
+      if (self && ia > 0) rc = (int)b.rseg[(size_t)p * nd + c];
     }
     __syncwarp();
     sh.rx[lane] = pr.x;
@@ -234,7 +240,7 @@ __device__ __forceinline__ void tile_run(const State& s, const Geometry& g, cons
       size_t cj = 0;
       if (!diag && lane < mb) {
         cj = (size_t)q * nd + mc;
-        cc = ia == 0 ? 0 : b.rcur[cj];
+        cc = ia == 0 ? 0 : (int)b.rseg[cj];
       }
       sh.rmask[lane] = rm;
       sh.rcur[lane] = rc;
@@ -243,7 +249,7 @@ __device__ __forceinline__ void tile_run(const State& s, const Geometry& g, cons
       // its rows in ascending order, so its rank in the column's segment
       // counts up from the cursor (in the diagonal block the bits below the
       // lane are all of the column's bits below each row taken).  A side
-      // without a row entry (a wall, or a rank beyond hit_cap) is marked
+      // without a row entry (a wall, or a rank beyond kSegMax) is marked
       // kRankNone; the pair kernels skip a pair with neither.
       unsigned em = diag ? (cm & below) : cm;
       const unsigned lbase = (unsigned)(32 * ia) | ((unsigned)(32 * jb + lane) << 16);
@@ -308,11 +314,11 @@ __device__ __forceinline__ void tile_run(const State& s, const Geometry& g, cons
           ln += __popc(hb);
         }
       }
-      if (!diag && lane < mb) b.rcur[cj] = cc + __popc(cm);
+      if (!diag && lane < mb) b.rseg[cj] = (unsigned)(cc + __popc(cm));
       __syncwarp();
       rc += __popc(rm);
     }
-    if (lane < ma) b.rcur[(size_t)p * nd + c] = rc;
+    if (lane < ma) b.rseg[(size_t)p * nd + c] = (unsigned)rc;
   }
   if (ln > 0) {
     __syncwarp();
@@ -351,14 +357,10 @@ __global__ void __launch_bounds__(32 * kTileWarps, 10) tile_kernel(State s, Geom
   }
 }
 
-// Row offsets of every particle from its per-slot counts (a wall's row
-// holds its fluid neighbours); the positions' fixed-point copies for the
-// pair kernels.
-__global__ void __launch_bounds__(256) row_scan_kernel(State s, Geometry g, Consts k,
-                                                       BinScratch b) {
-  const int n = *b.d_n;
-  const int i = blockIdx.x * 256 + threadIdx.x;
-  if (i >= n) return;
+// Particle i's part of row_count_kernel: returns its row in units of four
+// entries.
+__device__ __forceinline__ int row_count_body(const State& s, const Geometry& g, const Consts& k,
+                                              const BinScratch& b, int i) {
   long long X[3] = {0, 0, 0};
   for (int d = 0; d < k.dim; ++d) {
     X[d] = fx_fix(s.x[d][i], k.fx_k);
@@ -373,6 +375,7 @@ __global__ void __launch_bounds__(256) row_scan_kernel(State s, Geometry g, Cons
   bool over = __ldg(&b.cell_start[key + 1]) - __ldg(&b.cell_start[key]) > 0xffff;
   const bool own_fluid = __ldg(&b.cell_fluid[key]) != 0;
   int run = 0;
+  unsigned* seg = b.rseg + (size_t)i * nd;
   for (int c = 0; c < nd; ++c) {
     const int nk = key + g.key_diff[c];
     int cnt = 0;
@@ -382,20 +385,73 @@ __global__ void __launch_bounds__(256) row_scan_kernel(State s, Geometry g, Cons
       // a tile between two cells without fluid is skipped (no pair of it
       // involves a fluid particle), so its counts are not written
       else if (m > 0 && (own_fluid || __ldg(&b.cell_fluid[nk]) != 0))
-        cnt = b.rcur[(size_t)i * nd + c];
+        cnt = (int)seg[c];
     }
-    b.roff[(size_t)i * nd + c] = run;
+    if (cnt > kSegMax) over = true;
+    seg[c] = (unsigned)cnt;
     run += cnt;
   }
-  if (over || run > b.hit_cap) {
-    // an overflowed target has no row entries: its offsets lie beyond the
-    // row, so the pair passes treat its side like a wall's (and leave the
-    // row to the traversal, which uses it as scratch)
-    for (int c = 0; c < nd; ++c) b.roff[(size_t)i * nd + c] = kNoRow;
-    run = b.hit_cap + 1;
+  if (over) {
+    // an overflowed target has no row: the pair passes treat its side like
+    // one beyond the rows and its sums traverse
+    b.hit_count[i] = kRowOver;
     *b.d_rover = 1;
+    return 0;
   }
   b.hit_count[i] = run;
+  return (run + 3) >> 2;
+}
+
+// Each particle's row length from its per-slot counts (a wall's row holds
+// its fluid neighbours), the row in 128-byte units for the scan, and the
+// positions' fixed-point copies for the pair kernels.  Threads up to `cap`
+// (inclusive) write c4, so that the scan's last element gives the total.
+__global__ void __launch_bounds__(256) row_count_kernel(State s, Geometry g, Consts k,
+                                                        BinScratch b, int cap) {
+  __shared__ int block_sum;
+  if (threadIdx.x == 0) block_sum = 0;
+  __syncthreads();
+  const int n = *b.d_n;
+  const int i = blockIdx.x * 256 + threadIdx.x;
+  const int c4 = i < n ? row_count_body(s, g, k, b, i) : 0;
+  if (i <= cap) b.c4[i] = c4;
+  // the exact total (64-bit) beside the scan's int32 one
+  const int ws = __reduce_add_sync(0xffffffffu, c4);
+  if ((threadIdx.x & 31) == 0 && ws) atomicAdd(&block_sum, ws);
+  __syncthreads();
+  if (threadIdx.x == 0 && block_sum) atomicAdd(b.d_rowsum, (unsigned long long)block_sum);
+}
+
+// Each segment's absolute first entry from the row's start (row_base, the
+// scan of c4) and the per-slot counts, in place.  Rows beyond row_cap: every
+// target traverses this pass (the pair list's overflow flag) and the host,
+// which reads need_host between passes, grows the rows.  The fit is decided
+// on the exact 64-bit total; when it fits (row_cap < 2^32 entries), the
+// int32 scan cannot have wrapped.
+__global__ void __launch_bounds__(256) row_offsets_kernel(Geometry g, BinScratch b) {
+  const int n = *b.d_n;
+  const int i = blockIdx.x * 256 + threadIdx.x;
+  if (i >= n) return;
+  const unsigned long long total = 4ull * *b.d_rowsum;
+  if (total > (unsigned long long)b.row_cap) {
+    if (i == 0) {
+      *b.d_pover = 1;
+      if (b.need_host && *b.need_host < total) *b.need_host = total;
+    }
+    return;
+  }
+  const int nd = g.n_diff;
+  unsigned* seg = b.rseg + (size_t)i * nd;
+  if (b.hit_count[i] == kRowOver) {
+    for (int c = 0; c < nd; ++c) seg[c] = kNoRow;
+    return;
+  }
+  unsigned off = 4u * __ldg(&b.row_base[i]);  // < row_cap < 2^32
+  for (int c = 0; c < nd; ++c) {
+    const unsigned cnt = seg[c];
+    seg[c] = off;
+    off += cnt;
+  }
 }
 
 // The force records (FxRec) of every particle from the SoA state: the
@@ -421,15 +477,14 @@ __global__ void __launch_bounds__(256) frec_build_kernel(State s, BinScratch b) 
 
 // The FP64 evaluation of the listed pairs into the rows (PH 0: density,
 // 1: force).  Threads stride over the list.  A side writes its entry only
-// when its target is fluid and has a row (walls and overflowed targets have
-// none); every entry is written whole.
+// when its target has a row (overflowed targets have none) and, in the force
+// pass, is fluid; every entry is written whole.
 template <int DIM, int PH>
 __global__ void __launch_bounds__(256, PH == 0 ? 6 : 5) pair_list_kernel(State s, Geometry g, Consts k,
                                                         BinScratch b, int threads_total) {
   if (*b.d_pover) return;  // every target traverses
   const long long np = (long long)*b.d_npairs;
   const int nd = g.n_diff;
-  const size_t cap = (size_t)b.hit_cap;
   int av = 0;
   for (long long e = (long long)blockIdx.x * 256 + threadIdx.x; e < np; e += threads_total) {
     const int p = __ldg(&b.pair_p[e]);
@@ -437,18 +492,18 @@ __global__ void __launch_bounds__(256, PH == 0 ? 6 : 5) pair_list_kernel(State s
     const unsigned m = __ldg(&b.pair_m[e]);
     const int c = (int)((m >> 20) & 31u);
     const bool fp = (m & kPWall) == 0u, fq = (m & kQWall) == 0u;
-    // entry positions (a rank of kRankNone, or a target without a row, lands
-    // beyond hit_cap); the density pass fills wall rows too (the wall
-    // pressure's neighbours), the force pass fluid rows only
-    const int vp = (PH == 0 || fp) ? __ldg(&b.roff[(size_t)p * nd + c]) + (int)(m & 1023u)
-                                   : b.hit_cap;
-    const int vq = (PH == 0 || fq)
-                       ? __ldg(&b.roff[(size_t)q * nd + (nd - 1 - c)]) + (int)((m >> 10) & 1023u)
-                       : b.hit_cap;
-    const bool wp = vp < b.hit_cap, wq = vq < b.hit_cap;
+    // entry positions: the segment's first entry plus the rank (a rank of
+    // kRankNone, or a target without a row, writes nothing); the density
+    // pass fills wall rows too (the wall pressure's neighbours), the force
+    // pass fluid rows only
+    const unsigned rp = m & 1023u, rq = (m >> 10) & 1023u;
+    unsigned bp = kNoRow, bq = kNoRow;
+    if ((PH == 0 || fp) && rp != kRankNone) bp = __ldg(&b.rseg[(size_t)p * nd + c]);
+    if ((PH == 0 || fq) && rq != kRankNone) bq = __ldg(&b.rseg[(size_t)q * nd + (nd - 1 - c)]);
+    const bool wp = bp != kNoRow, wq = bq != kNoRow;
     if (!wp && !wq) continue;
-    RowEntry* const ep = b.rows + (size_t)p * cap + vp;
-    RowEntry* const eq = b.rows + (size_t)q * cap + vq;
+    RowEntry* const ep = b.rows + (wp ? (size_t)bp + rp : 0);
+    RowEntry* const eq = b.rows + (wq ? (size_t)bq + rq : 0);
     const unsigned long long qbits = (unsigned)q | (fq ? 0u : 0x80000000u);
     const unsigned long long pbits = (unsigned)p | (fp ? 0u : 0x80000000u);
     if (PH == 0) {
@@ -532,8 +587,9 @@ __global__ void __launch_bounds__(256, PH == 0 ? 6 : 5) pair_list_kernel(State s
 }
 
 template <int DIM>
-void tiles_dim(cudaStream_t st, const State& s, const Geometry& g, const Consts& k,
-               const BinScratch& b, int cap, int phase) {
+cudaError_t tiles_dim(const LaunchCtx& c, const State& s, const Geometry& g, const Consts& k,
+                      const BinScratch& b, int cap, int phase) {
+  const cudaStream_t st = c.stream;
   static const int tile_wave = resident_blocks(tile_kernel<DIM>, 32 * kTileWarps);
   static const int dens_wave = resident_blocks(pair_list_kernel<DIM, 0>, 256);
   static const int force_wave = resident_blocks(pair_list_kernel<DIM, 1>, 256);
@@ -541,14 +597,22 @@ void tiles_dim(cudaStream_t st, const State& s, const Geometry& g, const Consts&
     const long long slots = (long long)b.max_items * (g.n_diff / 2 + 1);
     const int tb = (int)std::max(
         1LL, std::min<long long>((slots + kTileWarps - 1) / kTileWarps, tile_wave));
-    cudaMemsetAsync(b.d_npairs, 0, 16, st);  // pair count and overflow flags
+    // pair count, overflow flags and the rows' 64-bit total
+    cudaMemsetAsync(b.d_npairs, 0, 24, st);
     tile_kernel<DIM><<<tb, 32 * kTileWarps, 0, st>>>(s, g, k, b, tb * kTileWarps);
-    row_scan_kernel<<<(cap + 255) / 256, 256, 0, st>>>(s, g, k, b);
+    row_count_kernel<<<cap / 256 + 1, 256, 0, st>>>(s, g, k, b, cap);
+    // the rows' starts: c4[0 .. cap] -> row_base (row_base[n] = the total);
+    // the scan's launches are counted by the caller with the tile kernels
+    const LaunchCtx quiet{st, nullptr, nullptr};
+    const cudaError_t e = launch_scan(quiet, b.c4, (int*)b.row_base, cap + 1, b.pscan_tmp);
+    if (e != cudaSuccess) return e;
+    row_offsets_kernel<<<(cap + 255) / 256, 256, 0, st>>>(g, b);
     pair_list_kernel<DIM, 0><<<dens_wave, 256, 0, st>>>(s, g, k, b, dens_wave * 256);
   } else {
     frec_build_kernel<DIM><<<(cap + 255) / 256, 256, 0, st>>>(s, b);
     pair_list_kernel<DIM, 1><<<force_wave, 256, 0, st>>>(s, g, k, b, force_wave * 256);
   }
+  return cudaGetLastError();
 }
 
 // sph_arith_check's kernel: one value per thread
@@ -576,9 +640,8 @@ __global__ void arith_check_kernel(int op, int k, int n, const double* a, const 
 cudaError_t launch_tiles_fp64(const LaunchCtx& c, const State& s, const Geometry& g,
                               const Consts& k, const BinScratch& b, int cap, int phase) {
   if (cap <= 0) return cudaSuccess;
-  if (k.dim == 2) tiles_dim<2>(c.stream, s, g, k, b, cap, phase);
-  else tiles_dim<3>(c.stream, s, g, k, b, cap, phase);
-  return cudaGetLastError();
+  return k.dim == 2 ? tiles_dim<2>(c, s, g, k, b, cap, phase)
+                    : tiles_dim<3>(c, s, g, k, b, cap, phase);
 }
 
 }  // namespace sphgpu

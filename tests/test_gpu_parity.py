@@ -253,10 +253,9 @@ def test_large_2d_first_steps_bitexact(gpu, oracle_mod):
     assert_same_state(g, o, fields=("x", "v", "rho", "P", "a"))
 
 
-def test_row_overflow_bitexact(gpu, oracle_mod):
-    """3D dam break with H = 4.6 dr: interior targets have ~400 neighbours,
-    more than a row holds (384), and fall back to the traversal; targets near
-    the walls and the free surface keep their rows."""
+def test_long_rows_bitexact(gpu, oracle_mod):
+    """3D dam break with H = 4.6 dr: interior targets have ~400 neighbours
+    per row (rows are sized from the counts, so they hold them)."""
     c = G.dam_break(3, 0.1, h_factor=2.3)
     g, o = make(c, oracle_mod)
     g.init_state()
@@ -269,11 +268,11 @@ def test_row_overflow_bitexact(gpu, oracle_mod):
     g.synchronize()
 
 
-def test_pair_list_overflow_bitexact(gpu, oracle_mod):
+def test_row_segment_overflow_bitexact(gpu, oracle_mod):
     """1,000 fluid and 500 wall particles inside one cell, all within H of one
-    another: every fluid row (1,499 neighbours) overflows its 384 entries and
-    the step's pair list (~5e5 pairs listed) overflows its capacity (192 per
-    particle), so every target takes the traversal."""
+    another: every fluid row has a segment of 1,499 neighbours, more than a
+    10-bit rank addresses (1,022), so every row is marked overflowed and
+    every target takes the traversal."""
     rng = np.random.default_rng(3)
     nf, nw = 1000, 500
     n = nf + nw
@@ -296,6 +295,36 @@ def test_pair_list_overflow_bitexact(gpu, oracle_mod):
         g.step(1)
         assert g.pair_count(reset=True) == o.step(1)
     assert_same_state(g, o)
+    g.synchronize()
+
+
+@pytest.mark.parametrize("dim,dr", [(2, 0.04), (3, 0.08)])
+def test_rows_grow_when_the_flow_needs_more(gpu, oracle_mod, dim, dr):
+    """The FP64 rows are sized from the counts of the first density pass
+    (which traverses, having none).  A flow that packs its particles closer
+    needs more entries than the rows hold: that pass traverses instead
+    (results unchanged), reports the shortfall, and the rows grow before
+    the next pass -- inside sph_step's captured step graph too, which is then
+    captured again.  Bit-exact with the oracle throughout."""
+    c = G.dam_break(dim, dr)
+    g, o = make(c, oracle_mod)
+    g.init_state()
+    assert g.pair_count(reset=True) == o.init_state()
+    used0 = g.memory_usage()
+    st = o.state()
+    x = st["x"].copy()
+    fl = st["type"] == G.FLUID
+    x0 = x[fl, :dim].min(axis=0)
+    x[fl, :dim] = x0 + 0.85 * (x[fl, :dim] - x0)  # about 1/0.85^dim the neighbours
+    g.set("x", x)
+    o.set_state(x=x)
+    g.step(1)  # its density pass overflows and traverses
+    assert g.pair_count(reset=True) == o.step(1)
+    assert_same_state(g, o)
+    g.step(6)  # the step graph: the rows grow first, then it is captured again
+    assert g.pair_count(reset=True) == o.step(6)
+    assert_same_state(g, o)
+    assert g.memory_usage() > used0
     g.synchronize()
 
 

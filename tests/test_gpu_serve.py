@@ -53,6 +53,11 @@ def test_served_results_equal_alone(gpu, device_lattice):
 
 
 def test_usage_matches_estimate(gpu):
+    """Mixed precision: the estimate is the exact allocation.  FP64: the rows
+    are sized from the counts of the first density pass; the estimate (a
+    full lattice neighbourhood for every particle) bounds them on a dam
+    break, and the device's own free memory agrees with the usage."""
+    import torch
     r = Request(0, 3, 0.07, 2, sphgpu.MIXED, 0.0)
     c = r.case()
     g = sphgpu.ParticleSystem(c.params, r.precision)
@@ -63,4 +68,21 @@ def test_usage_matches_estimate(gpu):
     assert g.memory_usage() == sphgpu.memory_estimate(c.params, c.n, r.precision)
     g.synchronize()
     assert g.idle()
+    g.close()
+    r = Request(1, 3, 0.04, 2, sphgpu.FP64, 0.0)
+    c = r.case()
+    est = sphgpu.memory_estimate(c.params, c.n, r.precision)
+    torch.cuda.synchronize()
+    free0 = torch.cuda.mem_get_info()[0]
+    g = sphgpu.ParticleSystem(c.params, r.precision)
+    g.upload(c.x, c.v, type=c.type)
+    g.init_state()
+    g.step(6)
+    g.synchronize()
+    used = g.memory_usage()
+    assert 0 < used <= est
+    # cudaMalloc rounds each allocation up to its page size; the context may
+    # reserve local memory for the kernels on their first launch
+    taken = free0 - torch.cuda.mem_get_info()[0]
+    assert used <= taken <= used + 512 * 2**20
     g.close()
