@@ -104,13 +104,15 @@ def parse():
     ap.add_argument("--ens-steps", type=int, default=1000)
     ap.add_argument("--ens-seed", type=int, default=2024)
     # served stream of solve requests (continuous batching, HBM budget)
-    ap.add_argument("--serve-requests", type=int, default=24)
-    ap.add_argument("--serve-rate", type=float, default=1.0, help="arrivals per second")
+    ap.add_argument("--serve-requests", type=int, default=100)
+    ap.add_argument("--serve-rate", type=float, default=2.0, help="arrivals per second")
     ap.add_argument("--serve-min-particles", type=float, default=5e3)
-    ap.add_argument("--serve-max-particles", type=float, default=2e5)
+    ap.add_argument("--serve-max-particles", type=float, default=2e6)
     ap.add_argument("--serve-seed", type=int, default=5)
-    ap.add_argument("--serve-budget-frac", type=float, default=0.8,
+    ap.add_argument("--serve-budget-frac", type=float, default=0.15,
                     help="HBM budget as a fraction of the device memory free at start")
+    ap.add_argument("--serve-max-wait", type=float, default=20.0,
+                    help="aging bound of the skip-ahead admission (seconds)")
     ap.add_argument("--only", choices=["all", "ensemble", "serve"], default="all")
     return ap.parse_args()
 
@@ -446,25 +448,36 @@ def run_ensemble(args, torch, dev):
 def run_served(args, torch, dev):
     """A seeded Poisson stream of dam-break solve requests served with
     continuous batching under an HBM budget."""
+    import sphgpu
     from sphgpu.serve import Server, request_stream, summarize
-    free, total = torch.cuda.mem_get_info(dev)
+    free, total = sphgpu.device_memory(dev)
     budget = int(args.serve_budget_frac * free)
     reqs = request_stream(args.serve_requests, args.serve_rate, seed=args.serve_seed,
                           n_lo=args.serve_min_particles, n_hi=args.serve_max_particles)
-    srv = Server(budget, max_slots=64, chunk=10, device=dev)
+    srv = Server(budget, max_slots=64, chunk=10, device=dev, max_wait_s=args.serve_max_wait)
     t0 = time.perf_counter()
-    done = srv.run(reqs)
+    with ClockSampler(dev) as clk:
+        done = srv.run(reqs)
     makespan = time.perf_counter() - t0
     out = summarize(done, makespan)
+    n = np.array([r.n for r in done])
     out.update({
         "workload": (f"{len(reqs)} requests, Poisson arrivals at {args.serve_rate:g}/s (seed "
                      f"{args.serve_seed}): 2D or 3D dam break, particles log-uniform in "
                      f"[{args.serve_min_particles:g}, {args.serve_max_particles:g}], steps U[200, "
                      "2000], FP64 or mixed"),
-        "budget_bytes": budget, "hbm_total_bytes": int(total),
-        "peak_admitted_bytes": srv.peak_bytes, "peak_concurrent": srv.peak_slots,
+        "particles": {"min": int(n.min()), "median": int(np.median(n)), "max": int(n.max())},
+        "budget_bytes": budget, "hbm_free_at_start": int(free), "hbm_total_bytes": int(total),
+        "peak_admitted_bytes": srv.peak_bytes,
+        "peak_admitted_frac": srv.peak_bytes / budget,
+        "peak_device_bytes": srv.peak_device_bytes,
+        "peak_concurrent": srv.peak_slots,
+        "admission": {"skipped_ahead": srv.skipped_ahead, "aging_holds": srv.aged,
+                      "max_wait_s": args.serve_max_wait},
+        "pools": {"rebuilds": srv.pool_rebuilds, "peak_members": srv.pool_peak_members},
         "latency": "arrival to final fields (x, v, rho, P) on the host",
         "mean_queue_s": float(np.mean([r.admitted - r.arrival for r in done])),
+        "clocks": clk.summary(),
     })
     return out
 

@@ -311,6 +311,13 @@ int sph_shape_count(int device, int dim, const sph_shape* shapes, int count, int
 int sph_memory_estimate(const sph_params* params, int64_t n, uint64_t* bytes);
 int sph_memory_usage(const sph_system* sys, uint64_t* bytes);
 int sph_query(sph_system* sys, int* idle);
+/* The temporary device bytes sph_generate / sph_shape_count allocate (and
+ * free before returning) for these shapes: one word per point of the largest
+ * shape's bounding lattice plus scan scratch; host arithmetic only. */
+int sph_generate_scratch(int dim, const sph_shape* shapes, int count, uint64_t* bytes);
+/* cudaMemGetInfo of `device`: the bytes free and in total (what a server
+ * compares its admitted budget with). */
+int sph_device_memory(int device, uint64_t* free_bytes, uint64_t* total_bytes);
 
 /* ---- batched ensembles (no reference counterpart)
  *
@@ -344,6 +351,9 @@ int sph_batch_stats(sph_batch* batch, int64_t* kernels_per_graph, int64_t* graph
                     int64_t* kernels);
 /* the stream the graph is launched on (a cudaStream_t) */
 int sph_batch_stream(sph_batch* batch, void** stream);
+/* *idle = 1 when everything queued by the batch and by its members has
+ * finished, 0 otherwise (never waits). */
+int sph_batch_query(sph_batch* batch, int* idle);
 
 /* ---- allocation-free cell-list build (no counterpart in the reference)
  *

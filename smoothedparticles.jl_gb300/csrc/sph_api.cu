@@ -764,6 +764,50 @@ static int shapes_run(int dim, const sph_shape* shapes, int count, cudaStream_t 
   return rc;
 }
 
+// The temporary device bytes shapes_run allocates for these shapes (host
+// arithmetic only; the same expressions as shapes_run).
+static int shapes_scratch(int dim, const sph_shape* shapes, int count, size_t* out) {
+  long long maxp = 0, maxo = 0;
+  for (int i = 0; i < count; ++i) {
+    LatticeShape ls;
+    std::vector<double> offs;
+    if (lattice_prepare(shapes[i], dim, ls, offs) != SPH_OK) return SPH_ERR_ARG;
+    const long long np = lattice_points(ls);
+    if (np > 0x7fffffffLL - 4096) return SPH_ERR_ARG;
+    maxp = std::max(maxp, np);
+    maxo = std::max(maxo, (long long)offs.size());
+  }
+  const size_t scan_ints = scan_tmp_ints((int)(maxp + 1)) + 64;
+  *out = 8 * (size_t)(maxp + 1) + 4 * scan_ints + 8 * (size_t)(maxo + 3) + 1024;
+  return SPH_OK;
+}
+
+int sph_generate_scratch(int dim, const sph_shape* shapes, int count, uint64_t* bytes) {
+  if (!bytes || count < 0 || (count > 0 && !shapes) || (dim != 2 && dim != 3)) return SPH_ERR_ARG;
+  size_t b = 0;
+  const int rc = shapes_scratch(dim, shapes, count, &b);
+  if (rc == SPH_OK) *bytes = (uint64_t)b;
+  return rc;
+}
+
+int sph_device_memory(int device, uint64_t* free_bytes, uint64_t* total_bytes) {
+  if (!free_bytes || !total_bytes) return SPH_ERR_ARG;
+  int ndev = 0;
+  if (cudaGetDeviceCount(&ndev) != cudaSuccess || device < 0 || device >= ndev) {
+    cudaGetLastError();
+    return SPH_ERR_CUDA;
+  }
+  DeviceGuard guard(device);
+  size_t f = 0, t = 0;
+  if (cudaMemGetInfo(&f, &t) != cudaSuccess) {
+    cudaGetLastError();
+    return SPH_ERR_CUDA;
+  }
+  *free_bytes = (uint64_t)f;
+  *total_bytes = (uint64_t)t;
+  return SPH_OK;
+}
+
 int sph_shape_count(int device, int dim, const sph_shape* shapes, int count, int64_t* n_out) {
   if (!n_out || count < 0 || (count > 0 && !shapes) || (dim != 2 && dim != 3)) return SPH_ERR_ARG;
   int ndev = 0;
@@ -1575,6 +1619,25 @@ int sph_batch_stats(sph_batch* b, int64_t* kernels_per_graph, int64_t* graph_lau
   if (kernels_per_graph) *kernels_per_graph = b->kernels_per_graph;
   if (graph_launches) *graph_launches = b->graph_launches;
   if (kernels) *kernels = b->launches;
+  return SPH_OK;
+}
+
+int sph_batch_query(sph_batch* b, int* idle) {
+  if (!b || !idle) return SPH_ERR_ARG;
+  DeviceGuard guard(b->device);
+  int all = 1;
+  std::vector<cudaStream_t> streams{b->origin};
+  for (auto* m : b->members) streams.push_back(m->stream);
+  for (cudaStream_t st : streams) {
+    const cudaError_t e = cudaStreamQuery(st);
+    if (e == cudaErrorNotReady) {
+      all = 0;
+    } else if (e != cudaSuccess) {
+      cudaGetLastError();
+      return bfail(b, SPH_ERR_CUDA, "stream query failed");
+    }
+  }
+  *idle = all;
   return SPH_OK;
 }
 

@@ -359,6 +359,13 @@ class Batch:
         self._check(self._lib.sph_batch_stream(self._h, C.byref(p)))
         return p.value or 0
 
+    def idle(self) -> bool:
+        """True when everything the batch and its members queued has
+        finished (never waits)."""
+        i = C.c_int()
+        self._check(self._lib.sph_batch_query(self._h, C.byref(i)))
+        return bool(i.value)
+
     def stats(self) -> dict:
         a, b_, c = C.c_int64(), C.c_int64(), C.c_int64()
         self._check(self._lib.sph_batch_stats(self._h, C.byref(a), C.byref(b_), C.byref(c)))
@@ -459,9 +466,35 @@ def shape_count(dim: int, shapes, device: int = 0) -> int:
     return n.value
 
 
+def generate_scratch(dim: int, shapes) -> int:
+    """Temporary device bytes the device generator allocates for ``shapes``
+    while it runs (host-side arithmetic)."""
+    lib = L.load()
+    arr = L.make_shapes(shapes)
+    b = C.c_uint64()
+    rc = lib.sph_generate_scratch(int(dim), arr, len(shapes), C.byref(b))
+    if rc != 0:
+        raise SphError(rc, "sph_generate_scratch: invalid shape")
+    return b.value
+
+
+def device_memory(device: int = 0) -> tuple:
+    """(free, total) device bytes (cudaMemGetInfo)."""
+    lib = L.load()
+    f, t = C.c_uint64(), C.c_uint64()
+    rc = lib.sph_device_memory(int(device), C.byref(f), C.byref(t))
+    if rc != 0:
+        raise SphError(rc, "sph_device_memory failed (no CUDA device)")
+    return f.value, t.value
+
+
 def memory_estimate(params: dict, n: int, precision: int = FP64) -> int:
     """Device bytes a system with these parameters holds with n particles
-    (host-side arithmetic, no GPU needed)."""
+    (host-side arithmetic, no GPU needed).  Mixed precision: the exact
+    allocation.  FP64: the rows are sized at the first density pass from
+    the counts; the estimate gives them a full lattice neighbourhood per
+    particle, an upper bound for a dam break (a clustering flow can need
+    more)."""
     lib = L.load()
     p = L.make_params(L.sph_params, params, precision)
     b = C.c_uint64()

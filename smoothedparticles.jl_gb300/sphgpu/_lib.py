@@ -193,6 +193,9 @@ PROTOTYPES = {
     "sph_batch_set_fused": (C.c_int, [_P, C.c_int]),
     "sph_batch_set_tuning": (C.c_int, [_P, C.c_int]),
     "sph_memory_estimate": (C.c_int, [C.POINTER(sph_params), _I64, C.POINTER(C.c_uint64)]),
+    "sph_generate_scratch": (C.c_int, [C.c_int, _P, C.c_int, C.POINTER(C.c_uint64)]),
+    "sph_device_memory": (C.c_int, [C.c_int, C.POINTER(C.c_uint64), C.POINTER(C.c_uint64)]),
+    "sph_batch_query": (C.c_int, [_P, C.POINTER(C.c_int)]),
     "sph_memory_usage": (C.c_int, [_P, C.POINTER(C.c_uint64)]),
     "sph_query": (C.c_int, [_P, C.POINTER(C.c_int)]),
     "sph_assemble_matrix": (C.c_int, [_P, C.c_int, C.c_double, C.POINTER(_P)]),

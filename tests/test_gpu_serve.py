@@ -21,28 +21,41 @@ def alone(r, fields):
     return out
 
 
-@pytest.mark.parametrize("device_lattice", [True, False])
-def test_served_results_equal_alone(gpu, device_lattice):
+@pytest.mark.parametrize("device_lattice,pools", [(True, True), (False, True), (True, False)])
+def test_served_results_equal_alone(gpu, device_lattice, pools):
+    """Requests arriving while others run, admitted by the budget: FP64 ones
+    on their own streams, mixed ones of one dimension joining and leaving a
+    fused pool between chunks (step counts that are not multiples of the
+    chunk, so members leave and finish alone).  Every result equals the same
+    request run alone, bit for bit; the budget is never exceeded, neither by
+    the charges nor by the device memory actually taken."""
     F, M = sphgpu.FP64, sphgpu.MIXED
     reqs = [Request(0, 2, 0.04, 24, F, 0.00), Request(1, 3, 0.08, 10, M, 0.02),
             Request(2, 2, 0.03, 31, M, 0.05), Request(3, 3, 0.06, 12, F, 0.05),
             Request(4, 2, 0.05, 7, F, 0.10, col_height=1.4, alpha=0.06),
-            Request(5, 2, 0.035, 20, M, 0.12, col_height=1.1)]
-    est = []
+            Request(5, 2, 0.035, 20, M, 0.12, col_height=1.1),
+            Request(6, 2, 0.045, 26, M, 0.13, col_height=1.7),
+            Request(7, 3, 0.09, 18, M, 0.14, alpha=0.05)]
+    srv = Server(10**13, max_slots=8, chunk=4, device_lattice=device_lattice, pools=pools)
+    charges = []
     for r in reqs:
-        c = r.case()
-        est.append(sphgpu.memory_estimate(c.params, c.n, r.precision))
+        c = r.shapes() if device_lattice else r.case()
+        n = sphgpu.shape_count(r.dim, c.shapes) if device_lattice else c.n
+        charges.append(srv._charge(sphgpu, r, c, n))
     # room for the three largest together: later arrivals must wait for memory
-    budget = sum(sorted(est)[-3:])
-    srv = Server(budget, max_slots=4, chunk=4, device_lattice=device_lattice)
+    budget = sum(sorted(charges)[-3:])
+    srv.budget = budget
     t = __import__("time").perf_counter()
     done = srv.run(reqs)
     makespan = __import__("time").perf_counter() - t
     assert sorted(r.rid for r in done) == list(range(len(reqs)))
     assert srv.peak_bytes <= budget
-    assert srv.peak_slots <= 4
+    assert srv.peak_device_bytes <= budget
+    assert srv.peak_slots <= 8
+    if pools:
+        assert srv.pool_peak_members >= 2 and srv.pool_rebuilds >= 2
     for r in done:
-        assert r.bytes == est[r.rid]
+        assert r.bytes == charges[r.rid]
         assert r.admitted >= r.arrival and r.done >= r.admitted
         ref = alone(r, srv.result_fields)
         for f in srv.result_fields:
@@ -50,6 +63,8 @@ def test_served_results_equal_alone(gpu, device_lattice):
         assert r.pairs > 0
     s = summarize(done, makespan)
     assert s["requests"] == len(reqs) and s["p99_latency_s"] >= s["p50_latency_s"]
+    if pools:
+        assert s["pooled_step_frac"] > 0
 
 
 def test_usage_matches_estimate(gpu):
