@@ -186,12 +186,13 @@ struct Proc64 {
         ay = __fma_rn(cf, d1, ay);
         if (DIM == 3) az = __fma_rn(cf, fx_sep2(X2, &s.x[2][i], QX2, &s.x[2][q], k.fx_k), az);
         if ((e & 0x80000000u) == 0u) {
-          // fluid neighbour: + wx (v_q - v_p)
+          // fluid neighbour: + wx (v_q - v_p), the velocity differences on
+          // the integer pipes (isub_rn: the IEEE subtraction's result)
           double qv1, qv2;
           frec_load_v12(b.frec + q, qv1, qv2);
-          sx = __fma_rn(-wx, vp[0] - qv0, sx);
-          sy = __fma_rn(-wx, vp[1] - qv1, sy);
-          if (DIM == 3) sz = __fma_rn(-wx, vp[2] - qv2, sz);
+          sx = __fma_rn(-wx, isub_rn(vp[0], qv0), sx);
+          sy = __fma_rn(-wx, isub_rn(vp[1], qv1), sy);
+          if (DIM == 3) sz = __fma_rn(-wx, isub_rn(vp[2], qv2), sz);
           ++c0;
         } else {
           ++c1;

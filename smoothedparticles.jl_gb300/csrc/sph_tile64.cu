@@ -545,8 +545,10 @@ __global__ void __launch_bounds__(256, PH == 0 ? 6 : 5) pair_list_kernel(State s
           frec_load_v(b.frec + q, qv1, qv2, qrho, qpr);
           sp = ppr + qpr;
           rs = prho + qrho;
-          dv1 = pv1 - qv1;
-          dv2 = DIM == 3 ? pv2 - qv2 : 0.0;
+          // velocity differences on the integer pipes (isub_rn: the IEEE
+          // subtraction's result)
+          dv1 = isub_rn(pv1, qv1);
+          dv2 = DIM == 3 ? isub_rn(pv2, qv2) : 0.0;
         }
         long long PX0, PX1, PX2, QX0, QX1, QX2;
         double pv0, qv0;
@@ -554,7 +556,7 @@ __global__ void __launch_bounds__(256, PH == 0 ? 6 : 5) pair_list_kernel(State s
         frec_load_x(b.frec + q, QX0, QX1, QX2, qv0);
         const double d0 = fx_sep2(PX0, &s.x[0][p], QX0, &s.x[0][q], k.fx_k);
         const double d1 = fx_sep2(PX1, &s.x[1][p], QX1, &s.x[1][q], k.fx_k);
-        const double dv0 = pv0 - qv0;
+        const double dv0 = isub_rn(pv0, qv0);
         double vdx = __fma_rn(dv1, d1, dv0 * d0);
         if (DIM == 3) {
           const double d2 = fx_sep2(PX2, &s.x[2][p], QX2, &s.x[2][q], k.fx_k);
@@ -629,8 +631,10 @@ __global__ void arith_check_kernel(int op, int k, int n, const double* a, const 
     r = isqrt_rn(x);
   } else if (op == 2) {
     r = ircp_rn(x);
-  } else {
+  } else if (op == 3) {
     r = two_over(x);
+  } else {
+    r = isub_rn(x, b[i]);
   }
   out[i] = r;
 }
@@ -648,9 +652,9 @@ cudaError_t launch_tiles_fp64(const LaunchCtx& c, const State& s, const Geometry
 
 extern "C" int sph_arith_check(int device, int op, int k, int n, const double* a, const double* b,
                                double* out) {
-  if (n < 0 || op < 0 || op > 3) return SPH_ERR_ARG;
+  if (n < 0 || op < 0 || op > 4) return SPH_ERR_ARG;
   if (n == 0) return SPH_OK;
-  if (!a || !out || (op == 0 && !b)) return SPH_ERR_ARG;
+  if (!a || !out || ((op == 0 || op == 4) && !b)) return SPH_ERR_ARG;
   int prev = 0;
   if (cudaGetDevice(&prev) != cudaSuccess || cudaSetDevice(device) != cudaSuccess) {
     cudaGetLastError();
@@ -662,7 +666,8 @@ extern "C" int sph_arith_check(int device, int op, int k, int n, const double* a
   if (cudaMalloc(&d, 3 * bytes) != cudaSuccess) {
     rc = SPH_ERR_NOMEM;
   } else if (cudaMemcpy(d, a, bytes, cudaMemcpyHostToDevice) != cudaSuccess ||
-             (op == 0 && cudaMemcpy(d + n, b, bytes, cudaMemcpyHostToDevice) != cudaSuccess)) {
+             ((op == 0 || op == 4) &&
+              cudaMemcpy(d + n, b, bytes, cudaMemcpyHostToDevice) != cudaSuccess)) {
     rc = SPH_ERR_CUDA;
   } else {
     sphgpu::arith_check_kernel<<<(n + 255) / 256, 256>>>(op, k, n, d, d + n, d + 2 * (size_t)n);
