@@ -437,9 +437,8 @@ def run_ensemble(args, torch, dev):
         "unbatched": {"value": pairs_plain / t_plain, "ms_per_step": 1e3 * t_plain / S,
                       "note": "same members, sph_step per member on its own stream (a two-step "
                               "graph of that member alone), host timer"},
-        "autotune": {str(k): {"warps_per_block": v[0],
-                              "ms_per_step": {str(w): round(t, 4) for w, t in v[1].items()}}
-                     for k, v in sorted(table.items())},
+        "autotune": autotune.describe(table),
+        "tuned": {k: v["choice"] for k, v in autotune.describe(table).items()},
         "autotune_s": t_tune, "setup_lattices_s": t_geo, "clocks": clk.summary(),
         "l2": "no flush: resident state of all members > 129 MB L2",
     }

@@ -229,6 +229,15 @@ int sph_launch_count(sph_system* sys, int64_t* launches);
  * it; the batched ensemble's autotuner picks it per size class. */
 int sph_set_tuning(sph_system* sys, int warps_per_block);
 int sph_get_tuning(const sph_system* sys, int* warps_per_block);
+/* Threads per cell chunk of the mixed-precision pair passes (no reference
+ * counterpart): 32, 64 or 128 threads share one work item (<= 32 targets of
+ * one cell), each warp taking every 1st, 2nd or 4th 32-candidate chunk of the
+ * neighbour sequence, their FP64 sums added in warp order (default 32).  The
+ * mixed results depend on it at the FP32 level (the batches of each lane's
+ * FP32 sums change), bit-exactly reproducibly for a given setting; the FP64
+ * path ignores it.  The batched ensemble's autotuner picks it per size class. */
+int sph_set_chunk_threads(sph_system* sys, int threads);
+int sph_get_chunk_threads(const sph_system* sys, int* threads);
 
 /* ---- assemble_matrix / assemble_vector (src/core.jl:164-225) on the device
  * and the conjugate-gradient solve of the implicit example

@@ -446,6 +446,7 @@ static int setup_host(const sph_params* p, sph_system* s) {
   Consts& k = s->k;
   k.dim = p->dim;
   k.warps = 4;
+  k.split = 1;
   k.h = H;
   k.inv_h = 1.0 / H;
   const double h2 = H * H;
@@ -1240,6 +1241,22 @@ int sph_get_tuning(const sph_system* s, int* warps_per_block) {
   return SPH_OK;
 }
 
+int sph_set_chunk_threads(sph_system* s, int threads) {
+  if (!s) return SPH_ERR_ARG;
+  if (threads != 32 && threads != 64 && threads != 128)
+    return fail(s, SPH_ERR_ARG, "threads per cell chunk must be 32, 64 or 128 (got %d)", threads);
+  const int split = threads / 32;
+  if (s->k.split != split) ++s->generation;
+  s->k.split = split;
+  return SPH_OK;
+}
+
+int sph_get_chunk_threads(const sph_system* s, int* threads) {
+  if (!s || !threads) return SPH_ERR_ARG;
+  *threads = 32 * s->k.split;
+  return SPH_OK;
+}
+
 // Multiprocessors assumed by sph_memory_estimate (no CUDA call there): at
 // least the count of any single GPU of this class, so the traversal scratch
 // it adds is an upper bound.
@@ -1356,11 +1373,16 @@ static int batch_capture_fused(sph_batch* b) {
     std::swap(a.cur, a.alt);
     args[1].push_back(a);
   }
+  // the pair launches' warps per block: at least every member's split (a
+  // block holds whole items of one member)
+  int warps = b->fused_warps;
+  for (int j = 0; j < M; ++j) warps = std::max(warps, b->members[j]->k.split);
   std::vector<int2> maps[kShapeCount];
   for (int sh = 0; sh < kShapeCount; ++sh)
     for (int j = 0; j < M; ++j) {
       const sph_system* m = b->members[j];
-      const int nb = fused_blocks(sh, m->n_host, m->geo.key_max, m->b.max_items, b->fused_warps);
+      const int nb = fused_blocks(sh, m->n_host, m->geo.key_max, m->b.max_items * m->k.split,
+                                  warps);
       for (int i = 0; i < nb; ++i) maps[sh].push_back(make_int2(j, i));
     }
   size_t bytes = 2 * align_up(sizeof(MemberArgs) * M);
@@ -1389,7 +1411,7 @@ static int batch_capture_fused(sph_batch* b) {
   }
   fb.members = M;
   fb.dim = b->members[0]->params.dim;
-  fb.warps = b->fused_warps;
+  fb.warps = warps;
   cudaError_t e = cudaStreamBeginCapture(b->origin, cudaStreamCaptureModeThreadLocal);
   if (e != cudaSuccess) return bfail(b, SPH_ERR_CUDA, "cudaStreamBeginCapture failed");
   b->counted = 0;

@@ -64,6 +64,11 @@ struct Consts {
   int vaxis;
   int dim;
   int warps;  // warps per block of the pair passes (2, 4 or 8; tunable)
+  // mixed-precision pair passes: warps sharing one work item (1, 2 or 4,
+  // i.e. 32, 64 or 128 threads per cell chunk of <= 32 targets; tunable):
+  // warp s of an item takes the chunks gi = s, s + split, ... of the
+  // neighbour sequence, and the partial sums are added in warp order
+  int split;
   // FP32 candidate classification (see the pair kernels): a candidate whose
   // FP32 squared distance lies below s_lo is inside the support, above s_hi
   // outside; in between the FP64 test decides.

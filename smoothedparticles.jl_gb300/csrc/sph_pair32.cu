@@ -29,6 +29,8 @@
 // the mask capacity traverses in both passes.
 // Built with FMA contraction (the FP64 band test uses explicit intrinsics;
 // any FP32 evaluation order stays within the classification band's margin).
+#include <algorithm>
+
 #include "sph_cellwarp.cuh"
 #include "sph_launch.h"
 #include "sphgpu.h"
@@ -334,15 +336,16 @@ __device__ __forceinline__ bool mx_chunk_table(const Geometry& g, const BinScrat
 struct MxCursor {
   int gi;       // current chunk
   unsigned cm;  // its bits not yet taken
-  unsigned nm;  // mask of chunk gi + 1 (loaded ahead)
+  unsigned nm;  // mask of chunk gi + step (loaded ahead)
+  int step;     // the warps sharing the item: this warp takes every step-th chunk
 };
 
 __device__ __forceinline__ int mx_next(const unsigned* mrow, const MxShared<SPH_OP_FORCE>& sh,
                                        int nc, MxCursor& c, int& cell) {
-  while (c.cm == 0u && c.gi + 1 < nc) {
-    ++c.gi;
+  while (c.cm == 0u && c.gi + c.step < nc) {
+    c.gi += c.step;
     c.cm = c.nm;
-    if (c.gi + 1 < nc) c.nm = __ldg(mrow + (size_t)(c.gi + 1) * 32);
+    if (c.gi + c.step < nc) c.nm = __ldg(mrow + (size_t)(c.gi + c.step) * 32);
   }
   if (c.cm == 0u) return -1;
   const int u = __ffs(c.cm) - 1;
@@ -355,12 +358,13 @@ template <int DIM>
 __device__ __forceinline__ void mx_walk(const State& s, const BinScratch& b,
                                         const MxShared<SPH_OP_FORCE>& sh, int lane,
                                         const CwTarget& t, Acc32<DIM, SPH_OP_FORCE>& a, int ck,
-                                        int nc) {
+                                        int nc, int part, int split) {
   const unsigned* mrow = b.ck_mask + (size_t)ck * 32 + lane;
   MxCursor cur;
-  cur.gi = t.active ? -1 : nc;
+  cur.step = split;
+  cur.gi = t.active ? part - split : nc;
   cur.cm = 0u;
-  cur.nm = t.active && nc > 0 ? __ldg(mrow) : 0u;
+  cur.nm = t.active && part < nc ? __ldg(mrow + (size_t)part * 32) : 0u;
   int qa = -1, qb = -1, ca = 0, cb = 0;
   for (;;) {
     // take two hits per step until every lane is done or a lane with hits
@@ -389,10 +393,13 @@ __device__ __forceinline__ void mx_walk(const State& s, const BinScratch& b,
 
 // list_mode: 0 traverse; 1 traverse and store the hit masks (density
 // passes); 2 read the masks stored by the density pass of this binning.
+// The item's chunks are shared by `split` warps: this one takes the chunks
+// gi with gi % split == part.
 template <int DIM, int OP>
 __device__ __forceinline__ void mx_pass(const State& s, const Geometry& g, const Consts& k,
                                         const BinScratch& b, MxShared<OP>& sh, int lane, int item,
-                                        const CwTarget& t, Acc32<DIM, OP>& a, int list_mode) {
+                                        const CwTarget& t, Acc32<DIM, OP>& a, int list_mode,
+                                        int part, int split) {
   // this item's mask slots: the binning counted every cell's chunks
   int ck = -1, nc = 0;
   if (list_mode != 0 && b.ck_mask) {
@@ -415,7 +422,7 @@ __device__ __forceinline__ void mx_pass(const State& s, const Geometry& g, const
   __syncwarp();
   if constexpr (OP == SPH_OP_FORCE) {
     if (read && mx_chunk_table(g, b, sh, lane, t, nc)) {
-      mx_walk<DIM>(s, b, sh, lane, t, a, ck, nc);
+      mx_walk<DIM>(s, b, sh, lane, t, a, ck, nc, part, split);
       a.fold();
       return;
     }
@@ -431,6 +438,10 @@ __device__ __forceinline__ void mx_pass(const State& s, const Geometry& g, const
     const float ax = t.pi4.x - off.x, ay = t.pi4.y - off.y, az = t.pi4.z - off.z;
     for (int base = st; base < en; base += 32) {
       const int m = min(32, en - base);
+      if (split > 1 && gi % split != part) {  // another warp's chunk
+        ++gi;
+        continue;
+      }
       unsigned mask;
       if (read && gi < nc) {
         mask = t.active ? __ldg(&b.ck_mask[((size_t)ck + gi) * 32 + lane]) : 0u;
@@ -470,6 +481,62 @@ __device__ __forceinline__ void mx_pass(const State& s, const Geometry& g, const
   a.fold();
 }
 
+// The FP64 accumulators a warp of a shared item hands to the item's first
+// warp (by lane): density 1, wall pressure 3, force 6, written over the
+// warp's own staging area once its traversal is done.
+template <int OP>
+constexpr int kCombWords = (OP == SPH_OP_DENSITY || OP == SPH_OP_DENSITY_REF) ? 1
+                           : OP == SPH_OP_WALL_PRESSURE                       ? 3
+                                                                              : 6;
+
+template <int OP>
+__device__ __forceinline__ double (*comb_of(MxShared<OP>& sh))[32] {
+  static_assert(sizeof(MxShared<OP>) >= sizeof(double) * 32 * kCombWords<OP>,
+                "a warp's staging area holds its partial sums");
+  return reinterpret_cast<double (*)[32]>(&sh);
+}
+
+template <int DIM, int OP>
+__device__ __forceinline__ void comb_put(double (*c)[32], int lane, const Acc32<DIM, OP>& p) {
+  // every lane of the warp has left the staging area (the caller syncs)
+  if (OP == SPH_OP_DENSITY || OP == SPH_OP_DENSITY_REF) {
+    c[0][lane] = p.acc;
+  } else if (OP == SPH_OP_WALL_PRESSURE) {
+    c[0][lane] = p.wp;
+    c[1][lane] = p.wg;
+    c[2][lane] = p.ws;
+  } else {
+    c[0][lane] = p.ax;
+    c[1][lane] = p.ay;
+    c[2][lane] = p.az;
+    c[3][lane] = p.sx;
+    c[4][lane] = p.sy;
+    c[5][lane] = p.sz;
+  }
+}
+
+template <int DIM, int OP>
+__device__ __forceinline__ void comb_add(const double (*c)[32], int lane, Acc32<DIM, OP>& p) {
+  if (OP == SPH_OP_DENSITY || OP == SPH_OP_DENSITY_REF) {
+    p.acc += c[0][lane];
+  } else if (OP == SPH_OP_WALL_PRESSURE) {
+    p.wp += c[0][lane];
+    p.wg += c[1][lane];
+    p.ws += c[2][lane];
+  } else {
+    p.ax += c[0][lane];
+    p.ay += c[1][lane];
+    p.az += c[2][lane];
+    p.sx += c[3][lane];
+    p.sy += c[4][lane];
+    p.sz += c[5][lane];
+  }
+}
+
+// One work item (<= 32 targets of one cell) per `split` warps of the block
+// (k.split: 1, 2 or 4, dividing WARPS): warp `part` of an item takes every
+// split-th chunk of the neighbour sequence, and the item's first warp adds
+// the others' FP64 sums to its own in warp order before the epilogue.
 template <int DIM, int OP, int WARPS>
 __device__ __forceinline__ void pair32_body(const State& s, const Geometry& g, const Consts& k,
                                             const BinScratch& b, int self, int reset,
@@ -477,11 +544,14 @@ __device__ __forceinline__ void pair32_body(const State& s, const Geometry& g, c
                                             MxShared<OP>* shared) {
   const int lane = threadIdx.x & 31;
   const int w = threadIdx.x >> 5;
-  const int item = blk * WARPS + w;
+  const int split = k.split;  // block-uniform
+  const int item = blk * (WARPS / split) + w / split;
+  const int part = w % split;
   int first = 0, count = 0;
-  if (!cw_item(b, g, item, first, count)) return;  // warp-uniform
+  const bool has = cw_item(b, g, item, first, count);  // warp-uniform
+  if (split == 1 && !has) return;  // no barriers below when the item is one warp's
   const int i = first + lane;
-  const bool valid = lane < count;
+  const bool valid = has && lane < count;
   const int ti = valid ? s.type[i] : -1;
   const int want = OP == SPH_OP_WALL_PRESSURE ? kWall : kFluid;
   CwTarget t;
@@ -495,7 +565,7 @@ __device__ __forceinline__ void pair32_body(const State& s, const Geometry& g, c
   t.xp[2] = (DIM == 3 && valid) ? s.x[2][i] : 0.0;
   Acc32<DIM, OP> p(k);
   p.pi4 = t.pi4;
-  if (t.active) {
+  if (t.active && part == 0) {
     if (OP == SPH_OP_DENSITY) {
       if (!reset) p.acc = s.rho[i];
     } else if (OP == SPH_OP_DENSITY_REF) {
@@ -506,13 +576,25 @@ __device__ __forceinline__ void pair32_body(const State& s, const Geometry& g, c
         p.sx = s.xs[0][i]; p.sy = s.xs[1][i];
         if (DIM == 3) { p.az = s.a[2][i]; p.sz = s.xs[2][i]; }
       }
-      float4 r0;
-      ld_rec(s.rec + 2 * i, r0, p.vp);
-      p.rhop = fabsf(r0.w);
     }
   }
+  if (OP == SPH_OP_FORCE && t.active) {
+    float4 r0;
+    ld_rec(s.rec + 2 * i, r0, p.vp);
+    p.rhop = fabsf(r0.w);
+  }
   if (__any_sync(0xffffffffu, t.active))
-    mx_pass<DIM, OP>(s, g, k, b, shared[w], lane, item, t, p, list_mode);
+    mx_pass<DIM, OP>(s, g, k, b, shared[w], lane, item, t, p, list_mode, part, split);
+  if (split > 1) {
+    // the other warps' sums to the item's first warp, added in warp order
+    __syncwarp();
+    if (part > 0) comb_put<DIM, OP>(comb_of(shared[w]), lane, p);
+    __syncthreads();
+    if (part == 0)
+      for (int o = 1; o < split; ++o) comb_add<DIM, OP>(comb_of(shared[w + o]), lane, p);
+    cw_count<OP>(b, p.c0, p.c1, p.c2);
+    if (part > 0 || !has) return;
+  }
   if (valid && !t.active) {
     if (reset) {
       if (OP == SPH_OP_DENSITY) {
@@ -562,7 +644,7 @@ __device__ __forceinline__ void pair32_body(const State& s, const Geometry& g, c
       }
     }
   }
-  cw_count<OP>(b, p.c0, p.c1, p.c2);
+  if (split == 1) cw_count<OP>(b, p.c0, p.c1, p.c2);
 }
 
 // The force pass (latency bound on its record gathers) runs at 8 blocks of 4
@@ -636,8 +718,9 @@ template <int DIM>
 cudaError_t launch_dim(const LaunchCtx& c, const State& s, const Geometry& g, const Consts& k,
                        const BinScratch& b, int cap, int op, int self, int reset, int fuse_eos,
                        int aux_fresh, int list_mode) {
-  const int W = k.warps;
-  const int blocks = (b.max_items + W - 1) / W;
+  // a block holds whole items: at least `split` warps
+  const int W = std::max(k.warps, k.split);
+  const int blocks = (int)(((long long)b.max_items * k.split + W - 1) / W);
   if (!aux_fresh && (op == SPH_OP_FORCE || op == SPH_OP_WALL_PRESSURE)) {
     mark(c, SPH_KERNEL_UNARY, 0);
     aux_refresh_kernel<DIM><<<(cap + 255) / 256, 256, 0, c.stream>>>(s, b);

@@ -306,6 +306,16 @@ class ParticleSystem:
         self._check(self._lib.sph_get_tuning(self._h, C.byref(w)))
         return w.value
 
+    def set_chunk_threads(self, threads: int):
+        """Threads per cell chunk of the mixed pair passes (32, 64 or 128);
+        mixed results change at the FP32 level, reproducibly per setting."""
+        self._check(self._lib.sph_set_chunk_threads(self._h, int(threads)))
+
+    def chunk_threads(self) -> int:
+        t = C.c_int()
+        self._check(self._lib.sph_get_chunk_threads(self._h, C.byref(t)))
+        return t.value
+
     def pair_stats(self, reset: bool = False) -> dict:
         """Hits per category: density, wall (pressure pass), force_fluid,
         force_wall, force_av."""

@@ -182,6 +182,8 @@ PROTOTYPES = {
                                   C.c_void_p]),
     "sph_cell_list_noalloc": (C.c_int, [C.POINTER(sph_params), _I64, _P, _P, _P, _P]),
     "sph_set_tuning": (C.c_int, [_P, C.c_int]),
+    "sph_set_chunk_threads": (C.c_int, [_P, C.c_int]),
+    "sph_get_chunk_threads": (C.c_int, [_P, C.POINTER(C.c_int)]),
     "sph_get_tuning": (C.c_int, [_P, C.POINTER(C.c_int)]),
     "sph_batch_create": (C.c_int, [C.POINTER(_P), C.c_int, C.POINTER(_P)]),
     "sph_batch_destroy": (C.c_int, [_P]),

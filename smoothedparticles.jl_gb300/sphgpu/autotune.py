@@ -1,24 +1,31 @@
-"""Autotuner of the pair-pass launch shape for batched ensembles.
+"""Autotuner of the pair passes' launch shape for batched ensembles.
 
-The knob is the number of warps per block of the pair passes (2, 4 or 8, i.e.
-64, 128 or 256 threads; each warp owns up to 32 targets of one cell, so this
-sets how many cell chunks share a block's shared memory and scheduling slot).
-Results never depend on it, only the speed does.
+Two knobs:
+
+* warps per block of the pair passes (2, 4 or 8, i.e. 64, 128 or 256
+  threads): how many work items (<= 32 targets of one cell each) share a
+  block's shared memory and scheduling slot.  Results never depend on it.
+* threads per cell chunk of the mixed-precision passes (32, 64 or 128): how
+  many warps share one work item, each taking every 1st, 2nd or 4th
+  32-candidate chunk of the neighbour sequence.  More threads per item give
+  a small member more warps in flight and split long hit lists; the mixed
+  results change at the FP32 level (reproducibly per setting).
 
 * Fused batches (mixed-precision members of one dimension: every kernel of
-  the step is one launch over all members) have one setting for the whole
-  launch; the tuner times the batched graph with each choice.
-* Otherwise every member runs its own launches and is tuned by size class
-  (powers of two of the particle count).  A small member stepped alone is
-  bound by launch latency, so each class's settings are timed where they run:
-  inside the batched graph, with every other class held at its current choice
-  (one sweep of coordinate descent, classes largest first).
+  the step is one launch over all members) have one warps-per-block setting
+  for the whole launch, then threads per chunk per size class (powers of two
+  of the particle count), each class timed inside the batched graph with
+  every other class held at its current choice (one sweep of coordinate
+  descent, classes largest first).
+* Otherwise every member runs its own launches and is tuned by size class the
+  same way (warps per block; threads per chunk for mixed members).
 """
 from __future__ import annotations
 
 import math
 
 CHOICES = (2, 4, 8)
+THREADS = (32, 64, 128)
 
 
 def size_class(n: int) -> int:
@@ -27,26 +34,35 @@ def size_class(n: int) -> int:
 
 def _time(batch, steps: int) -> float:
     """Milliseconds per step of `batch` (graph captured outside the timed
-    region)."""
-    import torch
+    region), timed on the batch's stream with the library's own clock-free
+    means: host time around a synchronised run of `steps` steps."""
+    import time
     batch.step(2)
     batch.synchronize()
-    st = torch.cuda.ExternalStream(batch.stream())
-    e0 = torch.cuda.Event(enable_timing=True)
-    e1 = torch.cuda.Event(enable_timing=True)
-    e0.record(st)
+    t0 = time.perf_counter()
     batch.step(steps)
-    e1.record(st)
-    e1.synchronize()
-    return e0.elapsed_time(e1) / steps
+    batch.synchronize()
+    return 1e3 * (time.perf_counter() - t0) / steps
 
 
-def tune_batch(systems, steps: int = 4, choices=CHOICES) -> dict:
-    """Chooses warps per block by timing the batched graph; steps the systems
-    (their states advance).  Returns {"fused": (warps, {warps: ms})} for a
-    fused batch, else {size_class: (warps, {warps: ms})} with every system set
-    to its class's choice."""
+def _classes(systems):
+    classes = {}
+    for g in systems:
+        classes.setdefault(size_class(g.n), []).append(g)
+    weight = {c: sum(g.n for g in gs) for c, gs in classes.items()}
+    return classes, sorted(classes, key=lambda c: -weight[c])
+
+
+def tune_batch(systems, steps: int = 4, choices=CHOICES, threads=THREADS) -> dict:
+    """Chooses the launch shape by timing the batched graph; steps the systems
+    (their states advance).  Returns {"fused": (warps, {warps: ms}),
+    ("threads", size_class): (threads, {threads: ms}), ...} for a fused batch,
+    else {size_class: (warps, {warps: ms}), ("threads", size_class): ...}, with
+    every system set to its class's choices."""
     import sphgpu
+    classes, order = _classes(systems)
+    mixed = {c for c in order if all(g.precision == sphgpu.MIXED for g in classes[c])}
+    table = {}
     b = sphgpu.Batch(systems)
     try:
         if b.fused:
@@ -56,39 +72,61 @@ def tune_batch(systems, steps: int = 4, choices=CHOICES) -> dict:
                 times[w] = _time(b, steps)
             best = min(times, key=times.get)
             b.set_tuning(best)
-            return {"fused": (best, times)}
+            table["fused"] = (best, times)
+            for c in order:
+                tt = {}
+                for t in threads:
+                    for g in classes[c]:
+                        g.set_chunk_threads(t)
+                    tt[t] = _time(b, steps)
+                bt = min(tt, key=tt.get)
+                for g in classes[c]:
+                    g.set_chunk_threads(bt)
+                table[("threads", c)] = (bt, tt)
+            return table
     finally:
         b.close()
-    classes = {}
-    for g in systems:
-        classes.setdefault(size_class(g.n), []).append(g)
-    weight = {c: sum(g.n for g in gs) for c, gs in classes.items()}
-    table = {}
-    for c in sorted(classes, key=lambda c: -weight[c]):
-        times = {}
-        for w in choices:
+    for c in order:
+        knobs = [("warps", choices)] + ([("threads", threads)] if c in mixed else [])
+        for knob, values in knobs:
+            times = {}
+            for v in values:
+                for g in classes[c]:
+                    g.set_tuning(v) if knob == "warps" else g.set_chunk_threads(v)
+                bb = sphgpu.Batch(systems)
+                try:
+                    times[v] = _time(bb, steps)
+                finally:
+                    bb.close()
+            best = min(times, key=times.get)
             for g in classes[c]:
-                g.set_tuning(w)
-            bb = sphgpu.Batch(systems)
-            try:
-                times[w] = _time(bb, steps)
-            finally:
-                bb.close()
-        best = min(times, key=times.get)
-        for g in classes[c]:
-            g.set_tuning(best)
-        table[c] = (best, times)
+                g.set_tuning(best) if knob == "warps" else g.set_chunk_threads(best)
+            table[c if knob == "warps" else ("threads", c)] = (best, times)
     return table
 
 
 def apply(systems, table: dict, batch=None):
-    """Sets the tuning from a table: the fused setting on `batch`, else every
-    system's from the table of its size class."""
-    if "fused" in table:
-        if batch is not None:
-            batch.set_tuning(table["fused"][0])
-        return
+    """Sets the tuning from a table: the fused setting on `batch`, every
+    system's warps and threads per chunk from the entries of its size class."""
+    if "fused" in table and batch is not None:
+        batch.set_tuning(table["fused"][0])
     for g in systems:
-        entry = table.get(size_class(g.n))
-        if entry is not None:
+        c = size_class(g.n)
+        entry = table.get(c)
+        if entry is not None and "fused" not in table:
             g.set_tuning(entry[0])
+        th = table.get(("threads", c))
+        if th is not None:
+            g.set_chunk_threads(th[0])
+
+
+def describe(table: dict) -> dict:
+    """The table as plain JSON: per size class (particles 2^c .. 2^(c+1)) the
+    choices and the timings behind them."""
+    out = {}
+    for k, (best, times) in table.items():
+        key = k if isinstance(k, str) else (f"threads@2^{k[1]}" if isinstance(k, tuple)
+                                            else f"warps@2^{k}")
+        out[key] = {"choice": best, "ms_per_step": {str(v): round(t, 4) for v, t in times.items()},
+                    "spread": round(max(times.values()) / min(times.values()) - 1.0, 4)}
+    return out

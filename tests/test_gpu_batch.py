@@ -181,3 +181,48 @@ def test_fused_equals_branches_and_alone(gpu):
     fp = sphgpu.Batch([make(cases[0], sphgpu.FP64)])
     with pytest.raises(sphgpu.SphError):
         fp.set_fused(True)         # FP64 members step as graph branches
+
+
+def test_chunk_threads_accuracy_and_batch_identity(gpu):
+    """Threads per cell chunk (32/64/128 threads sharing a work item) of the
+    mixed passes: the pair set is unchanged (pair counts equal the FP64
+    path's), the fields stay within the mixed path's stated bounds of FP64
+    (test_gpu_mixed.py), and a fused batch whose members use different
+    settings gives each member's fields exactly as stepping it alone."""
+    cases = [G.dam_break(2, 0.03), G.dam_break(2, 0.045, col_height=1.4, alpha=0.05),
+             G.dam_break(2, 0.025, col_height=1.8)]
+    g64 = make(cases[0], sphgpu.FP64)
+    g64.step(6)
+    for threads in (64, 128):
+        g = sphgpu.ParticleSystem(cases[0].params, sphgpu.MIXED)
+        g.set_chunk_threads(threads)
+        assert g.chunk_threads() == threads
+        g.upload(cases[0].x, cases[0].v, type=cases[0].type)
+        g.init_state()
+        g.step(6)
+        assert g.pair_count() == g64.pair_count()
+        dx = np.abs(g.get("x") - g64.get("x")).max()
+        rho = np.abs(g.get("rho") / g64.get("rho") - 1.0).max()
+        assert dx / cases[0].dr <= 1e-6 and rho <= 1e-6, (threads, dx, rho)
+        g.close()
+    settings = (32, 64, 128)
+
+    def member(c, t):
+        g = sphgpu.ParticleSystem(c.params, sphgpu.MIXED)
+        g.set_chunk_threads(t)
+        g.upload(c.x, c.v, type=c.type)
+        g.init_state()
+        return g
+    mem = [member(c, t) for c, t in zip(cases, settings)]
+    ref = [member(c, t) for c, t in zip(cases, settings)]
+    b = sphgpu.Batch(mem)
+    assert b.fused
+    b.set_tuning(2)  # the launch grows to hold the 128-thread member's items
+    for nsteps in (4, 3, 6):
+        b.step(nsteps)
+        for r in ref:
+            r.step(nsteps)
+        b.synchronize()
+        for m, r in zip(mem, ref):
+            assert_equal(m, r)
+    b.close()

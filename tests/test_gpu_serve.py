@@ -30,20 +30,23 @@ def test_served_results_equal_alone(gpu, device_lattice, pools):
     request run alone, bit for bit; the budget is never exceeded, neither by
     the charges nor by the device memory actually taken."""
     F, M = sphgpu.FP64, sphgpu.MIXED
+    # the 2D mixed requests 2, 5 and 6 arrive together (one pool; they leave
+    # at different chunks), request 8 joins them a little later
     reqs = [Request(0, 2, 0.04, 24, F, 0.00), Request(1, 3, 0.08, 10, M, 0.02),
-            Request(2, 2, 0.03, 31, M, 0.05), Request(3, 3, 0.06, 12, F, 0.05),
+            Request(2, 2, 0.03, 61, M, 0.05), Request(3, 3, 0.06, 12, F, 0.05),
             Request(4, 2, 0.05, 7, F, 0.10, col_height=1.4, alpha=0.06),
-            Request(5, 2, 0.035, 20, M, 0.12, col_height=1.1),
-            Request(6, 2, 0.045, 26, M, 0.13, col_height=1.7),
-            Request(7, 3, 0.09, 18, M, 0.14, alpha=0.05)]
-    srv = Server(10**13, max_slots=8, chunk=4, device_lattice=device_lattice, pools=pools)
+            Request(5, 2, 0.035, 42, M, 0.05, col_height=1.1),
+            Request(6, 2, 0.045, 26, M, 0.05, col_height=1.7),
+            Request(7, 3, 0.09, 18, M, 0.14, alpha=0.05),
+            Request(8, 2, 0.04, 30, M, 0.052, col_height=1.3)]
+    srv = Server(10**13, max_slots=9, chunk=4, device_lattice=device_lattice, pools=pools)
     charges = []
     for r in reqs:
         c = r.shapes() if device_lattice else r.case()
         n = sphgpu.shape_count(r.dim, c.shapes) if device_lattice else c.n
         charges.append(srv._charge(sphgpu, r, c, n))
-    # room for the three largest together: later arrivals must wait for memory
-    budget = sum(sorted(charges)[-3:])
+    # room for the four largest together: later arrivals may wait for memory
+    budget = sum(sorted(charges)[-4:])
     srv.budget = budget
     t = __import__("time").perf_counter()
     done = srv.run(reqs)
@@ -51,7 +54,7 @@ def test_served_results_equal_alone(gpu, device_lattice, pools):
     assert sorted(r.rid for r in done) == list(range(len(reqs)))
     assert srv.peak_bytes <= budget
     assert srv.peak_device_bytes <= budget
-    assert srv.peak_slots <= 8
+    assert srv.peak_slots <= 9
     if pools:
         assert srv.pool_peak_members >= 2 and srv.pool_rebuilds >= 2
     for r in done:
