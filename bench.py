@@ -421,6 +421,7 @@ def run_ensemble(args, torch, dev):
     n = [c.n for c in cases]
     for g in mem:
         g.close()
+    floor = chain_floor(args, torch, dev, len(cases), bst["kernels_per_graph"] // 2)
     return {
         "workload": (f"{len(cases)} independent 2D dam breaks (seed {args.ens_seed}): dr U[0.004, "
                      "0.02], column height U[1, 2], alpha U[0.01, 0.1]; mixed precision"),
@@ -441,7 +442,42 @@ def run_ensemble(args, torch, dev):
         "tuned": {k: v["choice"] for k, v in autotune.describe(table).items()},
         "autotune_s": t_tune, "setup_lattices_s": t_geo, "clocks": clk.summary(),
         "l2": "no flush: resident state of all members > 129 MB L2",
+        "chain_floor": dict(floor, share_of_step=round(floor["ms_per_step"] / (ms / S), 4)),
     }
+
+
+def chain_floor(args, torch, dev, members, kernels_per_step, steps=200):
+    """The same fused graph (the step's chain of kernels, one launch each over
+    all members) on `members` tiny dam breaks (dr = 0.1: ~300 particles each):
+    what the chain costs when the kernels have next to nothing to do -- the
+    most that fusing the whole step into one persistent launch could save."""
+    import sphgpu
+    sy = []
+    for j in range(members):
+        c = __import__("sphgpu.geometry", fromlist=["dam_break"]).dam_break(
+            2, 0.1, col_height=1.0 + (j % 5) * 0.2, name=f"tiny{j}")
+        g = sphgpu.ParticleSystem(c.params, sphgpu.MIXED, device=dev)
+        g.upload(c.x, c.v, type=c.type)
+        g.init_state()
+        sy.append(g)
+    b = sphgpu.Batch(sy)
+    b.step(4)
+    b.synchronize()
+    st = torch.cuda.ExternalStream(b.stream(), device=dev)
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record(st)
+    b.step(steps)
+    e1.record(st)
+    e1.synchronize()
+    ms = e0.elapsed_time(e1) / steps
+    kps = b.stats()["kernels_per_graph"] // 2
+    parts = sum(g.n for g in sy)
+    b.close()
+    for g in sy:
+        g.close()
+    return {"members": members, "particles_total": parts, "ms_per_step": ms,
+            "kernels_per_step": kps, "us_per_kernel": round(1e3 * ms / max(kps, 1), 3)}
 
 
 def run_served(args, torch, dev):

@@ -35,3 +35,27 @@ def test_collision_circles():
     # two mirror-image circles: equal halves
     assert c.n % 2 == 0
     assert (c.v[: c.n // 2, 0] == 1.0).all() and (c.v[c.n // 2:, 0] == -1.0).all()
+
+
+# tests/test_geometry.jl restated for the shapes and grids this library
+# generates (square and cubic grids): the covering's particle count times the
+# cell area (volume) of a grid of spacing 1/N, N = 200, against the shape's
+# area (volume), within the test's tolerances rtol_2d = 0.01, rtol_3d = 0.03
+# (test_geometry.jl:6-11, :17-45).  The reference covers the rectangle with
+# its hexagonal grid; here it is covered with the square grid.
+N = 200
+
+
+def test_geometry_area_circle():
+    x = G.circle(2, 1.0 / N, 0.0, 0.0, 1.0)           # test_geometry.jl:66-68
+    assert abs(x.shape[0] / N ** 2 / 3.141592653589793 - 1.0) < 0.01
+
+
+def test_geometry_area_rectangle():
+    x = G.fill_box(2, 1.0 / N, G.rectangle(0.0, -1.0, 2.0, 5.0))  # :70-72
+    assert abs(x.shape[0] / N ** 2 / 12.0 - 1.0) < 0.01
+
+
+def test_geometry_volume_box():
+    x = G.fill_box(3, 1.0 / N, G.box3(-0.7, -0.6, -0.5, 0.7, 0.6, 0.5))  # :118-120
+    assert abs(x.shape[0] / N ** 3 / (1.4 * 1.2 * 1.0) - 1.0) < 0.03
