@@ -168,6 +168,8 @@ size_t carve(sph_system* s, char* base, size_t C) {
     b.ck_cap = (int)(cap < 0x3ffffffLL * 16 ? cap : 0x3ffffffLL * 16);
     b.ck_mask = (unsigned*)take(4 * 32 * (size_t)b.ck_cap);
     b.hit_count = nullptr;
+    b.wall_list = nullptr;
+    b.wall_cap = 0;
     b.row_base = nullptr;
     b.c4 = nullptr;
     b.rseg = nullptr;
@@ -182,12 +184,15 @@ size_t carve(sph_system* s, char* base, size_t C) {
     // row length and start, the per-slot segment offsets, the positions'
     // fixed-point copies and the force records
     b.hit_count = (int*)take(4 * C);
+    b.wall_list = (int*)take(4 * C);
+    b.wall_cap = (int)C;
     b.row_base = (unsigned*)take(4 * (C + 1));
     b.c4 = (int*)take(4 * (C + 1));
     b.pscan_tmp = (int*)take(4 * (scan_tmp_ints((int)C + 1) + 64));
     for (int d = 0; d < 3; ++d) b.xfix[d] = d < D ? (long long*)take(8 * C) : nullptr;
     b.frec = (FxRec*)take(sizeof(FxRec) * C);  // 256-byte aligned start
     b.rseg = (unsigned*)take(4 * (size_t)s->geo.n_diff * C);
+    b.rseg_stride = (int)C;
     // the traversal's hit lists: one slot per warp of its persistent grid,
     // about one warp per 32 particles up to a full device (64 warps per SM)
     b.trav_slots = (int)std::min<size_t>(C / 32 + 64, 64 * (size_t)s->sms);
@@ -594,6 +599,7 @@ int sph_create(const sph_params* p, int device, sph_system** out) {
   s->b.d_pover = (int*)(c + 1288);
   s->b.d_rover = (int*)(c + 1292);
   s->b.d_rowsum = (unsigned long long*)(c + 1296);
+  s->b.d_nwall = (int*)(c + 1304);
   s->d_debug = (int*)(c + 1536);
   s->b.work_ctr = (int*)(c + 1600);
   if (cudaMemsetAsync(cells, 0, bytes, s->stream) != cudaSuccess ||
@@ -1412,6 +1418,8 @@ static int batch_capture_fused(sph_batch* b) {
   fb.members = M;
   fb.dim = b->members[0]->params.dim;
   fb.warps = warps;
+  fb.split = 0;
+  for (int j = 0; j < M; ++j) fb.split |= b->members[j]->k.split > 1 ? 1 : 0;
   cudaError_t e = cudaStreamBeginCapture(b->origin, cudaStreamCaptureModeThreadLocal);
   if (e != cudaSuccess) return bfail(b, SPH_ERR_CUDA, "cudaStreamBeginCapture failed");
   b->counted = 0;

@@ -159,7 +159,8 @@ struct BinScratch {
   // entry 4 * row_base[i] of `rows` (every row padded to a multiple of four
   // entries, 128 bytes).  The row is split into one segment per
   // neighbour-cell slot c (key_diff order): the tile kernel counts each
-  // segment's hits into rseg[i * n_diff + c], the row scan turns the counts
+  // segment's hits into rseg[c * rseg_stride + i] (slot-major, so that the
+  // passes over the particles read and write it coalesced), the row scan turns the counts
   // into the segments' absolute first entries (sph_tile64.cu).  A row that
   // cannot be used (a segment of more than kSegMax hits, a neighbour cell of
   // more than 65535 particles) has hit_count kRowOver and its target
@@ -170,6 +171,7 @@ struct BinScratch {
   unsigned* row_base;   // cap + 1: exclusive prefix of c4 (row starts / 4)
   int* c4;              // cap + 1: (hit_count + 3) / 4, 0 for rows not used
   unsigned* rseg;       // n_diff per particle: hits per slot, then first entries
+  int rseg_stride;      // particles per slot of rseg (the arena's capacity)
   int* hit_count;
   // the largest row total a pass needed beyond row_cap (host-mapped memory,
   // read by the host to grow the rows between passes)
@@ -195,6 +197,13 @@ struct BinScratch {
   // with the pair count and the flags), so that an int32 scan that wrapped
   // is never trusted
   unsigned long long* d_rowsum;
+  // walls of the current cells (the density pass's row count lists them):
+  // wall_list[0 .. d_nwall[0]) the walls with fluid neighbours in their rows,
+  // wall_list[cap - 1 - j], j < d_nwall[1], the walls without (follows
+  // d_rowsum: cleared with it)
+  int* d_nwall;
+  int* wall_list;
+  int wall_cap;
   int* cell_fluid;    // key_max + 3: fluid particles per cell
   // mixed-precision passes: one 32-bit hit mask per lane and 32-candidate
   // chunk of the neighbour sequence (sph_pair32.cu); item j of cell k owns
@@ -209,6 +218,10 @@ constexpr int kSegMax = 1022;        // hits of one row segment a rank can addre
 constexpr int kRowOver = 0x7fffffff; // hit_count of a row that is not used
 constexpr unsigned kNoRow = 0xffffffffu;
 constexpr int kTravCap = 256;        // entries of a traversal hit list
+
+__host__ __device__ __forceinline__ size_t rseg_at(const BinScratch& b, int i, int c) {
+  return (size_t)c * (size_t)b.rseg_stride + (size_t)i;
+}
 
 // Upper bound of the work-list length for n particles (every cell with
 // particles contributes ceil(c/32) <= c/32 + 1 items).
@@ -468,78 +481,6 @@ __device__ __forceinline__ double fx_diff(long long Xp, long long Xq, int k) {
   // to the exponent field one below the leading one's places it exactly
   return __longlong_as_double((long long)((neg & 0x8000000000000000ull) +
                                           ((unsigned long long)(L - k + 1022) << 52) + m));
-}
-
-// ---- FP64 subtraction on the integer pipes ---------------------------------
-// a - b correctly rounded (round to nearest, ties to even), formed with
-// integer instructions: the textbook floating-point addition of sign-magnitude
-// operands -- align the smaller significand to the larger one's exponent with
-// three extra bits (guard, round, sticky), add or subtract, normalise by at
-// most one place right or any number of places left (a left shift of more than
-// one place only happens when the exponents differ by at most one, and then
-// the difference is exact), round from the three extra bits (IEEE 754-2008,
-// 6.3; Muller et al., Handbook of Floating-Point Arithmetic, the chapter on
-// floating-point addition).  Zero operands are handled in line (with IEEE's
-// signs of zero); subnormal, infinite and NaN operands, and results that
-// would be subnormal or overflow, take the FP64 instruction out of line.
-static __device__ __noinline__ double isub_fallback(double a, double b) { return a - b; }
-
-__device__ __forceinline__ double isub_rn(double a, double b) {
-  const unsigned long long A = (unsigned long long)__double_as_longlong(a);
-  // x + y with y = -b
-  const unsigned long long B = (unsigned long long)__double_as_longlong(b) ^ 0x8000000000000000ull;
-  const unsigned long long MA = A & 0x7fffffffffffffffull, MB = B & 0x7fffffffffffffffull;
-  if (MB == 0ull) {
-    // x + (+-0): x, except -0 + +0 = +0
-    if (MA != 0ull) return a;
-    return __longlong_as_double((long long)(A & B));  // -0 only when both are -0
-  }
-  if (MA == 0ull) return __longlong_as_double((long long)B);  // +-0 - b = -b
-  // the larger magnitude first
-  const bool swap = MB > MA;
-  const unsigned long long X = swap ? B : A, Y = swap ? A : B;
-  const int ex = (int)((X >> 52) & 0x7ff), ey = (int)((Y >> 52) & 0x7ff);
-  if (ey == 0 || ex == 0x7ff) return isub_fallback(a, b);  // subnormal / inf / NaN
-  const unsigned long long mx = ((X & 0xfffffffffffffull) | (1ull << 52)) << 3;
-  const unsigned long long my0 = ((Y & 0xfffffffffffffull) | (1ull << 52)) << 3;
-  const int d = ex - ey;
-  unsigned long long my;
-  if (d == 0) {
-    my = my0;
-  } else if (d < 56) {
-    my = (my0 >> d) | ((my0 & ((1ull << d) - 1ull)) != 0ull ? 1ull : 0ull);
-  } else {
-    my = 1ull;  // only the sticky bit
-  }
-  unsigned long long s;
-  int e = ex;
-  if ((X ^ Y) >> 63) {
-    s = mx - my;
-    if (s == 0ull) return 0.0;  // exact cancellation: +0
-    const int lz = __clzll((long long)s) - 8;  // leading one to bit 55
-    if (lz > 0) {
-      s <<= lz;
-      e -= lz;
-    }
-  } else {
-    s = mx + my;
-    if (s >> 56) {
-      s = (s >> 1) | (s & 1ull);
-      ++e;
-    }
-  }
-  // round from the three extra bits, ties to even
-  const unsigned long long rb = s & 7ull;
-  unsigned long long m = s >> 3;
-  if (rb > 4ull || (rb == 4ull && (m & 1ull))) ++m;
-  if (m >> 53) {
-    m >>= 1;
-    ++e;
-  }
-  if (e <= 0 || e >= 0x7ff) return isub_fallback(a, b);  // subnormal or infinite result
-  return __longlong_as_double((long long)((X & 0x8000000000000000ull) |
-                                          ((unsigned long long)e << 52) |
-                                          (m & 0xfffffffffffffull)));
 }
 
 // The FP64 subtraction for positions without exact copies, out of line so

@@ -70,6 +70,7 @@ struct FusedBatch {
   int members;
   int dim;
   int warps;  // warps per block of the fused pair passes (2, 4 or 8)
+  int split;  // some member shares its work items between warps (chunk threads > 32)
 };
 
 // Blocks of each shape for one member (the single-system launch grids).

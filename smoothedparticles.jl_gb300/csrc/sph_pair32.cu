@@ -299,6 +299,46 @@ __device__ __forceinline__ void mx_resolve(const State& s, const Consts& k, cons
   }
 }
 
+// The density pass's hits of one chunk (bits of `mask`, candidates staged in
+// sh.c0) for a target at (ax, ay, az) relative to their cell: the shape
+// t^4 (5 - 4t), t = max(1 - r/h, 0), of two hits per packed FP32x2 pass
+// (the square roots one by one), added to f0 in hit order.
+template <int DIM, int OP>
+__device__ __forceinline__ void mx_density_hits(const MxShared<OP>& sh, const Consts& k,
+                                                unsigned mask, float ax, float ay, float az,
+                                                float& f0) {
+  const unsigned long long axp = f2_pack(ax, ax), ayp = f2_pack(ay, ay), azp = f2_pack(az, az);
+  const unsigned long long invh = f2_pack(k.inv_hf, k.inv_hf);
+  const unsigned long long one = f2_pack(1.f, 1.f), five = f2_pack(5.f, 5.f);
+  const unsigned long long m4 = f2_pack(-4.f, -4.f);
+  while (mask) {
+    const int u1 = __ffs(mask) - 1;
+    mask &= mask - 1u;
+    const bool two = mask != 0u;
+    const int u2 = two ? __ffs(mask) - 1 : u1;
+    if (two) mask &= mask - 1u;
+    const float4 q1 = sh.c0[u1], q2 = sh.c0[u2];
+    const unsigned long long dx = f2_sub(axp, f2_pack(q1.x, q2.x));
+    const unsigned long long dy = f2_sub(ayp, f2_pack(q1.y, q2.y));
+    unsigned long long ss = f2_fma(dy, dy, f2_mul(dx, dx));
+    if (DIM == 3) {
+      const unsigned long long dz = f2_sub(azp, f2_pack(q1.z, q2.z));
+      ss = f2_fma(dz, dz, ss);
+    }
+    const float s1 = __uint_as_float((unsigned)ss), s2 = __uint_as_float((unsigned)(ss >> 32));
+    const unsigned long long r = f2_pack(fsqrt(s1), fsqrt(s2));
+    const unsigned long long tt = f2_sub(one, f2_mul(r, invh));  // 1 - r/h
+    // 0 beyond the support (x > 1)
+    const unsigned long long t =
+        f2_pack(fmaxf(__uint_as_float((unsigned)tt), 0.f),
+                fmaxf(__uint_as_float((unsigned)(tt >> 32)), 0.f));
+    const unsigned long long t2 = f2_mul(t, t);
+    const unsigned long long w = f2_mul(f2_mul(t2, t2), f2_fma(m4, t, five));
+    f0 += __uint_as_float((unsigned)w);
+    if (two) f0 += __uint_as_float((unsigned)(w >> 32));
+  }
+}
+
 // Force pass over stored masks: the chunk table of the item (first candidate
 // and neighbour-cell number of every chunk, in traversal order).  False when
 // it does not match the slots the binning counted or does not fit.
@@ -427,7 +467,8 @@ __device__ __forceinline__ void mx_pass(const State& s, const Geometry& g, const
       return;
     }
   }
-  int gi = 0;  // chunk number in the item's neighbour sequence
+  int gi = 0;         // chunk number in the item's neighbour sequence
+  int mine = part;    // the next chunk this warp takes
   for (int c = 0; c < g.n_diff; ++c) {
     const int nk = t.key + g.key_diff[c];
     if (nk < 1 || nk > g.key_max) continue;  // core.jl:98
@@ -438,9 +479,12 @@ __device__ __forceinline__ void mx_pass(const State& s, const Geometry& g, const
     const float ax = t.pi4.x - off.x, ay = t.pi4.y - off.y, az = t.pi4.z - off.z;
     for (int base = st; base < en; base += 32) {
       const int m = min(32, en - base);
-      if (split > 1 && gi % split != part) {  // another warp's chunk
-        ++gi;
-        continue;
+      if (split > 1) {
+        if (gi != mine) {  // another warp's chunk
+          ++gi;
+          continue;
+        }
+        mine += split;
       }
       unsigned mask;
       if (read && gi < nc) {
@@ -469,12 +513,18 @@ __device__ __forceinline__ void mx_pass(const State& s, const Geometry& g, const
         a.nh += hits;
         a.c0 += hits;
       }
-      while (mask) {
-        const int u = __ffs(mask) - 1;
-        mask &= mask - 1u;
-        float4 vq = make_float4(0.f, 0.f, 0.f, 0.f);
-        if constexpr (MxShared<OP>::kRec) vq = sh.c1[u];
-        a.hit_rel(sh.c0[u], vq, ax, ay, az);
+      if constexpr (OP == SPH_OP_DENSITY || OP == SPH_OP_DENSITY_REF) {
+        // the density's kernel shape for two hits per packed FP32x2
+        // evaluation, added to the batch in hit order
+        mx_density_hits<DIM>(sh, k, mask, ax, ay, az, a.f0);
+      } else {
+        while (mask) {
+          const int u = __ffs(mask) - 1;
+          mask &= mask - 1u;
+          float4 vq = make_float4(0.f, 0.f, 0.f, 0.f);
+          if constexpr (MxShared<OP>::kRec) vq = sh.c1[u];
+          a.hit_rel(sh.c0[u], vq, ax, ay, az);
+        }
       }
     }
   }
@@ -537,16 +587,18 @@ __device__ __forceinline__ void comb_add(const double (*c)[32], int lane, Acc32<
 // (k.split: 1, 2 or 4, dividing WARPS): warp `part` of an item takes every
 // split-th chunk of the neighbour sequence, and the item's first warp adds
 // the others' FP64 sums to its own in warp order before the epilogue.
-template <int DIM, int OP, int WARPS>
+// SPLIT = false compiles the one-warp-per-item code alone (its registers).
+template <int DIM, int OP, int WARPS, bool SPLIT>
 __device__ __forceinline__ void pair32_body(const State& s, const Geometry& g, const Consts& k,
                                             const BinScratch& b, int self, int reset,
                                             int fuse_eos, int list_mode, int blk,
                                             MxShared<OP>* shared) {
   const int lane = threadIdx.x & 31;
   const int w = threadIdx.x >> 5;
-  const int split = k.split;  // block-uniform
-  const int item = blk * (WARPS / split) + w / split;
-  const int part = w % split;
+  const int split = SPLIT ? k.split : 1;  // block-uniform: 1, 2 or 4
+  const int lg = split >> 1;  // log2(split)
+  const int item = (blk * WARPS + w) >> lg;
+  const int part = w & (split - 1);
   int first = 0, count = 0;
   const bool has = cw_item(b, g, item, first, count);  // warp-uniform
   if (split == 1 && !has) return;  // no barriers below when the item is one warp's
@@ -652,31 +704,36 @@ __device__ __forceinline__ void pair32_body(const State& s, const Geometry& g, c
 template <int OP, int WARPS>
 constexpr int kMinBlocks32 = (OP == SPH_OP_FORCE && WARPS == 4) ? 8 : 0;
 
-template <int DIM, int OP, int WARPS>
+template <int DIM, int OP, int WARPS, bool SPLIT>
 __global__ void __launch_bounds__(32 * WARPS, kMinBlocks32<OP, WARPS>) pair32_kernel(State s, Geometry g, Consts k,
                                                             BinScratch b, int self, int reset,
                                                             int fuse_eos, int list_mode) {
   __shared__ MxShared<OP> shared[WARPS];
-  pair32_body<DIM, OP, WARPS>(s, g, k, b, self, reset, fuse_eos, list_mode, blockIdx.x, shared);
+  pair32_body<DIM, OP, WARPS, SPLIT>(s, g, k, b, self, reset, fuse_eos, list_mode, blockIdx.x,
+                                     shared);
 }
 
 // fused batches: block i works on map[i] = (member, block of that member)
-template <int DIM, int OP, int WARPS>
+template <int DIM, int OP, int WARPS, bool SPLIT>
 __global__ void __launch_bounds__(32 * WARPS) pair32_fused_kernel(
     const MemberArgs* __restrict__ margs, const int2* __restrict__ map, int self, int reset,
     int fuse_eos, int list_mode) {
   __shared__ MxShared<OP> shared[WARPS];
   const int2 e = map[blockIdx.x];
   const MemberArgs& m = margs[e.x];
-  pair32_body<DIM, OP, WARPS>(m.cur, m.g, m.k, m.b, self, reset, fuse_eos, list_mode, e.y,
-                              shared);
+  pair32_body<DIM, OP, WARPS, SPLIT>(m.cur, m.g, m.k, m.b, self, reset, fuse_eos, list_mode, e.y,
+                                     shared);
 }
 
 template <int DIM, int OP, int WARPS>
 void fused_launch(const FusedBatch& fb, int p, cudaStream_t st, int self, int reset, int fuse_eos,
                   int list_mode) {
-  pair32_fused_kernel<DIM, OP, WARPS><<<(unsigned)fb.blocks[kShapeItems], 32 * WARPS, 0, st>>>(
-      fb.args[p], fb.map[kShapeItems], self, reset, fuse_eos, list_mode);
+  if (fb.split)
+    pair32_fused_kernel<DIM, OP, WARPS, true><<<(unsigned)fb.blocks[kShapeItems], 32 * WARPS, 0, st>>>(
+        fb.args[p], fb.map[kShapeItems], self, reset, fuse_eos, list_mode);
+  else
+    pair32_fused_kernel<DIM, OP, WARPS, false><<<(unsigned)fb.blocks[kShapeItems], 32 * WARPS, 0, st>>>(
+        fb.args[p], fb.map[kShapeItems], self, reset, fuse_eos, list_mode);
 }
 
 template <int DIM, int OP>
@@ -714,6 +771,18 @@ cudaError_t launch_fused_dim(const LaunchCtx& c, const FusedBatch& fb, int p, in
   return cudaGetLastError();
 }
 
+template <int DIM, int OP, int WARPS>
+void p32_launch(bool split, int blocks, cudaStream_t st, const State& s, const Geometry& g,
+                const Consts& k, const BinScratch& b, int self, int reset, int fuse_eos,
+                int list_mode) {
+  if (split)
+    pair32_kernel<DIM, OP, WARPS, true><<<blocks, 32 * WARPS, 0, st>>>(s, g, k, b, self, reset,
+                                                                        fuse_eos, list_mode);
+  else
+    pair32_kernel<DIM, OP, WARPS, false><<<blocks, 32 * WARPS, 0, st>>>(s, g, k, b, self, reset,
+                                                                         fuse_eos, list_mode);
+}
+
 template <int DIM>
 cudaError_t launch_dim(const LaunchCtx& c, const State& s, const Geometry& g, const Consts& k,
                        const BinScratch& b, int cap, int op, int self, int reset, int fuse_eos,
@@ -721,6 +790,7 @@ cudaError_t launch_dim(const LaunchCtx& c, const State& s, const Geometry& g, co
   // a block holds whole items: at least `split` warps
   const int W = std::max(k.warps, k.split);
   const int blocks = (int)(((long long)b.max_items * k.split + W - 1) / W);
+  const bool sp = k.split > 1;
   if (!aux_fresh && (op == SPH_OP_FORCE || op == SPH_OP_WALL_PRESSURE)) {
     mark(c, SPH_KERNEL_UNARY, 0);
     aux_refresh_kernel<DIM><<<(cap + 255) / 256, 256, 0, c.stream>>>(s, b);
@@ -732,24 +802,24 @@ cudaError_t launch_dim(const LaunchCtx& c, const State& s, const Geometry& g, co
   mark(c, kid, 0);
   switch (op) {
     case SPH_OP_DENSITY:
-      if (W == 2) pair32_kernel<DIM, SPH_OP_DENSITY, 2><<<blocks, 64, 0, c.stream>>>(s, g, k, b, self, reset, fuse_eos, 1);
-      else if (W == 8) pair32_kernel<DIM, SPH_OP_DENSITY, 8><<<blocks, 256, 0, c.stream>>>(s, g, k, b, self, reset, fuse_eos, 1);
-      else pair32_kernel<DIM, SPH_OP_DENSITY, 4><<<blocks, 128, 0, c.stream>>>(s, g, k, b, self, reset, fuse_eos, 1);
+      if (W == 2) p32_launch<DIM, SPH_OP_DENSITY, 2>(sp, blocks, c.stream, s, g, k, b, self, reset, fuse_eos, 1);
+      else if (W == 8) p32_launch<DIM, SPH_OP_DENSITY, 8>(sp, blocks, c.stream, s, g, k, b, self, reset, fuse_eos, 1);
+      else p32_launch<DIM, SPH_OP_DENSITY, 4>(sp, blocks, c.stream, s, g, k, b, self, reset, fuse_eos, 1);
       break;
     case SPH_OP_DENSITY_REF:
-      if (W == 2) pair32_kernel<DIM, SPH_OP_DENSITY_REF, 2><<<blocks, 64, 0, c.stream>>>(s, g, k, b, self, reset, 0, 1);
-      else if (W == 8) pair32_kernel<DIM, SPH_OP_DENSITY_REF, 8><<<blocks, 256, 0, c.stream>>>(s, g, k, b, self, reset, 0, 1);
-      else pair32_kernel<DIM, SPH_OP_DENSITY_REF, 4><<<blocks, 128, 0, c.stream>>>(s, g, k, b, self, reset, 0, 1);
+      if (W == 2) p32_launch<DIM, SPH_OP_DENSITY_REF, 2>(sp, blocks, c.stream, s, g, k, b, self, reset, 0, 1);
+      else if (W == 8) p32_launch<DIM, SPH_OP_DENSITY_REF, 8>(sp, blocks, c.stream, s, g, k, b, self, reset, 0, 1);
+      else p32_launch<DIM, SPH_OP_DENSITY_REF, 4>(sp, blocks, c.stream, s, g, k, b, self, reset, 0, 1);
       break;
     case SPH_OP_WALL_PRESSURE:
-      if (W == 2) pair32_kernel<DIM, SPH_OP_WALL_PRESSURE, 2><<<blocks, 64, 0, c.stream>>>(s, g, k, b, 0, 0, 0, 0);
-      else if (W == 8) pair32_kernel<DIM, SPH_OP_WALL_PRESSURE, 8><<<blocks, 256, 0, c.stream>>>(s, g, k, b, 0, 0, 0, 0);
-      else pair32_kernel<DIM, SPH_OP_WALL_PRESSURE, 4><<<blocks, 128, 0, c.stream>>>(s, g, k, b, 0, 0, 0, 0);
+      if (W == 2) p32_launch<DIM, SPH_OP_WALL_PRESSURE, 2>(sp, blocks, c.stream, s, g, k, b, 0, 0, 0, 0);
+      else if (W == 8) p32_launch<DIM, SPH_OP_WALL_PRESSURE, 8>(sp, blocks, c.stream, s, g, k, b, 0, 0, 0, 0);
+      else p32_launch<DIM, SPH_OP_WALL_PRESSURE, 4>(sp, blocks, c.stream, s, g, k, b, 0, 0, 0, 0);
       break;
     default:
-      if (W == 2) pair32_kernel<DIM, SPH_OP_FORCE, 2><<<blocks, 64, 0, c.stream>>>(s, g, k, b, self, reset, 0, list_mode);
-      else if (W == 8) pair32_kernel<DIM, SPH_OP_FORCE, 8><<<blocks, 256, 0, c.stream>>>(s, g, k, b, self, reset, 0, list_mode);
-      else pair32_kernel<DIM, SPH_OP_FORCE, 4><<<blocks, 128, 0, c.stream>>>(s, g, k, b, self, reset, 0, list_mode);
+      if (W == 2) p32_launch<DIM, SPH_OP_FORCE, 2>(sp, blocks, c.stream, s, g, k, b, self, reset, 0, list_mode);
+      else if (W == 8) p32_launch<DIM, SPH_OP_FORCE, 8>(sp, blocks, c.stream, s, g, k, b, self, reset, 0, list_mode);
+      else p32_launch<DIM, SPH_OP_FORCE, 4>(sp, blocks, c.stream, s, g, k, b, self, reset, 0, list_mode);
       break;
   }
   mark(c, kid, 1);

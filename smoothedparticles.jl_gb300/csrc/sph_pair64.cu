@@ -186,13 +186,12 @@ struct Proc64 {
         ay = __fma_rn(cf, d1, ay);
         if (DIM == 3) az = __fma_rn(cf, fx_sep2(X2, &s.x[2][i], QX2, &s.x[2][q], k.fx_k), az);
         if ((e & 0x80000000u) == 0u) {
-          // fluid neighbour: + wx (v_q - v_p), the velocity differences on
-          // the integer pipes (isub_rn: the IEEE subtraction's result)
+          // fluid neighbour: + wx (v_q - v_p)
           double qv1, qv2;
           frec_load_v12(b.frec + q, qv1, qv2);
-          sx = __fma_rn(-wx, isub_rn(vp[0], qv0), sx);
-          sy = __fma_rn(-wx, isub_rn(vp[1], qv1), sy);
-          if (DIM == 3) sz = __fma_rn(-wx, isub_rn(vp[2], qv2), sz);
+          sx = __fma_rn(-wx, vp[0] - qv0, sx);
+          sy = __fma_rn(-wx, vp[1] - qv1, sy);
+          if (DIM == 3) sz = __fma_rn(-wx, vp[2] - qv2, sz);
           ++c0;
         } else {
           ++c1;
@@ -371,94 +370,32 @@ __global__ void __launch_bounds__(256, 5) row_sum_kernel(State s, Consts k, BinS
 }
 
 // The wall pressure of a step over the walls' rows (their fluid neighbours,
-// written by the density pass): one warp per 32 consecutive particles.  The
-// warp takes its walls that have fluid neighbours one after another; for
-// each, its lanes form the terms of 32 row entries at once (the entry, the
-// neighbour's record, the kernel value from the stored t, g . d), and lane 0
-// adds them up in the row's order -- the reference's summation order, as
-// Proc64::rows forms it.  A wall without fluid neighbours gets the empty sum
-// (P = 0).  Walls whose rows are not used (kRowOver, or every target after an
-// overflow) are left to pair64_kernel.
+// written by the density pass): one thread per wall, taken from the lists
+// the row count made -- threads [0, A) the A walls with fluid neighbours (so
+// every lane of a warp has a row to sum: the FP64 pipe, GB300's scarcest,
+// issues only for walls with work), threads [A, A + B) the walls without,
+// which get the empty sum (P = 0).  Each sum runs over the wall's row in its
+// order -- the reference's summation order, as Proc64::rows forms it.  Walls
+// whose rows are not used (kRowOver, or every target after an overflow) are
+// left to pair64_kernel.
 template <int DIM>
 __global__ void __launch_bounds__(256) wall_rows_kernel(State s, Consts k, BinScratch b) {
-  __shared__ double terms[8][3][32];
-  const unsigned full = 0xffffffffu;
-  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-  const int n = *b.d_n;
-  const int i0 = (blockIdx.x * 8 + w) * 32;
-  if (i0 >= n) return;  // warp-uniform
-  const int i = i0 + lane;
-  const bool pover = *b.d_pover != 0;
-  int cnt = 0;
-  bool use = false;
-  if (i < n && s.type[i] == kWall) {
-    cnt = __ldg(&b.hit_count[i]);
-    use = !pover && cnt != kRowOver;
-  }
-  if (use && cnt == 0) {
+  if (*b.d_pover) return;  // every wall traverses
+  const int na = b.d_nwall[0], nb = b.d_nwall[1];
+  const int t = blockIdx.x * 256 + threadIdx.x;
+  int c0 = 0;
+  if (t < na) {
+    const int i = b.wall_list[t];
+    const int cnt = __ldg(&b.hit_count[i]);
+    Proc64<DIM, SPH_OP_WALL_PRESSURE> p(s, k);
+    p.rows(b, i, cnt);
+    target_epilogue<DIM, SPH_OP_WALL_PRESSURE>(s, k, i, p, 0, 0);
+    c0 = p.c0;
+  } else if (t < na + nb) {
+    const int i = b.wall_list[b.wall_cap - 1 - (t - na)];
     s.P[i] = 0.0;
     s.Pr[i] = 0.0 / (k.rho0 * k.rho0);
     s.rho[i] = k.rho0;
-  }
-  int c0 = use ? cnt : 0;
-  unsigned todo = __ballot_sync(full, use && cnt > 0);
-  while (todo) {
-    const int j = __ffs(todo) - 1;
-    todo &= todo - 1u;
-    const int t = i0 + j;
-    const int tc = __shfl_sync(full, cnt, j);
-    const RowEntry* row = b.rows + 4 * (size_t)__ldg(&b.row_base[t]);
-    const long long X0 = __ldg(&b.xfix[0][t]), X1 = __ldg(&b.xfix[1][t]);
-    const long long X2 = DIM == 3 ? __ldg(&b.xfix[2][t]) : 0;
-    double wp = 0.0, wg = 0.0, ws = 0.0;
-    for (int e0 = 0; e0 < tc; e0 += 32) {
-      const int m = min(32, tc - e0);
-      double tw = 0.0, ta = 0.0, tb = 0.0;
-      bool ok = false;
-      if (lane < m) {
-        const RowEntry en = row_load(row + e0 + lane);
-        const int q = (int)(en.q & 0x7fffffffu);
-        ok = q < n;
-        if (ok) {
-          const double tt = en.c;  // ker_t of the stored distance
-          const double t2 = tt * tt;
-          tw = (k.cw * (t2 * t2)) * __fma_rn(-4.0, tt, 5.0);
-          // q's position half of its record (written by the density pass)
-          long long QX0, QX1, QX2;
-          double qv0;
-          frec_load_x(b.frec + q, QX0, QX1, QX2, qv0);
-          const double d0 = fx_sep2(X0, &s.x[0][t], QX0, &s.x[0][q], k.fx_k);
-          const double d1 = fx_sep2(X1, &s.x[1][t], QX1, &s.x[1][q], k.fx_k);
-          double gd = __fma_rn(k.g[1], d1, k.g[0] * d0);
-          if (DIM == 3) gd = __fma_rn(k.g[2], fx_sep2(X2, &s.x[2][t], QX2, &s.x[2][q], k.fx_k), gd);
-          ta = __ldg(&s.P[q]);
-          tb = __ldg(&s.rho[q]) * gd;
-        }
-      }
-      // an entry the tile passes did not write: reported, skipped
-      const unsigned valid = __ballot_sync(full, ok);
-      if (lane == 0 && __popc(valid) != m) atomicOr(b.d_err, kErrBounds);
-      terms[w][0][lane] = tw;
-      terms[w][1][lane] = ta;
-      terms[w][2][lane] = tb;
-      __syncwarp();
-      if (lane == 0) {
-        for (int u = 0; u < m; ++u) {
-          if (!((valid >> u) & 1u)) continue;
-          const double ww = terms[w][0][u];
-          wp = __fma_rn(terms[w][1][u], ww, wp);
-          wg = __fma_rn(terms[w][2][u], ww, wg);
-          ws = ws + ww;
-        }
-      }
-      __syncwarp();
-    }
-    if (lane == 0) {
-      const double P = ws > 0.0 ? (wp + wg) / ws : 0.0;
-      s.P[t] = P;
-      s.Pr[t] = P / (k.rho0 * k.rho0);
-      s.rho[t] = k.rho0;
-    }
   }
   cw_count<SPH_OP_WALL_PRESSURE>(b, c0, 0, 0);
 }

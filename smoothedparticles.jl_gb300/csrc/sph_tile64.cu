@@ -157,7 +157,7 @@ __device__ __forceinline__ void tile_run(const State& s, const Geometry& g, cons
       pr.y = pr.y - oy;
       pr.z = pr.z - oz;
       // in the own cell's tile, earlier blocks counted p's hits as a column
-      if (self && ia > 0) rc = (int)b.rseg[(size_t)p * nd + c];
+      if (self && ia > 0) rc = (int)b.rseg[rseg_at(b, p, c)];
     }
     __syncwarp();
     sh.rx[lane] = pr.x;
@@ -239,7 +239,7 @@ __device__ __forceinline__ void tile_run(const State& s, const Geometry& g, cons
       int cc = rc;
       size_t cj = 0;
       if (!diag && lane < mb) {
-        cj = (size_t)q * nd + mc;
+        cj = rseg_at(b, q, mc);
         cc = ia == 0 ? 0 : (int)b.rseg[cj];
       }
       sh.rmask[lane] = rm;
@@ -318,7 +318,7 @@ __device__ __forceinline__ void tile_run(const State& s, const Geometry& g, cons
       __syncwarp();
       rc += __popc(rm);
     }
-    if (lane < ma) b.rseg[(size_t)p * nd + c] = (unsigned)rc;
+    if (lane < ma) b.rseg[rseg_at(b, p, c)] = (unsigned)rc;
   }
   if (ln > 0) {
     __syncwarp();
@@ -358,9 +358,10 @@ __global__ void __launch_bounds__(32 * kTileWarps, 10) tile_kernel(State s, Geom
 }
 
 // Particle i's part of row_count_kernel: returns its row in units of four
-// entries.
+// entries and, for a wall, its list (1: with fluid neighbours, 2: without, 0:
+// its row is not used).
 __device__ __forceinline__ int row_count_body(const State& s, const Geometry& g, const Consts& k,
-                                              const BinScratch& b, int i) {
+                                              const BinScratch& b, int i, int& wall) {
   long long X[3] = {0, 0, 0};
   for (int d = 0; d < k.dim; ++d) {
     X[d] = fx_fix(s.x[d][i], k.fx_k);
@@ -375,7 +376,7 @@ __device__ __forceinline__ int row_count_body(const State& s, const Geometry& g,
   bool over = __ldg(&b.cell_start[key + 1]) - __ldg(&b.cell_start[key]) > 0xffff;
   const bool own_fluid = __ldg(&b.cell_fluid[key]) != 0;
   int run = 0;
-  unsigned* seg = b.rseg + (size_t)i * nd;
+  unsigned* seg = b.rseg + i;  // seg[c * rseg_stride]: slot-major
   for (int c = 0; c < nd; ++c) {
     const int nk = key + g.key_diff[c];
     int cnt = 0;
@@ -385,20 +386,23 @@ __device__ __forceinline__ int row_count_body(const State& s, const Geometry& g,
       // a tile between two cells without fluid is skipped (no pair of it
       // involves a fluid particle), so its counts are not written
       else if (m > 0 && (own_fluid || __ldg(&b.cell_fluid[nk]) != 0))
-        cnt = (int)seg[c];
+        cnt = (int)seg[(size_t)c * b.rseg_stride];
     }
     if (cnt > kSegMax) over = true;
-    seg[c] = (unsigned)cnt;
+    seg[(size_t)c * b.rseg_stride] = (unsigned)cnt;
     run += cnt;
   }
+  const bool is_wall = s.type[i] == kWall;
   if (over) {
     // an overflowed target has no row: the pair passes treat its side like
     // one beyond the rows and its sums traverse
     b.hit_count[i] = kRowOver;
     *b.d_rover = 1;
+    wall = 0;
     return 0;
   }
   b.hit_count[i] = run;
+  wall = is_wall ? (run > 0 ? 1 : 2) : 0;
   return (run + 3) >> 2;
 }
 
@@ -413,8 +417,25 @@ __global__ void __launch_bounds__(256) row_count_kernel(State s, Geometry g, Con
   __syncthreads();
   const int n = *b.d_n;
   const int i = blockIdx.x * 256 + threadIdx.x;
-  const int c4 = i < n ? row_count_body(s, g, k, b, i) : 0;
+  int wall = 0;
+  const int c4 = i < n ? row_count_body(s, g, k, b, i, wall) : 0;
   if (i <= cap) b.c4[i] = c4;
+  // the wall pressure's lists (one atomic per warp and list; the order
+  // within a list does not matter: every wall's sum is its own)
+  const unsigned full = 0xffffffffu;
+  const int lane = threadIdx.x & 31;
+  for (int l = 1; l <= 2; ++l) {
+    const unsigned m = __ballot_sync(full, wall == l);
+    if (!m) continue;
+    const int leader = __ffs(m) - 1;
+    int base = 0;
+    if (lane == leader) base = atomicAdd(&b.d_nwall[l - 1], __popc(m));
+    base = __shfl_sync(full, base, leader);
+    if (wall == l) {
+      const int j = base + __popc(m & lanemask_lt());
+      b.wall_list[l == 1 ? j : b.wall_cap - 1 - j] = i;
+    }
+  }
   // the exact total (64-bit) beside the scan's int32 one
   const int ws = __reduce_add_sync(0xffffffffu, c4);
   if ((threadIdx.x & 31) == 0 && ws) atomicAdd(&block_sum, ws);
@@ -441,15 +462,15 @@ __global__ void __launch_bounds__(256) row_offsets_kernel(Geometry g, BinScratch
     return;
   }
   const int nd = g.n_diff;
-  unsigned* seg = b.rseg + (size_t)i * nd;
+  unsigned* seg = b.rseg + i;  // seg[c * rseg_stride]: slot-major
   if (b.hit_count[i] == kRowOver) {
-    for (int c = 0; c < nd; ++c) seg[c] = kNoRow;
+    for (int c = 0; c < nd; ++c) seg[(size_t)c * b.rseg_stride] = kNoRow;
     return;
   }
   unsigned off = 4u * __ldg(&b.row_base[i]);  // < row_cap < 2^32
   for (int c = 0; c < nd; ++c) {
-    const unsigned cnt = seg[c];
-    seg[c] = off;
+    const unsigned cnt = seg[(size_t)c * b.rseg_stride];
+    seg[(size_t)c * b.rseg_stride] = off;
     off += cnt;
   }
 }
@@ -498,8 +519,8 @@ __global__ void __launch_bounds__(256, PH == 0 ? 6 : 5) pair_list_kernel(State s
     // pass fluid rows only
     const unsigned rp = m & 1023u, rq = (m >> 10) & 1023u;
     unsigned bp = kNoRow, bq = kNoRow;
-    if ((PH == 0 || fp) && rp != kRankNone) bp = __ldg(&b.rseg[(size_t)p * nd + c]);
-    if ((PH == 0 || fq) && rq != kRankNone) bq = __ldg(&b.rseg[(size_t)q * nd + (nd - 1 - c)]);
+    if ((PH == 0 || fp) && rp != kRankNone) bp = __ldg(&b.rseg[rseg_at(b, p, c)]);
+    if ((PH == 0 || fq) && rq != kRankNone) bq = __ldg(&b.rseg[rseg_at(b, q, nd - 1 - c)]);
     const bool wp = bp != kNoRow, wq = bq != kNoRow;
     if (!wp && !wq) continue;
     RowEntry* const ep = b.rows + (wp ? (size_t)bp + rp : 0);
@@ -545,10 +566,8 @@ __global__ void __launch_bounds__(256, PH == 0 ? 6 : 5) pair_list_kernel(State s
           frec_load_v(b.frec + q, qv1, qv2, qrho, qpr);
           sp = ppr + qpr;
           rs = prho + qrho;
-          // velocity differences on the integer pipes (isub_rn: the IEEE
-          // subtraction's result)
-          dv1 = isub_rn(pv1, qv1);
-          dv2 = DIM == 3 ? isub_rn(pv2, qv2) : 0.0;
+          dv1 = pv1 - qv1;
+          dv2 = DIM == 3 ? pv2 - qv2 : 0.0;
         }
         long long PX0, PX1, PX2, QX0, QX1, QX2;
         double pv0, qv0;
@@ -556,7 +575,7 @@ __global__ void __launch_bounds__(256, PH == 0 ? 6 : 5) pair_list_kernel(State s
         frec_load_x(b.frec + q, QX0, QX1, QX2, qv0);
         const double d0 = fx_sep2(PX0, &s.x[0][p], QX0, &s.x[0][q], k.fx_k);
         const double d1 = fx_sep2(PX1, &s.x[1][p], QX1, &s.x[1][q], k.fx_k);
-        const double dv0 = isub_rn(pv0, qv0);
+        const double dv0 = pv0 - qv0;
         double vdx = __fma_rn(dv1, d1, dv0 * d0);
         if (DIM == 3) {
           const double d2 = fx_sep2(PX2, &s.x[2][p], QX2, &s.x[2][q], k.fx_k);
@@ -599,8 +618,8 @@ cudaError_t tiles_dim(const LaunchCtx& c, const State& s, const Geometry& g, con
     const long long slots = (long long)b.max_items * (g.n_diff / 2 + 1);
     const int tb = (int)std::max(
         1LL, std::min<long long>((slots + kTileWarps - 1) / kTileWarps, tile_wave));
-    // pair count, overflow flags and the rows' 64-bit total
-    cudaMemsetAsync(b.d_npairs, 0, 24, st);
+    // pair count, overflow flags, the rows' 64-bit total, the wall counts
+    cudaMemsetAsync(b.d_npairs, 0, 32, st);
     tile_kernel<DIM><<<tb, 32 * kTileWarps, 0, st>>>(s, g, k, b, tb * kTileWarps);
     row_count_kernel<<<cap / 256 + 1, 256, 0, st>>>(s, g, k, b, cap);
     // the rows' starts: c4[0 .. cap] -> row_base (row_base[n] = the total);
@@ -631,10 +650,8 @@ __global__ void arith_check_kernel(int op, int k, int n, const double* a, const 
     r = isqrt_rn(x);
   } else if (op == 2) {
     r = ircp_rn(x);
-  } else if (op == 3) {
-    r = two_over(x);
   } else {
-    r = isub_rn(x, b[i]);
+    r = two_over(x);
   }
   out[i] = r;
 }
@@ -652,9 +669,9 @@ cudaError_t launch_tiles_fp64(const LaunchCtx& c, const State& s, const Geometry
 
 extern "C" int sph_arith_check(int device, int op, int k, int n, const double* a, const double* b,
                                double* out) {
-  if (n < 0 || op < 0 || op > 4) return SPH_ERR_ARG;
+  if (n < 0 || op < 0 || op > 3) return SPH_ERR_ARG;
   if (n == 0) return SPH_OK;
-  if (!a || !out || ((op == 0 || op == 4) && !b)) return SPH_ERR_ARG;
+  if (!a || !out || (op == 0 && !b)) return SPH_ERR_ARG;
   int prev = 0;
   if (cudaGetDevice(&prev) != cudaSuccess || cudaSetDevice(device) != cudaSuccess) {
     cudaGetLastError();
@@ -666,8 +683,7 @@ extern "C" int sph_arith_check(int device, int op, int k, int n, const double* a
   if (cudaMalloc(&d, 3 * bytes) != cudaSuccess) {
     rc = SPH_ERR_NOMEM;
   } else if (cudaMemcpy(d, a, bytes, cudaMemcpyHostToDevice) != cudaSuccess ||
-             ((op == 0 || op == 4) &&
-              cudaMemcpy(d + n, b, bytes, cudaMemcpyHostToDevice) != cudaSuccess)) {
+             (op == 0 && cudaMemcpy(d + n, b, bytes, cudaMemcpyHostToDevice) != cudaSuccess)) {
     rc = SPH_ERR_CUDA;
   } else {
     sphgpu::arith_check_kernel<<<(n + 255) / 256, 256>>>(op, k, n, d, d + n, d + 2 * (size_t)n);
