@@ -111,7 +111,7 @@ def parse():
     ap.add_argument("--serve-seed", type=int, default=5)
     ap.add_argument("--serve-budget-frac", type=float, default=0.15,
                     help="HBM budget as a fraction of the device memory free at start")
-    ap.add_argument("--serve-max-wait", type=float, default=20.0,
+    ap.add_argument("--serve-max-wait", type=float, default=60.0,
                     help="aging bound of the skip-ahead admission (seconds)")
     ap.add_argument("--only", choices=["all", "ensemble", "serve"], default="all")
     return ap.parse_args()

@@ -92,7 +92,8 @@ struct Consts {
 // whole): the neighbour index (bit 31 set for walls) and up to three values
 // -- after the density pass m W, the kernel distance r and t = 1 - r/H (the
 // force pass's kernel derivative starts from it), after the force pass the
-// pressure factor and the XSPH factor.
+// pressure factor and the XSPH factor.  A wall's row (its fluid neighbours)
+// holds W (without the mass), g.(x_w - x_q) and t for its pressure.
 struct __align__(32) RowEntry {
   unsigned long long q;
   double a, b, c;
@@ -160,8 +161,9 @@ struct BinScratch {
   // entries, 128 bytes).  The row is split into one segment per
   // neighbour-cell slot c (key_diff order): the tile kernel counts each
   // segment's hits into rseg[c * rseg_stride + i] (slot-major, so that the
-  // passes over the particles read and write it coalesced), the row scan turns the counts
-  // into the segments' absolute first entries (sph_tile64.cu).  A row that
+  // passes over the particles read and write it coalesced), the row count
+  // turns the counts into the segments' first entries relative to the row's
+  // start (the pair kernels add 4 row_base[i]; sph_tile64.cu).  A row that
   // cannot be used (a segment of more than kSegMax hits, a neighbour cell of
   // more than 65535 particles) has hit_count kRowOver and its target
   // traverses; so does every target when the rows do not fit row_cap (the
@@ -170,7 +172,7 @@ struct BinScratch {
   long long row_cap;    // entries `rows` holds (< 2^32)
   unsigned* row_base;   // cap + 1: exclusive prefix of c4 (row starts / 4)
   int* c4;              // cap + 1: (hit_count + 3) / 4, 0 for rows not used
-  unsigned* rseg;       // n_diff per particle: hits per slot, then first entries
+  unsigned* rseg;       // n_diff per particle: hits per slot, then relative first entries
   int rseg_stride;      // particles per slot of rseg (the arena's capacity)
   int* hit_count;
   // the largest row total a pass needed beyond row_cap (host-mapped memory,

@@ -135,10 +135,10 @@ struct Proc64 {
       for (int j = 0; j < cnt; ++j) acc = acc + __ldg(&row[j].a);
       c0 += cnt;
     } else if (OP == SPH_OP_WALL_PRESSURE) {
-      // a wall's row: its fluid neighbours with their distances and t = 1 - r/H
+      // a wall's row: its fluid neighbours with the kernel value W(r) (no
+      // mass) and g.(x_w - x_q), both formed by the density pass's pair
+      // kernel in the same expressions as process() forms them
       const int n = *b.d_n;
-      const long long X0 = b.xfix[0][i], X1 = b.xfix[1][i];
-      const long long X2 = DIM == 3 ? b.xfix[2][i] : 0;
       for (int j = 0; j < cnt; ++j) {
         const RowEntry en = row_load(row + j);
         const int q = (int)(en.q & 0x7fffffffu);
@@ -146,17 +146,7 @@ struct Proc64 {
           atomicOr(b.d_err, kErrBounds);
           continue;
         }
-        const double t = en.c;  // ker_t of the stored distance
-        const double t2 = t * t;
-        const double w = (k.cw * (t2 * t2)) * __fma_rn(-4.0, t, 5.0);
-        // q's position half of its record (the density pass's row scan)
-        long long QX0, QX1, QX2;
-        double qv0;
-        frec_load_x(b.frec + q, QX0, QX1, QX2, qv0);
-        const double d0 = fx_sep2(X0, &s.x[0][i], QX0, &s.x[0][q], k.fx_k);
-        const double d1 = fx_sep2(X1, &s.x[1][i], QX1, &s.x[1][q], k.fx_k);
-        double gd = __fma_rn(k.g[1], d1, k.g[0] * d0);
-        if (DIM == 3) gd = __fma_rn(k.g[2], fx_sep2(X2, &s.x[2][i], QX2, &s.x[2][q], k.fx_k), gd);
+        const double w = en.a, gd = en.b;
         wp = __fma_rn(__ldg(&s.P[q]), w, wp);
         wg = __fma_rn(__ldg(&s.rho[q]) * gd, w, wg);
         ws = ws + w;

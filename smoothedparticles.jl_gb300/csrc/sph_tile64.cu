@@ -35,12 +35,15 @@
 // Passes of a step (launch order):
 //   tiles    classify once: rseg := hits per (target, slot); the pair list
 //            (p, q, both ranks, slot, wall bits)
-//   count    hit_count (the row length), c4 = the row in 128-byte units;
-//            the fixed-point positions (xfix and the records' first halves)
+//   count    hit_count (the row length), c4 = the row in 128-byte units,
+//            rseg := each segment's first entry relative to the row's start;
+//            the fixed-point positions (xfix and the records' first halves);
+//            the walls' lists for the wall pressure
 //   scan     row_base := exclusive prefix of c4 over the particles
-//   offsets  rseg := each segment's absolute first entry; rows beyond
-//            row_cap send every target to the traversal (and tell the host)
-//   density  per pair: m W, r and t into both rows (at rseg + rank)
+//   fit      rows beyond row_cap send every target to the traversal (and
+//            tell the host)
+//   density  per pair: m W, r and t into both rows (at 4 row_base + rseg +
+//            rank); a wall's entry gets W and g.(x_w - x_f) instead
 //   [sum]    sph_pair64.cu: rho = the row's sum, self term, EOS
 //   [wall]   sph_pair64.cu: each wall's pressure over its row (fluid
 //            neighbours, the kernel value from the stored t)
@@ -389,13 +392,16 @@ __device__ __forceinline__ int row_count_body(const State& s, const Geometry& g,
         cnt = (int)seg[(size_t)c * b.rseg_stride];
     }
     if (cnt > kSegMax) over = true;
-    seg[(size_t)c * b.rseg_stride] = (unsigned)cnt;
+    // the segment's first entry relative to the row's start (the pair
+    // kernels add the start, 4 row_base[i], once the scan has it)
+    seg[(size_t)c * b.rseg_stride] = (unsigned)run;
     run += cnt;
   }
   const bool is_wall = s.type[i] == kWall;
   if (over) {
     // an overflowed target has no row: the pair passes treat its side like
     // one beyond the rows and its sums traverse
+    for (int c = 0; c < nd; ++c) seg[(size_t)c * b.rseg_stride] = kNoRow;
     b.hit_count[i] = kRowOver;
     *b.d_rover = 1;
     wall = 0;
@@ -443,35 +449,16 @@ __global__ void __launch_bounds__(256) row_count_kernel(State s, Geometry g, Con
   if (threadIdx.x == 0 && block_sum) atomicAdd(b.d_rowsum, (unsigned long long)block_sum);
 }
 
-// Each segment's absolute first entry from the row's start (row_base, the
-// scan of c4) and the per-slot counts, in place.  Rows beyond row_cap: every
+// Whether the rows fit row_cap (one thread, after the scan): otherwise every
 // target traverses this pass (the pair list's overflow flag) and the host,
 // which reads need_host between passes, grows the rows.  The fit is decided
 // on the exact 64-bit total; when it fits (row_cap < 2^32 entries), the
 // int32 scan cannot have wrapped.
-__global__ void __launch_bounds__(256) row_offsets_kernel(Geometry g, BinScratch b) {
-  const int n = *b.d_n;
-  const int i = blockIdx.x * 256 + threadIdx.x;
-  if (i >= n) return;
+__global__ void rows_fit_kernel(BinScratch b) {
   const unsigned long long total = 4ull * *b.d_rowsum;
   if (total > (unsigned long long)b.row_cap) {
-    if (i == 0) {
-      *b.d_pover = 1;
-      if (b.need_host && *b.need_host < total) *b.need_host = total;
-    }
-    return;
-  }
-  const int nd = g.n_diff;
-  unsigned* seg = b.rseg + i;  // seg[c * rseg_stride]: slot-major
-  if (b.hit_count[i] == kRowOver) {
-    for (int c = 0; c < nd; ++c) seg[(size_t)c * b.rseg_stride] = kNoRow;
-    return;
-  }
-  unsigned off = 4u * __ldg(&b.row_base[i]);  // < row_cap < 2^32
-  for (int c = 0; c < nd; ++c) {
-    const unsigned cnt = seg[(size_t)c * b.rseg_stride];
-    seg[(size_t)c * b.rseg_stride] = off;
-    off += cnt;
+    *b.d_pover = 1;
+    if (b.need_host && *b.need_host < total) *b.need_host = total;
   }
 }
 
@@ -519,8 +506,14 @@ __global__ void __launch_bounds__(256, PH == 0 ? 6 : 5) pair_list_kernel(State s
     // pass fluid rows only
     const unsigned rp = m & 1023u, rq = (m >> 10) & 1023u;
     unsigned bp = kNoRow, bq = kNoRow;
-    if ((PH == 0 || fp) && rp != kRankNone) bp = __ldg(&b.rseg[rseg_at(b, p, c)]);
-    if ((PH == 0 || fq) && rq != kRankNone) bq = __ldg(&b.rseg[rseg_at(b, q, nd - 1 - c)]);
+    if ((PH == 0 || fp) && rp != kRankNone) {
+      bp = __ldg(&b.rseg[rseg_at(b, p, c)]);
+      if (bp != kNoRow) bp += 4u * __ldg(&b.row_base[p]);
+    }
+    if ((PH == 0 || fq) && rq != kRankNone) {
+      bq = __ldg(&b.rseg[rseg_at(b, q, nd - 1 - c)]);
+      if (bq != kNoRow) bq += 4u * __ldg(&b.row_base[q]);
+    }
     const bool wp = bp != kNoRow, wq = bq != kNoRow;
     if (!wp && !wq) continue;
     RowEntry* const ep = b.rows + (wp ? (size_t)bp + rp : 0);
@@ -536,18 +529,32 @@ __global__ void __launch_bounds__(256, PH == 0 ? 6 : 5) pair_list_kernel(State s
       const double d0 = fx_sep2(PX0, &s.x[0][p], QX0, &s.x[0][q], k.fx_k);
       const double d1 = fx_sep2(PX1, &s.x[1][p], QX1, &s.x[1][q], k.fx_k);
       double ss = __fma_rn(d1, d1, d0 * d0);
+      double d2 = 0.0;
       if (DIM == 3) {
-        const double d2 = fx_sep2(PX2, &s.x[2][p], QX2, &s.x[2][q], k.fx_k);
+        d2 = fx_sep2(PX2, &s.x[2][p], QX2, &s.x[2][q], k.fx_k);
         ss = __fma_rn(d2, d2, ss);
       }
       const double r = isqrt_rn(ss);
       const double t = ker_t(k, r);
       const double t2 = t * t;
       const double w = (k.mcw * (t2 * t2)) * __fma_rn(-4.0, t, 5.0);  // m W
-      // t = 1 - r/H rides in the entry's spare slot, so that the force pass
-      // of this binning starts its kernel derivative from it
-      if (wp) row_store(ep, qbits, w, r, t);
-      if (wq) row_store(eq, pbits, w, r, t);
+      if (fp && fq) {
+        // t = 1 - r/H rides in the entry's spare slot, so that the force
+        // pass of this binning starts its kernel derivative from it
+        if (wp) row_store(ep, qbits, w, r, t);
+        if (wq) row_store(eq, pbits, w, r, t);
+      } else {
+        // a fluid-wall pair: the fluid target's entry as above; the wall's
+        // entry holds what its pressure sums (Proc64::rows): the kernel
+        // value without the mass and g.(x_w - x_f).  gd below is
+        // g.(x_p - x_q); the wall's is it when p is the wall and its
+        // negation (exact) when q is
+        const double wc = (k.cw * (t2 * t2)) * __fma_rn(-4.0, t, 5.0);
+        double gd = __fma_rn(k.g[1], d1, k.g[0] * d0);
+        if (DIM == 3) gd = __fma_rn(k.g[2], d2, gd);
+        if (wp) row_store(ep, qbits, fp ? w : wc, fp ? r : gd, t);
+        if (wq) row_store(eq, pbits, fq ? w : wc, fq ? r : -gd, t);
+      }
     } else {
       // m W, r and t as the density pass of this binning stored them
       const RowEntry en = row_load(wp ? ep : eq);
@@ -627,7 +634,7 @@ cudaError_t tiles_dim(const LaunchCtx& c, const State& s, const Geometry& g, con
     const LaunchCtx quiet{st, nullptr, nullptr};
     const cudaError_t e = launch_scan(quiet, b.c4, (int*)b.row_base, cap + 1, b.pscan_tmp);
     if (e != cudaSuccess) return e;
-    row_offsets_kernel<<<(cap + 255) / 256, 256, 0, st>>>(g, b);
+    rows_fit_kernel<<<1, 1, 0, st>>>(b);
     pair_list_kernel<DIM, 0><<<dens_wave, 256, 0, st>>>(s, g, k, b, dens_wave * 256);
   } else {
     frec_build_kernel<DIM><<<(cap + 255) / 256, 256, 0, st>>>(s, b);

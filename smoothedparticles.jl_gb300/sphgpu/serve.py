@@ -186,7 +186,8 @@ class Server:
         self.peak_slots = 0
         self.peak_device_bytes = 0
         self.skipped_ahead = 0       # admissions past an earlier request that did not fit
-        self.aged = 0                # times the aging bound held later requests back
+        self.aged = 0                # requests whose wait reached the aging bound (held the rest)
+        self._aged_ids = set()
         self.pool_rebuilds = 0
         self.pool_peak_members = 0
 
@@ -312,7 +313,9 @@ class Server:
                                            f"whole budget {self.budget} B")
                     if used + need > self.budget:
                         if now - r.arrival >= self.max_wait_s:
-                            self.aged += 1
+                            if r.rid not in self._aged_ids:
+                                self._aged_ids.add(r.rid)
+                                self.aged += 1
                             break          # nothing after it may pass it now
                         blocked = True
                         i += 1
