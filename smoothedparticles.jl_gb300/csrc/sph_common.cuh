@@ -163,16 +163,16 @@ struct BinScratch {
   // segment's hits into rseg[c * rseg_stride + i] (slot-major, so that the
   // passes over the particles read and write it coalesced), the row count
   // turns the counts into the segments' first entries relative to the row's
-  // start (the pair kernels add 4 row_base[i]; sph_tile64.cu).  A row that
-  // cannot be used (a segment of more than kSegMax hits, a neighbour cell of
-  // more than 65535 particles) has hit_count kRowOver and its target
+  // start and the offsets pass adds the start 4 row_base[i] (sph_tile64.cu).
+  // A row that cannot be used (a segment of more than kSegMax hits, a
+  // neighbour cell of more than 65535 particles) has hit_count kRowOver and its target
   // traverses; so does every target when the rows do not fit row_cap (the
   // host grows them before the next pass).
   RowEntry* rows;
   long long row_cap;    // entries `rows` holds (< 2^32)
   unsigned* row_base;   // cap + 1: exclusive prefix of c4 (row starts / 4)
   int* c4;              // cap + 1: (hit_count + 3) / 4, 0 for rows not used
-  unsigned* rseg;       // n_diff per particle: hits per slot, then relative first entries
+  unsigned* rseg;       // n_diff per particle: hits per slot, then first entries
   int rseg_stride;      // particles per slot of rseg (the arena's capacity)
   int* hit_count;
   // the largest row total a pass needed beyond row_cap (host-mapped memory,

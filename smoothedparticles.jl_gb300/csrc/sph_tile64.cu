@@ -40,10 +40,10 @@
 //            the fixed-point positions (xfix and the records' first halves);
 //            the walls' lists for the wall pressure
 //   scan     row_base := exclusive prefix of c4 over the particles
-//   fit      rows beyond row_cap send every target to the traversal (and
-//            tell the host)
-//   density  per pair: m W, r and t into both rows (at 4 row_base + rseg +
-//            rank); a wall's entry gets W and g.(x_w - x_f) instead
+//   offsets  rseg += the row's start 4 row_base; rows beyond row_cap send
+//            every target to the traversal (and tell the host)
+//   density  per pair: m W, r and t into both rows (at rseg + rank); a
+//            wall's entry gets W and g.(x_w - x_f) instead
 //   [sum]    sph_pair64.cu: rho = the row's sum, self term, EOS
 //   [wall]   sph_pair64.cu: each wall's pressure over its row (fluid
 //            neighbours, the kernel value from the stored t)
@@ -378,24 +378,34 @@ __device__ __forceinline__ int row_count_body(const State& s, const Geometry& g,
   const int nd = g.n_diff;
   bool over = __ldg(&b.cell_start[key + 1]) - __ldg(&b.cell_start[key]) > 0xffff;
   const bool own_fluid = __ldg(&b.cell_fluid[key]) != 0;
-  int run = 0;
   unsigned* seg = b.rseg + i;  // seg[c * rseg_stride]: slot-major
-  for (int c = 0; c < nd; ++c) {
-    const int nk = key + g.key_diff[c];
-    int cnt = 0;
-    if (nk >= 1 && nk <= g.key_max) {
-      const int m = __ldg(&b.cell_start[nk + 1]) - __ldg(&b.cell_start[nk]);
-      if (m > 0xffff) over = true;
-      // a tile between two cells without fluid is skipped (no pair of it
-      // involves a fluid particle), so its counts are not written
-      else if (m > 0 && (own_fluid || __ldg(&b.cell_fluid[nk]) != 0))
-        cnt = (int)seg[(size_t)c * b.rseg_stride];
+  // every slot's count first (independent loads), then the relative offsets
+  int cnt[27];
+#pragma unroll
+  for (int c = 0; c < 27; ++c) {
+    cnt[c] = 0;
+    if (c < nd) {
+      const int nk = key + g.key_diff[c];
+      if (nk >= 1 && nk <= g.key_max) {
+        const int m = __ldg(&b.cell_start[nk + 1]) - __ldg(&b.cell_start[nk]);
+        if (m > 0xffff) over = true;
+        // a tile between two cells without fluid is skipped (no pair of it
+        // involves a fluid particle), so its counts are not written
+        else if (m > 0 && (own_fluid || __ldg(&b.cell_fluid[nk]) != 0))
+          cnt[c] = (int)seg[(size_t)c * b.rseg_stride];
+      }
     }
-    if (cnt > kSegMax) over = true;
-    // the segment's first entry relative to the row's start (the pair
-    // kernels add the start, 4 row_base[i], once the scan has it)
-    seg[(size_t)c * b.rseg_stride] = (unsigned)run;
-    run += cnt;
+  }
+  int run = 0;
+#pragma unroll
+  for (int c = 0; c < 27; ++c) {
+    if (c < nd) {
+      if (cnt[c] > kSegMax) over = true;
+      // the segment's first entry relative to the row's start (the offsets
+      // pass adds the start, 4 row_base[i], once the scan has it)
+      seg[(size_t)c * b.rseg_stride] = (unsigned)run;
+      run += cnt[c];
+    }
   }
   const bool is_wall = s.type[i] == kWall;
   if (over) {
@@ -449,17 +459,34 @@ __global__ void __launch_bounds__(256) row_count_kernel(State s, Geometry g, Con
   if (threadIdx.x == 0 && block_sum) atomicAdd(b.d_rowsum, (unsigned long long)block_sum);
 }
 
-// Whether the rows fit row_cap (one thread, after the scan): otherwise every
-// target traverses this pass (the pair list's overflow flag) and the host,
-// which reads need_host between passes, grows the rows.  The fit is decided
-// on the exact 64-bit total; when it fits (row_cap < 2^32 entries), the
-// int32 scan cannot have wrapped.
-__global__ void rows_fit_kernel(BinScratch b) {
+// Each segment's absolute first entry: the row's start (4 row_base[i], the
+// scan of c4) added to the relative offsets the row count wrote, all 27
+// loaded before any is stored.  Rows beyond row_cap: every target traverses
+// this pass (the pair list's overflow flag) and the host, which reads
+// need_host between passes, grows the rows.  The fit is decided on the exact
+// 64-bit total; when it fits (row_cap < 2^32 entries), the int32 scan cannot
+// have wrapped.
+__global__ void __launch_bounds__(256) row_offsets_kernel(Geometry g, BinScratch b) {
+  const int n = *b.d_n;
+  const int i = blockIdx.x * 256 + threadIdx.x;
+  if (i >= n) return;
   const unsigned long long total = 4ull * *b.d_rowsum;
   if (total > (unsigned long long)b.row_cap) {
-    *b.d_pover = 1;
-    if (b.need_host && *b.need_host < total) *b.need_host = total;
+    if (i == 0) {
+      *b.d_pover = 1;
+      if (b.need_host && *b.need_host < total) *b.need_host = total;
+    }
+    return;
   }
+  const int nd = g.n_diff;
+  unsigned* seg = b.rseg + i;
+  unsigned rel[27];
+#pragma unroll
+  for (int c = 0; c < 27; ++c) rel[c] = c < nd ? seg[(size_t)c * b.rseg_stride] : 0u;
+  const unsigned base = 4u * __ldg(&b.row_base[i]);  // < row_cap < 2^32
+#pragma unroll
+  for (int c = 0; c < 27; ++c)
+    if (c < nd && rel[c] != kNoRow) seg[(size_t)c * b.rseg_stride] = base + rel[c];
 }
 
 // The force records (FxRec) of every particle from the SoA state: the
@@ -506,14 +533,8 @@ __global__ void __launch_bounds__(256, PH == 0 ? 6 : 5) pair_list_kernel(State s
     // pass fluid rows only
     const unsigned rp = m & 1023u, rq = (m >> 10) & 1023u;
     unsigned bp = kNoRow, bq = kNoRow;
-    if ((PH == 0 || fp) && rp != kRankNone) {
-      bp = __ldg(&b.rseg[rseg_at(b, p, c)]);
-      if (bp != kNoRow) bp += 4u * __ldg(&b.row_base[p]);
-    }
-    if ((PH == 0 || fq) && rq != kRankNone) {
-      bq = __ldg(&b.rseg[rseg_at(b, q, nd - 1 - c)]);
-      if (bq != kNoRow) bq += 4u * __ldg(&b.row_base[q]);
-    }
+    if ((PH == 0 || fp) && rp != kRankNone) bp = __ldg(&b.rseg[rseg_at(b, p, c)]);
+    if ((PH == 0 || fq) && rq != kRankNone) bq = __ldg(&b.rseg[rseg_at(b, q, nd - 1 - c)]);
     const bool wp = bp != kNoRow, wq = bq != kNoRow;
     if (!wp && !wq) continue;
     RowEntry* const ep = b.rows + (wp ? (size_t)bp + rp : 0);
@@ -634,7 +655,7 @@ cudaError_t tiles_dim(const LaunchCtx& c, const State& s, const Geometry& g, con
     const LaunchCtx quiet{st, nullptr, nullptr};
     const cudaError_t e = launch_scan(quiet, b.c4, (int*)b.row_base, cap + 1, b.pscan_tmp);
     if (e != cudaSuccess) return e;
-    rows_fit_kernel<<<1, 1, 0, st>>>(b);
+    row_offsets_kernel<<<(cap + 255) / 256, 256, 0, st>>>(g, b);
     pair_list_kernel<DIM, 0><<<dens_wave, 256, 0, st>>>(s, g, k, b, dens_wave * 256);
   } else {
     frec_build_kernel<DIM><<<(cap + 255) / 256, 256, 0, st>>>(s, b);
