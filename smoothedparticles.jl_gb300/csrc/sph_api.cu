@@ -879,25 +879,6 @@ int sph_num_particles(sph_system* s, int64_t* n) {
   return SPH_OK;
 }
 
-// The device's address of a pinned host buffer (cudaHostAlloc or
-// cudaHostRegister; its mapping is the same address under unified
-// addressing), or nullptr for pageable or device memory.  Fields are then
-// read and written by the kernel directly over the host link, in reference
-// order, instead of through the staging buffer and a copy.
-#ifndef SPH_IO_ZERO_COPY
-#define SPH_IO_ZERO_COPY 1
-#endif
-static void* mapped_host(const void* p) {
-  if (!SPH_IO_ZERO_COPY) return nullptr;
-  cudaPointerAttributes a;
-  if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
-    cudaGetLastError();
-    return nullptr;
-  }
-  if (a.type != cudaMemoryTypeHost || !a.devicePointer) return nullptr;
-  return a.devicePointer;
-}
-
 int sph_get_field(sph_system* s, int field, void* out) {
   if (!s || !out) return SPH_ERR_ARG;
   if (field < SPH_FIELD_X || field > SPH_FIELD_KEY) return fail(s, SPH_ERR_ARG, "unknown field %d", field);
@@ -906,16 +887,9 @@ int sph_get_field(sph_system* s, int field, void* out) {
   int rc = read_count(s, &n);
   if (rc) return rc;
   if (n == 0) return SPH_OK;
-  if (void* dev = mapped_host(out)) {
-    cudaError_t e = launch_field(ctx(s), s->cur, s->k, s->b, s->n_host, field, 0, dev, true);
-    if (e != cudaSuccess) return fail(s, SPH_ERR_CUDA, "field: %s", cudaGetErrorString(e));
-  } else {
-    cudaError_t e =
-        launch_field(ctx(s), s->cur, s->k, s->b, s->n_host, field, 0, s->staging, false);
-    if (e != cudaSuccess) return fail(s, SPH_ERR_CUDA, "field: %s", cudaGetErrorString(e));
-    CK(cudaMemcpyAsync(out, s->staging, field_bytes(field, n), cudaMemcpyDeviceToHost,
-                       s->stream));
-  }
+  cudaError_t e = launch_field(ctx(s), s->cur, s->k, s->b, s->n_host, field, 0, s->staging);
+  if (e != cudaSuccess) return fail(s, SPH_ERR_CUDA, "field: %s", cudaGetErrorString(e));
+  CK(cudaMemcpyAsync(out, s->staging, field_bytes(field, n), cudaMemcpyDeviceToHost, s->stream));
   CK(cudaStreamSynchronize(s->stream));
   return SPH_OK;
 }
@@ -941,16 +915,9 @@ int sph_set_field(sph_system* s, int field, const void* in) {
       if (t[i] != SPH_FLUID && t[i] != SPH_WALL)
         return fail(s, SPH_ERR_ARG, "particle %d has unknown type %d", i, t[i]);
   }
-  if (void* dev = mapped_host(in)) {
-    cudaError_t e = launch_field(ctx(s), s->cur, s->k, s->b, s->n_host, field, 1, dev, true);
-    if (e != cudaSuccess) return fail(s, SPH_ERR_CUDA, "field: %s", cudaGetErrorString(e));
-  } else {
-    CK(cudaMemcpyAsync(s->staging, in, field_bytes(field, n), cudaMemcpyHostToDevice,
-                       s->stream));
-    cudaError_t e =
-        launch_field(ctx(s), s->cur, s->k, s->b, s->n_host, field, 1, s->staging, false);
-    if (e != cudaSuccess) return fail(s, SPH_ERR_CUDA, "field: %s", cudaGetErrorString(e));
-  }
+  CK(cudaMemcpyAsync(s->staging, in, field_bytes(field, n), cudaMemcpyHostToDevice, s->stream));
+  cudaError_t e = launch_field(ctx(s), s->cur, s->k, s->b, s->n_host, field, 1, s->staging);
+  if (e != cudaSuccess) return fail(s, SPH_ERR_CUDA, "field: %s", cudaGetErrorString(e));
   CK(cudaStreamSynchronize(s->stream));
   if (field == SPH_FIELD_X) s->cells_valid = false;
   if (field == SPH_FIELD_X || field == SPH_FIELD_TYPE) s->lists_valid = s->hits_valid = false;

@@ -7,6 +7,9 @@
 // the support, q = p included (core.jl:210-213 keeps it, with r = 0).
 //   1. count: one thread per particle walks the 3^d cells in key_diff order
 //      and counts; the row offsets are an exclusive scan of the counts;
+//      every walk classifies its candidates with the pair passes' FP32
+//      pre-test first and forms the FP64 distance only for hits and band
+//      candidates (the decision equals the reference's r > h test);
 //   2. fill: the same walk writes (reference index of q, value) in the
 //      reference's push order; the projection matrix's diagonal needs the
 //      row's div_L_lambda! sums, formed first in the same order;
@@ -44,6 +47,33 @@ __device__ __forceinline__ double dist64(const State& s, const double* xp, int q
   return sqrt(ss);
 }
 
+// The pair passes' FP32 pre-test on cell-relative positions (the target at
+// (ax, ay, az) relative to the candidate's cell): 1 inside the support,
+// 0 beyond it, -1 in the band around r = h where the reference's FP64 test
+// decides.  Outside the band the FP32 decision equals the FP64 one, so the
+// FP64 distance is formed only for the hits and the band.
+template <int DIM>
+__device__ __forceinline__ int pre_test(const Consts& k, float ax, float ay, float az,
+                                        const float4& q) {
+  const float dx = ax - q.x, dy = ay - q.y;
+  float ss = dx * dx + dy * dy;
+  if (DIM == 3) {
+    const float dz = az - q.z;
+    ss = ss + dz * dz;
+  }
+  return ss > k.s_hi ? 0 : ss < k.s_lo ? 1 : -1;
+}
+
+// Particle i's position relative to neighbour cell nk (its own cell-relative
+// position minus the cell's offset, as the pair passes form it).
+__device__ __forceinline__ float4 rel_to(const Geometry& g, const Consts& k, const float4& pi,
+                                         int cx, int cy, int cz, int nk) {
+  int qx, qy, qz;
+  decode_key(g, nk, qx, qy, qz);
+  return make_float4(pi.x - (float)(qx - cx) * k.hf, pi.y - (float)(qy - cy) * k.hf,
+                     pi.z - (float)(qz - cz) * k.hf, 0.f);
+}
+
 // div_L_lambda! (collapse_dry_implicit.jl:140-145) of particle i over its
 // neighbours q != i in the reference order, after initialize! (div = L = 0,
 // lambda = 1)
@@ -55,13 +85,19 @@ __device__ void div_L_lambda(const State& s, const Geometry& g, const Consts& k,
   double vp[3] = {s.v[0][i], s.v[1][i], DIM == 3 ? s.v[2][i] : 0.0};
   const double m = k.mass, rho = k.rho0, dim = (double)DIM;
   double dv = 0.0, l = 0.0, la = 1.0;
+  const float4 pi = s.pl[i];
+  int cx, cy, cz;
+  decode_key(g, key, cx, cy, cz);
   for (int c = 0; c < g.n_diff; ++c) {
     const int nk = key + g.key_diff[c];
     if (nk < 1 || nk > g.key_max) continue;
+    const float4 a = rel_to(g, k, pi, cx, cy, cz, nk);
     for (int q = b.cell_start[nk]; q < b.cell_start[nk + 1]; ++q) {
+      const int pt = pre_test<DIM>(k, a.x, a.y, a.z, __ldg(&s.pl[q]));
+      if (pt == 0 || q == i) continue;
       double d[3];
       const double r = dist64<DIM>(s, xp, q, d);
-      if (r > k.h || q == i) continue;
+      if (pt < 0 && r > k.h) continue;
       const double rDk = ker_rdw(k, r);
       const double w0 = vp[0] - s.v[0][q];
       const double w1 = vp[1] - s.v[1][q];
@@ -86,12 +122,21 @@ __global__ void __launch_bounds__(kThreads) asm_count_kernel(State s, Geometry g
   const int key = s.cell[i];
   double xp[3] = {s.x[0][i], s.x[1][i], DIM == 3 ? s.x[2][i] : 0.0};
   int cnt = 0;
+  const float4 pi = s.pl[i];
+  int cx, cy, cz;
+  decode_key(g, key, cx, cy, cz);
   for (int c = 0; c < g.n_diff; ++c) {
     const int nk = key + g.key_diff[c];
     if (nk < 1 || nk > g.key_max) continue;
+    const float4 a = rel_to(g, k, pi, cx, cy, cz, nk);
     for (int q = b.cell_start[nk]; q < b.cell_start[nk + 1]; ++q) {
-      double d[3];
-      if (!(dist64<DIM>(s, xp, q, d) > k.h)) ++cnt;
+      const int pt = pre_test<DIM>(k, a.x, a.y, a.z, __ldg(&s.pl[q]));
+      if (pt == 1) {
+        ++cnt;
+      } else if (pt < 0) {
+        double d[3];
+        if (!(dist64<DIM>(s, xp, q, d) > k.h)) ++cnt;
+      }
     }
   }
   row_nnz[s.rid[i]] = cnt;
@@ -116,13 +161,19 @@ __global__ void __launch_bounds__(kThreads) asm_fill_kernel(State s, Geometry g,
   double xp[3] = {s.x[0][i], s.x[1][i], DIM == 3 ? s.x[2][i] : 0.0};
   int pos = row_ptr[s.rid[i]];
   const int end = row_ptr[s.rid[i] + 1];
+  const float4 pi = s.pl[i];
+  int cx, cy, cz;
+  decode_key(g, key, cx, cy, cz);
   for (int c = 0; c < g.n_diff; ++c) {
     const int nk = key + g.key_diff[c];
     if (nk < 1 || nk > g.key_max) continue;
+    const float4 a = rel_to(g, k, pi, cx, cy, cz, nk);
     for (int q = b.cell_start[nk]; q < b.cell_start[nk + 1]; ++q) {
+      const int pt = pre_test<DIM>(k, a.x, a.y, a.z, __ldg(&s.pl[q]));
+      if (pt == 0) continue;
       double d[3];
       const double r = dist64<DIM>(s, xp, q, d);
-      if (r > k.h) continue;
+      if (pt < 0 && r > k.h) continue;
       double v;
       if (func == SPH_MAT_KERNEL)
         v = ker_w(k, r);

@@ -169,11 +169,7 @@ cudaError_t launch_upload(const LaunchCtx& c, const State& s, const Consts& k,
                           const double* rho, const double* rho_ref, const int* type);
 // Field copy between the SoA state and a reference-ordered staging buffer.
 // dir 0: state -> staging, 1: staging -> state.
-// ref_order: one thread per reference index (a pinned host buffer reached
-// through its device mapping); otherwise one per storage index (the staging
-// buffer in device memory).
 cudaError_t launch_field(const LaunchCtx& c, const State& s, const Consts& k,
-                         const BinScratch& b, int cap, int field, int dir, void* staging,
-                         bool ref_order);
+                         const BinScratch& b, int cap, int field, int dir, void* staging);
 
 }  // namespace sphgpu

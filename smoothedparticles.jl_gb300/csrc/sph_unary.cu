@@ -125,19 +125,14 @@ __global__ void __launch_bounds__(kThreads) upload_kernel(State s, BinScratch b,
 }
 
 // dir 0: state (cell order) -> staging (reference order); dir 1: the reverse.
-// REF: one thread per reference index r (i = its storage index), so that the
-// buffer is read or written in order, each warp's accesses contiguous -- the
-// form for a pinned host buffer the kernel reaches through its device
-// mapping (no staging copy); otherwise one thread per storage index.
-template <int DIM, bool REF>
+template <int DIM>
 __global__ void __launch_bounds__(kThreads) field_kernel(State s, BinScratch b, int field,
                                                          int dir, void* staging, int eos,
                                                          double rho0sq) {
   const int n = *b.d_n;
-  const int t = blockIdx.x * kThreads + threadIdx.x;
-  if (t >= n) return;
-  const int i = REF ? b.inv_rid[t] : t;
-  const int r = REF ? t : s.rid[i];
+  const int i = blockIdx.x * kThreads + threadIdx.x;
+  if (i >= n) return;
+  const int r = s.rid[i];
   double* const* vec = nullptr;
   double* sc = nullptr;
   switch (field) {
@@ -225,22 +220,14 @@ cudaError_t launch_fused_unary(const LaunchCtx& c, const FusedBatch& fb, int p, 
 }
 
 cudaError_t launch_field(const LaunchCtx& c, const State& s, const Consts& k,
-                         const BinScratch& b, int cap, int field, int dir, void* staging,
-                         bool ref_order) {
+                         const BinScratch& b, int cap, int field, int dir, void* staging) {
   if (cap <= 0) return cudaSuccess;
   const int blocks = (cap + kThreads - 1) / kThreads;
   mark(c, SPH_KERNEL_IO, 0);
-  if (k.dim == 2) {
-    if (ref_order)
-      field_kernel<2, true><<<blocks, kThreads, 0, c.stream>>>(s, b, field, dir, staging, k.eos, k.rho0sq);
-    else
-      field_kernel<2, false><<<blocks, kThreads, 0, c.stream>>>(s, b, field, dir, staging, k.eos, k.rho0sq);
-  } else {
-    if (ref_order)
-      field_kernel<3, true><<<blocks, kThreads, 0, c.stream>>>(s, b, field, dir, staging, k.eos, k.rho0sq);
-    else
-      field_kernel<3, false><<<blocks, kThreads, 0, c.stream>>>(s, b, field, dir, staging, k.eos, k.rho0sq);
-  }
+  if (k.dim == 2)
+    field_kernel<2><<<blocks, kThreads, 0, c.stream>>>(s, b, field, dir, staging, k.eos, k.rho0sq);
+  else
+    field_kernel<3><<<blocks, kThreads, 0, c.stream>>>(s, b, field, dir, staging, k.eos, k.rho0sq);
   mark(c, SPH_KERNEL_IO, 1);
   return cudaGetLastError();
 }

@@ -295,7 +295,7 @@ int sph_vtk_save_frame(sph_vtk* v, unsigned fields, double time, int32_t* frame)
   for (int f = SPH_FIELD_X; f <= SPH_FIELD_KEY && e == cudaSuccess; ++f) {
     if (f != SPH_FIELD_X && !(fields & (1u << f))) continue;
     const FieldInfo fi = field_info(f);
-    if (cap > 0) e = launch_field(system_ctx(s), s->cur, s->k, s->b, cap, f, 0, d + pos, false);
+    if (cap > 0) e = launch_field(system_ctx(s), s->cur, s->k, s->b, cap, f, 0, d + pos);
     pos += align256((size_t)cap * fi.comps * fi.bytes);
   }
   if (e == cudaSuccess) e = cudaEventRecord(v->gathered[slot], s->stream);

@@ -1,7 +1,7 @@
-"""Fields through pinned host buffers (the kernel reads and writes them over
-the host link, in reference order) give the same bits as through pageable
-buffers (staging buffer + copy): every field read after steps with
-removals, and every settable field written before further steps."""
+"""Fields through pinned host buffers (the ``out=`` path of the e2e loop)
+give the same bits as through freshly allocated pageable arrays: every
+field read after steps with removals, and every settable field written
+before further steps."""
 import numpy as np
 import pytest
 
