@@ -699,10 +699,14 @@ __device__ __forceinline__ void pair32_body(const State& s, const Geometry& g, c
   if (split == 1) cw_count<OP>(b, p.c0, p.c1, p.c2);
 }
 
-// The force pass (latency bound on its record gathers) runs at 8 blocks of 4
-// warps per SM (64 registers); 0 leaves the other passes to the compiler.
+// The force pass (latency bound on its record gathers) runs at
+// SPH_FORCE_BLOCKS blocks of 4 warps per SM (8: 64 registers); 0 leaves the
+// other passes to the compiler.
+#ifndef SPH_FORCE_BLOCKS
+#define SPH_FORCE_BLOCKS 8
+#endif
 template <int OP, int WARPS>
-constexpr int kMinBlocks32 = (OP == SPH_OP_FORCE && WARPS == 4) ? 8 : 0;
+constexpr int kMinBlocks32 = (OP == SPH_OP_FORCE && WARPS == 4) ? SPH_FORCE_BLOCKS : 0;
 
 template <int DIM, int OP, int WARPS, bool SPLIT>
 __global__ void __launch_bounds__(32 * WARPS, kMinBlocks32<OP, WARPS>) pair32_kernel(State s, Geometry g, Consts k,
