@@ -409,9 +409,7 @@ int sph_pipe_peak(int device, int which, double* instr_per_s);
  * form on the integer pipes, applied on `device` to n host values, for tests
  * against the IEEE operations.  op 0: a[i] - b[i] through fixed-point copies
  * at scale 2^k (the FP64 subtraction when a value has no exact copy);
- * 1: sqrt(a[i]); 2: 1 / a[i]; 3: 2 / a[i]; 4: floor(a[i] / b[i]) as the
- * binning forms the cell index (a product with 1/b[i] away from integers).
- * out[i] receives the result. */
+ * 1: sqrt(a[i]); 2: 1 / a[i]; 3: 2 / a[i].  out[i] receives the result. */
 int sph_arith_check(int device, int op, int k, int n, const double* a, const double* b,
                     double* out);
 

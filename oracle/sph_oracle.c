@@ -328,6 +328,9 @@ static int64_t binary_one(orc_system* s, int op, int64_t p) {
   double acc = op == ORC_OP_DENSITY ? s->rho[p] : s->rho_ref[p];
   double ax = s->a[p][0], ay = s->a[p][1], az = s->a[p][2];
   double sx = s->xs[p][0], sy = s->xs[p][1], sz = s->xs[p][2];
+  /* XSPH: sum_q wx (v_q - v_p) formed as sum_q wx v_q - v_p sum_q wx, the
+   * two sums in the neighbour order */
+  double xw = 0.0, xv0 = 0.0, xv1 = 0.0, xv2 = 0.0;
   double wp = 0.0, wg = 0.0, ws = 0.0;
   const double* vp = s->v[p];
   const double rhop = s->rho[p], prp = s->Pr[p];
@@ -377,9 +380,10 @@ static int64_t binary_one(orc_system* s, int op, int64_t p) {
         ay = fma(cf, d[1], ay);
         az = fma(cf, d[2], az);
         const double wx = ((s->mcw * (t2 * t2)) * fma(-4.0, t, 5.0)) * inv_rb; /* m W / rho_bar */
-        sx = fma(-wx, dv0, sx); /* + wx (v_q - v_p) */
-        sy = fma(-wx, dv1, sy);
-        sz = fma(-wx, dv2, sz);
+        xw = xw + wx;
+        xv0 = fma(wx, s->v[q][0], xv0);
+        xv1 = fma(wx, s->v[q][1], xv1);
+        xv2 = fma(wx, s->v[q][2], xv2);
       } else {
         /* wall neighbour: pressure term only */
         const double ker = s->mcr * (t2 * t);
@@ -399,7 +403,9 @@ static int64_t binary_one(orc_system* s, int op, int64_t p) {
     s->rho[p] = s->p.rho0;
   } else {
     s->a[p][0] = ax; s->a[p][1] = ay; s->a[p][2] = az;
-    s->xs[p][0] = sx; s->xs[p][1] = sy; s->xs[p][2] = sz;
+    s->xs[p][0] = sx + fma(-vp[0], xw, xv0);
+    s->xs[p][1] = sy + fma(-vp[1], xw, xv1);
+    s->xs[p][2] = sz + fma(-vp[2], xw, xv2);
   }
   return pairs;
 }

@@ -406,26 +406,11 @@ __device__ __forceinline__ void eos_eval(const Consts& k, double rho, double rho
 
 // structs.jl:97-106 for an arbitrary point: -1 when a coordinate is NaN,
 // infinite or outside the Int64 range (the reference's try/catch).
-// floor(x / h) as the reference forms it -- floor of the correctly rounded
-// quotient (core.jl find_key) -- without the FP64 division unless the
-// quotient lies within a few ulps of an integer: q = x * fl(1/h) is within
-// 2^-52 |x/h| of x/h and fl(x/h) within 2^-53 of it, so both floors agree
-// when no integer lies within 2^-50 |q| of q.  Near an integer (positions on
-// a cell boundary, e.g. lattice walls) and for NaN the division decides.
-// The differences q - f and (f + 1) - q are exact where they are small.
-__device__ __forceinline__ double floor_div(double x, double h, double inv_h) {
-  const double q = x * inv_h;
-  const double f = floor(q);
-  const double tol = fabs(q) * 0x1p-50;
-  if (q - f > tol && (f + 1.0) - q > tol) return f;
-  return floor(x / h);
-}
-
 __device__ __forceinline__ long long find_key_point(const Geometry& g, const Consts& k,
                                                     const double x[3]) {
   long long ijk[3];
   for (int d = 0; d < 3; ++d) {
-    const double f = floor_div(x[d], k.h, k.inv_h);
+    const double f = floor(x[d] / k.h);
     if (!(f >= -9223372036854775808.0 && f < 9223372036854775808.0)) return -1;
     ijk[d] = 1 + (long long)f - g.key_phase[d];
   }

@@ -49,10 +49,14 @@ struct Proc64 {
   double vp[3];
   double rhop, prp;
   double acc, ax, ay, az, sx, sy, sz, wp, wg, ws;
+  // XSPH: sum_q wx (v_q - v_p) formed as sum_q wx v_q - v_p sum_q wx (the
+  // epilogue), the two sums in the neighbour order
+  double xw, xv0, xv1, xv2;
   int c0, c1, c2;
 
   __device__ Proc64(const State& s_, const Consts& k_) : s(s_), k(k_) {
     acc = ax = ay = az = sx = sy = sz = wp = wg = ws = 0.0;
+    xw = xv0 = xv1 = xv2 = 0.0;
     rhop = prp = 0.0;
     vp[0] = vp[1] = vp[2] = 0.0;
     c0 = c1 = c2 = 0;
@@ -112,9 +116,10 @@ struct Proc64 {
         ay = __fma_rn(cf, d[1], ay);
         if (DIM == 3) az = __fma_rn(cf, d[2], az);
         const double wx = ((k.mcw * (t2 * t2)) * __fma_rn(-4.0, t, 5.0)) * inv_rb;
-        sx = __fma_rn(-wx, dv0, sx);
-        sy = __fma_rn(-wx, dv1, sy);
-        if (DIM == 3) sz = __fma_rn(-wx, dv2, sz);
+        xw = xw + wx;
+        xv0 = __fma_rn(wx, vq[0], xv0);
+        xv1 = __fma_rn(wx, vq[1], xv1);
+        if (DIM == 3) xv2 = __fma_rn(wx, vq[2], xv2);
       } else {
         // wall neighbour: pressure term with the wall pressure
         const double ker = k.mcr * (t2 * t);
@@ -176,12 +181,13 @@ struct Proc64 {
         ay = __fma_rn(cf, d1, ay);
         if (DIM == 3) az = __fma_rn(cf, fx_sep2(X2, &s.x[2][i], QX2, &s.x[2][q], k.fx_k), az);
         if ((e & 0x80000000u) == 0u) {
-          // fluid neighbour: + wx (v_q - v_p)
+          // fluid neighbour: wx and wx v_q into the XSPH sums
           double qv1, qv2;
           frec_load_v12(b.frec + q, qv1, qv2);
-          sx = __fma_rn(-wx, vp[0] - qv0, sx);
-          sy = __fma_rn(-wx, vp[1] - qv1, sy);
-          if (DIM == 3) sz = __fma_rn(-wx, vp[2] - qv2, sz);
+          xw = xw + wx;
+          xv0 = __fma_rn(wx, qv0, xv0);
+          xv1 = __fma_rn(wx, qv1, xv1);
+          if (DIM == 3) xv2 = __fma_rn(wx, qv2, xv2);
           ++c0;
         } else {
           ++c1;
@@ -252,7 +258,10 @@ __device__ __forceinline__ void target_epilogue(const State& s, const Consts& k,
     s.Pr[i] = P / (k.rho0 * k.rho0);
     s.rho[i] = k.rho0;
   } else {
-    double ax = p.ax, ay = p.ay, az = p.az, sx = p.sx, sy = p.sy, sz = p.sz;
+    double ax = p.ax, ay = p.ay, az = p.az;
+    double sx = p.sx + __fma_rn(-p.vp[0], p.xw, p.xv0);
+    double sy = p.sy + __fma_rn(-p.vp[1], p.xw, p.xv1);
+    double sz = DIM == 3 ? p.sz + __fma_rn(-p.vp[2], p.xw, p.xv2) : p.sz;
     if (self) {
       const double ker = k.mass * ker_rdw(k, 0.0);
       const double inv_rb = 2.0 / (p.rhop + p.rhop);

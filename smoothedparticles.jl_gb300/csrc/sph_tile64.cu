@@ -678,10 +678,8 @@ __global__ void arith_check_kernel(int op, int k, int n, const double* a, const 
     r = isqrt_rn(x);
   } else if (op == 2) {
     r = ircp_rn(x);
-  } else if (op == 3) {
-    r = two_over(x);
   } else {
-    r = floor_div(x, b[i], 1.0 / b[i]);
+    r = two_over(x);
   }
   out[i] = r;
 }
@@ -699,9 +697,9 @@ cudaError_t launch_tiles_fp64(const LaunchCtx& c, const State& s, const Geometry
 
 extern "C" int sph_arith_check(int device, int op, int k, int n, const double* a, const double* b,
                                double* out) {
-  if (n < 0 || op < 0 || op > 4) return SPH_ERR_ARG;
+  if (n < 0 || op < 0 || op > 3) return SPH_ERR_ARG;
   if (n == 0) return SPH_OK;
-  if (!a || !out || ((op == 0 || op == 4) && !b)) return SPH_ERR_ARG;
+  if (!a || !out || (op == 0 && !b)) return SPH_ERR_ARG;
   int prev = 0;
   if (cudaGetDevice(&prev) != cudaSuccess || cudaSetDevice(device) != cudaSuccess) {
     cudaGetLastError();
@@ -713,7 +711,7 @@ extern "C" int sph_arith_check(int device, int op, int k, int n, const double* a
   if (cudaMalloc(&d, 3 * bytes) != cudaSuccess) {
     rc = SPH_ERR_NOMEM;
   } else if (cudaMemcpy(d, a, bytes, cudaMemcpyHostToDevice) != cudaSuccess ||
-             ((op == 0 || op == 4) && cudaMemcpy(d + n, b, bytes, cudaMemcpyHostToDevice) != cudaSuccess)) {
+             (op == 0 && cudaMemcpy(d + n, b, bytes, cudaMemcpyHostToDevice) != cudaSuccess)) {
     rc = SPH_ERR_CUDA;
   } else {
     sphgpu::arith_check_kernel<<<(n + 255) / 256, 256>>>(op, k, n, d, d + n, d + 2 * (size_t)n);

@@ -517,10 +517,9 @@ def memory_estimate(params: dict, n: int, precision: int = FP64) -> int:
 def arith_check(op: str, a, b=None, k: int = 59, device: int = 0):
     """The FP64 arithmetic the pair passes form on the integer pipes, applied
     on the device: op 'sub' (a - b through fixed-point copies at scale 2^k),
-    'sqrt', 'rcp' (1/a), 'two_over' (2/a) or 'floor_div' (floor(a / b) as
-    the binning forms cell indices).  For tests against IEEE results."""
+    'sqrt', 'rcp' (1/a) or 'two_over' (2/a).  For tests against IEEE results."""
     lib = L.load()
-    code = {"sub": 0, "sqrt": 1, "rcp": 2, "two_over": 3, "floor_div": 4}[op]
+    code = {"sub": 0, "sqrt": 1, "rcp": 2, "two_over": 3}[op]
     a = np.ascontiguousarray(a, dtype=np.float64)
     bb = np.ascontiguousarray(b if b is not None else a, dtype=np.float64)
     if bb.shape != a.shape:

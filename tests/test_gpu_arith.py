@@ -73,33 +73,3 @@ def test_fixed_point_difference_matches_ieee(gpu, k):
         want = a - b
     ok = same(got, want)
     assert ok.all(), (a[~ok][:5], b[~ok][:5], got[~ok][:5], want[~ok][:5])
-
-
-def test_floor_div_matches_ieee(gpu):
-    """The binning's cell index floor(x / h) without a division away from
-    integers equals numpy's floor of the IEEE quotient: random positions,
-    lattice points i*dr with h = 4 dr and 4.8 dr (many quotients exactly or
-    within an ulp of an integer), and values a few ulps either side of
-    multiples of h."""
-    rng = np.random.default_rng(11)
-    xs, hs = [], []
-    for dr in (0.0079, 0.0125, 0.02, 0.05, 0.0014, 1.0 / 3.0):
-        for fac in (4.0, 4.8, 2.0):
-            h = fac * dr
-            i = np.arange(-3000, 3000, dtype=np.float64)
-            x = i * dr
-            xs.append(x)
-            hs.append(np.full_like(x, h))
-            m = np.arange(-500, 500, dtype=np.float64) * h
-            for ulps in (-3, -2, -1, 1, 2, 3):
-                xs.append(m + ulps * np.spacing(m))
-                hs.append(np.full_like(m, h))
-    x = rng.uniform(-7.0, 7.0, 2_000_000)
-    xs.append(x)
-    hs.append(rng.choice([0.0316, 0.048, 0.00672, 0.1, 0.2], x.size))
-    a = np.concatenate(xs)
-    b = np.concatenate(hs)
-    got = sphgpu.arith_check("floor_div", a, b)
-    want = np.floor(a / b)
-    bad = np.nonzero(got != want)[0]
-    assert bad.size == 0, (a[bad[:5]], b[bad[:5]], got[bad[:5]], want[bad[:5]])
