@@ -744,12 +744,12 @@ PASS_KERNELS: dict = {"force": "one force pass: frec_build_kernel (particle reco
 
 # DRAM bytes (read + write) of one FP64 force pass from the ncu capture
 # summarised in profiles/fp64_tiles_3d_dr0.025.md: frec_build_kernel
-# 19,521,280 + 0 B, pair_list_kernel 961,536,256 + 1,082,870,528 B and
-# row_sum_kernel 1,132,064,768 + 21,510,656 B for the 3D dam break at
+# 19,521,024 + 1,280 B, pair_list_kernel 961,587,968 + 1,082,625,024 B and
+# row_sum_kernel 1,136,939,520 + 25,849,088 B for the 3D dam break at
 # dr = 0.025 (69,489,136 pair-interactions per step), scaled by
 # pair-interactions to the 5,746,633-particle case (2,078,775,269 per step).
-NCU_TRAFFIC: dict = {"force": int((19521280 + 961536256 + 1082870528 + 1132064768 + 21510656)
-                                  * 2078775269 / 69489136)}
+NCU_TRAFFIC: dict = {"force": int((19521024 + 1280 + 961587968 + 1082625024 + 1136939520
+                                   + 25849088) * 2078775269 / 69489136)}
 
 
 def main():
