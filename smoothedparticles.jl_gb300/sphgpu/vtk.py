@@ -110,6 +110,42 @@ def read_vtp(path: str) -> dict:
     return out
 
 
+# import_particles! reads these point-data arrays by the particle's field
+# names; the others stay at the constructor's values (zero here).
+_IMPORTED = ("v", "rho", "rho_ref", "type")
+
+
+def import_particles(system, path: str) -> int:
+    """import_particles!(sys, path, constructor) (IO.jl:83-118): the points of
+    the .vtp file at `path` are appended to the system's particles, in file
+    order, with every field the file holds under the system's field names
+    (v, rho, rho_ref, type); the others start at zero.  The particles already
+    in the system keep their reference order and fields (x, v, rho, rho_ref,
+    type; a later init_state or step recomputes the rest).  Returns the
+    number of particles added."""
+    d = read_vtp(path)
+    n_new = d["n"]
+    pts = np.asarray(d["points"], dtype=np.float64).reshape(n_new, 3)
+    pd = d["point_data"]
+    add = {"x": pts}
+    for f in _IMPORTED:
+        if f in pd:
+            a = np.asarray(pd[f])
+            add[f] = a.reshape(n_new, 3) if f == "v" else a.reshape(n_new)
+    n0 = system.n
+    old = {f: system.get(f) for f in ("x", "v", "rho", "rho_ref", "type")} if n0 else {}
+
+    def cat(f, shape, dtype):
+        a = old.get(f, np.zeros((0,) + shape, dtype))
+        b = add.get(f, np.zeros((n_new,) + shape, dtype)).astype(dtype)
+        return np.concatenate([a.reshape((-1,) + shape), b])
+
+    system.upload(cat("x", (3,), np.float64), cat("v", (3,), np.float64),
+                  rho=cat("rho", (), np.float64), rho_ref=cat("rho_ref", (), np.float64),
+                  type=cat("type", (), np.int32))
+    return n_new
+
+
 def read_pvd(path: str) -> list:
     """(time, file) of every frame of a collection."""
     root = ET.parse(path).getroot()
