@@ -52,7 +52,9 @@ extern "C" {
 #define SPH_OP_DENSITY 1       /* rho_p     += m W(r_pq); fluid p, every q         */
 #define SPH_OP_DENSITY_REF 2   /* rho_ref_p += m W(r_pq); fluid p, every q         */
 #define SPH_OP_FORCE 3         /* fluid p: a_p += pressure (+ Monaghan viscosity
-                                  between fluid particles); xsph_p += XSPH term */
+                                  between fluid particles); xsph_p += sum over
+                                  fluid q of wx (v_q - v_p), wx = m W / rho_bar,
+                                  formed (FP64) as sum wx v_q - v_p sum wx */
 #define SPH_OP_WALL_PRESSURE 4 /* wall p: P_p = (sum P_q W + sum rho_q (g.x_pq) W)
                                   / sum W over fluid q (Adami et al. 2012)       */
 /* ---- built-in unary operators: apply!(sys, op!) */
