@@ -37,6 +37,7 @@ struct orc_system {
   /* derived constants, computed once */
   double inv_h, cw, cr, B, hdt, eta2, alpha_c0, gmag;
   double mcw, mcr, ca; /* m C_w, m C_r, -(alpha c0) h_smooth */
+  double mcw5, mcw4;   /* 5 m C_w and -4 m C_w: m W = t^4 (5 m C_w - 4 m C_w t) */
   double c2, rho0sq;   /* c0^2, rho0^2 (ORC_EOS_LINEAR) */
   /* particles in the reference's order (0-based index = position in
    * sys.particles minus one) */
@@ -118,6 +119,8 @@ orc_system* orc_create(const orc_params* p) {
   s->eta2 = 0.01 * (p->h_smooth * p->h_smooth);
   s->alpha_c0 = p->alpha * p->c0;
   s->mcw = p->mass * s->cw;
+  s->mcw5 = 5.0 * s->mcw;
+  s->mcw4 = -4.0 * s->mcw;
   s->mcr = p->mass * s->cr;
   s->ca = -(s->alpha_c0 * p->h_smooth);
   s->gmag = fabs(p->gravity[p->vertical_axis]);
@@ -354,7 +357,7 @@ static int64_t binary_one(orc_system* s, int op, int64_t p) {
       const double t = ker_t(s, rk);
       const double t2 = t * t;
       if (op == ORC_OP_DENSITY || op == ORC_OP_DENSITY_REF) {
-        acc = acc + (s->mcw * (t2 * t2)) * fma(-4.0, t, 5.0); /* + m W */
+        acc = acc + (t2 * t2) * fma(s->mcw4, t, s->mcw5); /* + m W */
       } else if (op == ORC_OP_WALL_PRESSURE) {
         if (tq == ORC_FLUID) {
           const double w = (s->cw * (t2 * t2)) * fma(-4.0, t, 5.0);
@@ -379,7 +382,7 @@ static int64_t binary_one(orc_system* s, int op, int64_t p) {
         ax = fma(cf, d[0], ax);
         ay = fma(cf, d[1], ay);
         az = fma(cf, d[2], az);
-        const double wx = ((s->mcw * (t2 * t2)) * fma(-4.0, t, 5.0)) * inv_rb; /* m W / rho_bar */
+        const double wx = ((t2 * t2) * fma(s->mcw4, t, s->mcw5)) * inv_rb; /* m W / rho_bar */
         xw = xw + wx;
         xv0 = fma(wx, s->v[q][0], xv0);
         xv1 = fma(wx, s->v[q][1], xv1);

@@ -473,6 +473,8 @@ static int setup_host(const sph_params* p, sph_system* s) {
   k.eta2 = 0.01 * (p->h_smooth * p->h_smooth);
   k.alpha_c0 = p->alpha * p->c0;
   k.mcw = p->mass * k.cw;
+  k.mcw5 = 5.0 * k.mcw;
+  k.mcw4 = -4.0 * k.mcw;
   k.mcr = p->mass * k.cr;
   k.ca = -(k.alpha_c0 * p->h_smooth);
   k.h_smooth = p->h_smooth;

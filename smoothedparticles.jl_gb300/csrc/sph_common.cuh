@@ -77,6 +77,8 @@ struct Consts {
   double s_max;
   // folded constants of the FP64 pair arithmetic: m C_w, m C_r, -(alpha c0) h_smooth
   double mcw, mcr, ca;
+  // 5 m C_w and -4 m C_w: m W = t^4 fma(-4 m C_w, t, 5 m C_w)
+  double mcw5, mcw4;
   // scale of the positions' fixed-point copies: X = x 2^fx_k, |X| < 2^62
   // over the domain box
   int fx_k;

@@ -81,7 +81,7 @@ struct Proc64 {
       const double t = ker_t(k, r);
       const double t2 = t * t;
       if (OP == SPH_OP_DENSITY || OP == SPH_OP_DENSITY_REF) {
-        acc = acc + (k.mcw * (t2 * t2)) * __fma_rn(-4.0, t, 5.0);
+        acc = acc + (t2 * t2) * __fma_rn(k.mcw4, t, k.mcw5);
       } else if (OP == SPH_OP_WALL_PRESSURE) {
         // Adami, Hu & Adams (2012) wall pressure, g . (x_w - x_f)
         const double w = (k.cw * (t2 * t2)) * __fma_rn(-4.0, t, 5.0);
@@ -115,7 +115,7 @@ struct Proc64 {
         ax = __fma_rn(cf, d[0], ax);
         ay = __fma_rn(cf, d[1], ay);
         if (DIM == 3) az = __fma_rn(cf, d[2], az);
-        const double wx = ((k.mcw * (t2 * t2)) * __fma_rn(-4.0, t, 5.0)) * inv_rb;
+        const double wx = ((t2 * t2) * __fma_rn(k.mcw4, t, k.mcw5)) * inv_rb;
         xw = xw + wx;
         xv0 = __fma_rn(wx, vq[0], xv0);
         xv1 = __fma_rn(wx, vq[1], xv1);

@@ -558,7 +558,7 @@ __global__ void __launch_bounds__(256, PH == 0 ? 6 : 5) pair_list_kernel(State s
       const double r = isqrt_rn(ss);
       const double t = ker_t(k, r);
       const double t2 = t * t;
-      const double w = (k.mcw * (t2 * t2)) * __fma_rn(-4.0, t, 5.0);  // m W
+      const double w = (t2 * t2) * __fma_rn(k.mcw4, t, k.mcw5);  // m W
       if (fp && fq) {
         // t = 1 - r/H rides in the entry's spare slot, so that the force
         // pass of this binning starts its kernel derivative from it
