@@ -567,18 +567,18 @@ def run_ours(args):
     e2e_steps = args.e2e_steps if args.e2e_steps > 0 else args.steps
     torch.cuda.synchronize(dev)
     t0 = time.perf_counter()
+    ins = {f: h[f] for f in ("x", "v", "a", "xsph")}
+    outs = {f: h[f] for f in fields}
     for _ in range(e2e_steps):
-        for f in ("x", "v", "a", "xsph"):
-            g.set(f, h[f])
-        g.step(1)
-        for f in fields:
-            g.get(f, out=h[f])
+        g.step_io(ins, outs)
     t_e2e = time.perf_counter() - t0
     e2e = {"value": g.pair_count(reset=True) / t_e2e, "unit": UNIT,
            "h2d_bytes_per_step": int(n * 4 * 24), "d2h_bytes_per_step": int(n * (4 * 24 + 2 * 8)),
            "steps": e2e_steps, "ms_per_step": 1e3 * t_e2e / e2e_steps,
-           "note": "per step: set x, v, a, xsph from pinned host arrays; sph_step; get x, v, a, "
-                   "xsph, rho, P into pinned host arrays (reference particle order)"}
+           "note": "per step, one sph_step_io call: x, v, a, xsph set from pinned host arrays, "
+                   "one step, x, v, a, xsph, rho, P read into pinned host arrays (reference "
+                   "particle order; x after the binning and rho, P after the wall pressure are "
+                   "copied while the step's later passes run)"}
     # the FP64 run continues (untimed) to the comparison step
     done64 = args.warmup + args.steps + e2e_steps
     target = max(args.error_steps, done64)

@@ -168,6 +168,20 @@ int sph_sum_particle(sph_system* sys, int func, int64_t nq, const int64_t* index
  * on first use and kept until the system's buffers, particle count or tuning
  * change; the results are those of single steps. */
 int sph_step(sph_system* sys, int nsteps);
+
+/* One step with its host input and output, for a caller that keeps the
+ * particle state on the host between steps (no reference counterpart: the
+ * field reads and writes around a verlet_step! of a Julia time loop, in one
+ * call).  Sets the nin fields in_fields[i] from in[i] (as sph_set_field),
+ * takes one step (as sph_step(sys, 1)) and reads the nout fields
+ * out_fields[i] into out[i] (as sph_get_field, the count after the step's
+ * removals).  Each read starts on a second stream as soon as its field is
+ * final within the step -- positions, reference density, type, indices and
+ * keys after the binning, density and pressure after the wall pressure, the
+ * rest at the end -- so that its gather and copy overlap the step's
+ * remaining passes; reads into pageable memory all wait for the end. */
+int sph_step_io(sph_system* sys, int nin, const int32_t* in_fields, const void* const* in,
+                int nout, const int32_t* out_fields, void* const* out);
 /* Initial state of the dam break (collapse_symplectic.jl:186-191 plus the
  * hydrostatic reference density): bin, rho_ref sum, hydrostatic scaling,
  * density sum, EOS, wall pressure, force. */

@@ -633,6 +633,9 @@ int sph_destroy(sph_system* s) {
   if (s->need_host) cudaFreeHost(s->need_host);
   if (s->cells) cudaFree(s->cells);
   if (s->query) cudaFree(s->query);
+  for (auto e : s->io_ev)
+    if (e) cudaEventDestroy(e);
+  if (s->io_stream) cudaStreamDestroy(s->io_stream);
   cudaStreamDestroy(s->stream);
   delete s;
   return SPH_OK;
@@ -896,15 +899,9 @@ int sph_get_field(sph_system* s, int field, void* out) {
   return SPH_OK;
 }
 
-int sph_set_field(sph_system* s, int field, const void* in) {
-  if (!s || !in) return SPH_ERR_ARG;
-  if (field < SPH_FIELD_X || field > SPH_FIELD_TYPE)
-    return fail(s, SPH_ERR_ARG, "field %d cannot be set", field);
-  DeviceGuard guard(s->device);
-  int n = 0;
-  int rc = read_count(s, &n);
-  if (rc) return rc;
-  if (n == 0) return SPH_OK;
+// The host-side checks of a field about to be set (2D systems: no z
+// component; types: fluid or wall only).
+static int check_set(sph_system* s, int field, const void* in, int n) {
   if (s->params.dim == 2 && (field == SPH_FIELD_X || field == SPH_FIELD_V)) {
     const double* v = (const double*)in;
     for (int i = 0; i < n; ++i)
@@ -917,13 +914,32 @@ int sph_set_field(sph_system* s, int field, const void* in) {
       if (t[i] != SPH_FLUID && t[i] != SPH_WALL)
         return fail(s, SPH_ERR_ARG, "particle %d has unknown type %d", i, t[i]);
   }
+  return SPH_OK;
+}
+
+// What setting a field invalidates.
+static void after_set(sph_system* s, int field) {
+  if (field == SPH_FIELD_X) s->cells_valid = false;
+  if (field == SPH_FIELD_X || field == SPH_FIELD_TYPE) s->lists_valid = s->hits_valid = false;
+  s->aux_fluid = s->aux_wall = false;
+}
+
+int sph_set_field(sph_system* s, int field, const void* in) {
+  if (!s || !in) return SPH_ERR_ARG;
+  if (field < SPH_FIELD_X || field > SPH_FIELD_TYPE)
+    return fail(s, SPH_ERR_ARG, "field %d cannot be set", field);
+  DeviceGuard guard(s->device);
+  int n = 0;
+  int rc = read_count(s, &n);
+  if (rc) return rc;
+  if (n == 0) return SPH_OK;
+  rc = check_set(s, field, in, n);
+  if (rc) return rc;
   CK(cudaMemcpyAsync(s->staging, in, field_bytes(field, n), cudaMemcpyHostToDevice, s->stream));
   cudaError_t e = launch_field(ctx(s), s->cur, s->k, s->b, s->n_host, field, 1, s->staging);
   if (e != cudaSuccess) return fail(s, SPH_ERR_CUDA, "field: %s", cudaGetErrorString(e));
   CK(cudaStreamSynchronize(s->stream));
-  if (field == SPH_FIELD_X) s->cells_valid = false;
-  if (field == SPH_FIELD_X || field == SPH_FIELD_TYPE) s->lists_valid = s->hits_valid = false;
-  s->aux_fluid = s->aux_wall = false;
+  after_set(s, field);
   return SPH_OK;
 }
 
@@ -1054,6 +1070,113 @@ int sph_step(sph_system* s, int nsteps) {
     const int rc = step_once(s);
     if (rc) return rc;
   }
+  return SPH_OK;
+}
+
+// The phase of a step after which a field read by sph_step_io is final:
+// 0 after the binning (kick and drift done, state sorted), 1 after the wall
+// pressure (density and pressure of every particle), 2 at the end (the
+// force pass and the closing kick).
+static int final_phase(int field) {
+  switch (field) {
+    case SPH_FIELD_RHO:
+    case SPH_FIELD_P: return 1;
+    case SPH_FIELD_V:
+    case SPH_FIELD_A:
+    case SPH_FIELD_XSPH: return 2;
+    default: return 0;
+  }
+}
+
+int sph_step_io(sph_system* s, int nin, const int32_t* in_fields, const void* const* in, int nout,
+                const int32_t* out_fields, void* const* out) {
+  if (!s || nin < 0 || nout < 0 || (nin > 0 && (!in_fields || !in)) ||
+      (nout > 0 && (!out_fields || !out)))
+    return SPH_ERR_ARG;
+  for (int i = 0; i < nin; ++i)
+    if (in_fields[i] < SPH_FIELD_X || in_fields[i] > SPH_FIELD_TYPE || !in[i])
+      return fail(s, SPH_ERR_ARG, "input %d: field %d cannot be set", i, in_fields[i]);
+  for (int i = 0; i < nout; ++i)
+    if (out_fields[i] < SPH_FIELD_X || out_fields[i] > SPH_FIELD_KEY || !out[i])
+      return fail(s, SPH_ERR_ARG, "output %d: unknown field %d", i, out_fields[i]);
+  DeviceGuard guard(s->device);
+  int n = 0;
+  int rc = read_count(s, &n);
+  if (rc) return rc;
+  if (n == 0) return sph_step(s, 1);
+  if (!s->io_stream) {
+    CK(cudaStreamCreateWithFlags(&s->io_stream, cudaStreamNonBlocking));
+    for (auto& e : s->io_ev) CK(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+  }
+  // the inputs, one after the other through the staging area
+  for (int i = 0; i < nin; ++i) {
+    rc = check_set(s, in_fields[i], in[i], n);
+    if (rc) return rc;
+    CK(cudaMemcpyAsync(s->staging, in[i], field_bytes(in_fields[i], n), cudaMemcpyHostToDevice,
+                       s->stream));
+    cudaError_t e =
+        launch_field(ctx(s), s->cur, s->k, s->b, s->n_host, in_fields[i], 1, s->staging);
+    if (e != cudaSuccess) return fail(s, SPH_ERR_CUDA, "field: %s", cudaGetErrorString(e));
+    after_set(s, in_fields[i]);
+  }
+  // step_once, with an event after each phase that makes outputs final
+  rc = binning(s, 1, kGatherStep);
+  if (rc) return rc;
+  CK(cudaEventRecord(s->io_ev[0], s->stream));
+  // the particle count after the binning's removals sizes the reads
+  rc = read_count(s, &n);
+  if (rc) return rc;
+  rc = pair_pass(s, SPH_OP_DENSITY, 1, 1, 1);
+  if (!rc) rc = pair_pass(s, SPH_OP_WALL_PRESSURE, 0, 0, 0);
+  if (rc) return rc;
+  CK(cudaEventRecord(s->io_ev[1], s->stream));
+  // the reads final so far start now, on the second stream, while the rest
+  // of the step runs; each phase's fields share the staging area, which the
+  // next phase reuses once that stream has copied them out.  A copy into
+  // pageable memory would hold the host until it is done, so then every
+  // read waits for the end of the step.
+  bool pinned = true;
+  for (int i = 0; i < nout && pinned; ++i) {
+    cudaPointerAttributes a;
+    if (cudaPointerGetAttributes(&a, out[i]) != cudaSuccess) {
+      cudaGetLastError();
+      pinned = false;
+    } else {
+      pinned = a.type == cudaMemoryTypeHost;
+    }
+  }
+  const LaunchCtx quiet{s->io_stream, nullptr, nullptr};
+  const State cur = s->cur;  // the sorted state of this step
+  const size_t stage = 72 * (size_t)s->cap + 512;  // the staging area's bytes
+  auto reads = [&](int phase) -> int {
+    CK(cudaStreamWaitEvent(s->io_stream, s->io_ev[phase], 0));
+    size_t off = 0;
+    for (int i = 0; i < nout; ++i) {
+      if ((pinned ? final_phase(out_fields[i]) : 2) != phase) continue;
+      const size_t bytes = field_bytes(out_fields[i], n);
+      if (off + bytes > stage) {  // the area is full: let the copies drain
+        CK(cudaStreamSynchronize(s->io_stream));
+        off = 0;
+      }
+      char* st = (char*)s->staging + off;
+      cudaError_t e = launch_field(quiet, cur, s->k, s->b, s->n_host, out_fields[i], 0, st);
+      if (e != cudaSuccess) return fail(s, SPH_ERR_CUDA, "field: %s", cudaGetErrorString(e));
+      CK(cudaMemcpyAsync(out[i], st, bytes, cudaMemcpyDeviceToHost, s->io_stream));
+      off += align_up(bytes);
+    }
+    return SPH_OK;
+  };
+  rc = reads(0);
+  if (!rc) rc = reads(1);
+  if (rc) return rc;
+  rc = pair_pass(s, SPH_OP_FORCE, 0, 1, 0);
+  if (!rc) rc = unary(s, SPH_OP_KICK);
+  if (rc) return rc;
+  CK(cudaEventRecord(s->io_ev[2], s->stream));
+  rc = reads(2);
+  if (rc) return rc;
+  CK(cudaStreamSynchronize(s->io_stream));
+  CK(cudaStreamSynchronize(s->stream));
   return SPH_OK;
 }
 

@@ -65,6 +65,10 @@ struct sph_system {
   long long generation = 0;
   // sph_step's captured two-step graph (a batch of this system alone)
   sph_batch* solo = nullptr;
+  // sph_step_io: the stream its reads run on and the events they wait for
+  // (after the binning, after the wall pressure, at the end of the step)
+  cudaStream_t io_stream = nullptr;
+  cudaEvent_t io_ev[3] = {nullptr, nullptr, nullptr};
 };
 
 namespace sphgpu {

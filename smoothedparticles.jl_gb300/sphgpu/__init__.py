@@ -229,6 +229,45 @@ class ParticleSystem:
         CUDA graph of this system, with the same results."""
         self._check(self._lib.sph_step(self._h, int(nsteps)))
 
+    def step_io(self, inputs: dict, outputs: dict) -> dict:
+        """One step with host input and output (sph_step_io): the arrays of
+        ``inputs`` (field name -> array) are set, one step is taken, and the
+        fields named in ``outputs`` are read into its arrays (C-contiguous, of
+        the dtype and shape ``get`` returns for the count before the step;
+        with removals only the leading rows are written).  Reads into pinned
+        arrays overlap the rest of the step.  Returns ``outputs``."""
+        n = self.n
+        ins = []
+        for name, vals in inputs.items():
+            f = _FIELDS[name]
+            if f in _VECTOR:
+                a = np.ascontiguousarray(vals, dtype=np.float64).reshape(n, 3)
+            elif f == L.SPH_FIELD_TYPE:
+                a = np.ascontiguousarray(vals, dtype=np.int32).reshape(n)
+            else:
+                a = np.ascontiguousarray(vals, dtype=np.float64).reshape(n)
+            ins.append((f, a))
+        outs = []
+        for name, arr in outputs.items():
+            f = _FIELDS[name]
+            if f in _VECTOR:
+                shape, dt = (n, 3), np.float64
+            elif f == L.SPH_FIELD_TYPE:
+                shape, dt = (n,), np.int32
+            elif f in (L.SPH_FIELD_OID, L.SPH_FIELD_KEY):
+                shape, dt = (n,), np.int64
+            else:
+                shape, dt = (n,), np.float64
+            if arr.shape != shape or arr.dtype != dt or not arr.flags.c_contiguous:
+                raise ValueError(f"{name}: a C-contiguous {dt.__name__} array of shape {shape}")
+            outs.append((f, arr))
+        fi = (C.c_int32 * max(len(ins), 1))(*[f for f, _ in ins])
+        pi = (C.c_void_p * max(len(ins), 1))(*[a.ctypes.data for _, a in ins])
+        fo = (C.c_int32 * max(len(outs), 1))(*[f for f, _ in outs])
+        po = (C.c_void_p * max(len(outs), 1))(*[a.ctypes.data for _, a in outs])
+        self._check(self._lib.sph_step_io(self._h, len(ins), fi, pi, len(outs), fo, po))
+        return outputs
+
     def init_state(self):
         """The dam-break initialisation (collapse_symplectic.jl:186-191 + hydrostatic)."""
         self._check(self._lib.sph_init_state(self._h))

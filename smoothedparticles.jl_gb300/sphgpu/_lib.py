@@ -166,6 +166,8 @@ PROTOTYPES = {
     "sph_sum_point": (C.c_int, [_P, C.c_int, _I64, _P, _P]),
     "sph_sum_particle": (C.c_int, [_P, C.c_int, _I64, _P, _P]),
     "sph_step": (C.c_int, [_P, C.c_int]),
+    "sph_step_io": (C.c_int, [_P, C.c_int, C.c_void_p, C.c_void_p, C.c_int, C.c_void_p,
+                              C.c_void_p]),
     "sph_init_state": (C.c_int, [_P]),
     "sph_pair_count": (C.c_int, [_P, C.POINTER(C.c_uint64), C.c_int]),
     "sph_synchronize": (C.c_int, [_P]),
