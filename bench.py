@@ -103,6 +103,8 @@ def parse():
     ap.add_argument("--ens-members", type=int, default=256)
     ap.add_argument("--ens-steps", type=int, default=1000)
     ap.add_argument("--ens-seed", type=int, default=2024)
+    ap.add_argument("--ens-cell-tune", type=int, default=1,
+                    help="1: tune the mixed members' cell factor per size class first")
     # served stream of solve requests (continuous batching, HBM budget)
     ap.add_argument("--serve-requests", type=int, default=100)
     ap.add_argument("--serve-rate", type=float, default=2.0, help="arrivals per second")
@@ -378,14 +380,21 @@ def run_ensemble(args, torch, dev):
     t0 = time.perf_counter()
     cases = ensemble_cases(args.ens_members, seed=args.ens_seed)
     t_geo = time.perf_counter() - t0
-    mem = []
-    for c in cases:
-        g = sphgpu.ParticleSystem(c.params, sphgpu.MIXED, device=dev)
+
+    def make(c, factor):
+        g = sphgpu.ParticleSystem(dict(c.params, cell_factor=factor), sphgpu.MIXED, device=dev)
         g.upload(c.x, c.v, type=c.type)
         g.init_state()
-        mem.append(g)
+        return g
+
+    # the cell size per size class first (the members are rebuilt for each
+    # candidate), then the launch shape on the members as built
     t0 = time.perf_counter()
-    table = autotune.tune_batch(mem, steps=4)
+    table = autotune.tune_cell_factor(cases, make, steps=4) if args.ens_cell_tune else {}
+    t_cell = time.perf_counter() - t0
+    mem = [make(c, f) for c, f in zip(cases, autotune.cell_factors(cases, table))]
+    t0 = time.perf_counter()
+    table.update(autotune.tune_batch(mem, steps=4))
     t_tune = time.perf_counter() - t0
     b = sphgpu.Batch(mem)
     autotune.apply(mem, table, b)
@@ -440,7 +449,8 @@ def run_ensemble(args, torch, dev):
                               "graph of that member alone), host timer"},
         "autotune": autotune.describe(table),
         "tuned": {k: v["choice"] for k, v in autotune.describe(table).items()},
-        "autotune_s": t_tune, "setup_lattices_s": t_geo, "clocks": clk.summary(),
+        "autotune_s": t_tune, "cell_tune_s": t_cell, "setup_lattices_s": t_geo,
+        "clocks": clk.summary(),
         "l2": "no flush: resident state of all members > 129 MB L2",
         "chain_floor": dict(floor, share_of_step=round(floor["ms_per_step"] / (ms / S), 4)),
     }

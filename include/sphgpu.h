@@ -26,7 +26,7 @@
 extern "C" {
 #endif
 
-#define SPHGPU_ABI_VERSION 1
+#define SPHGPU_ABI_VERSION 2
 
 /* ---- status codes */
 #define SPH_OK 0
@@ -104,6 +104,11 @@ typedef struct sph_params {
   double col_height;     /* free-surface height for SPH_OP_HYDROSTATIC           */
   int32_t vertical_axis; /* 0-based axis along gravity                           */
   int32_t eos;           /* SPH_EOS_TAIT (0) or SPH_EOS_LINEAR (1), below         */
+  double cell_factor;    /* cell size / h: 0 or 1 = the reference's cells of size h
+                            (structs.jl:66-68); SPH_PREC_MIXED systems accept
+                            1..2 (the pair set does not depend on it; the
+                            neighbour order and the FP32 sums do).  No
+                            reference counterpart; ABI version 2. */
 } sph_params;
 
 /* Equation of state of SPH_OP_EOS and of the step's fused EOS, and the

@@ -424,13 +424,21 @@ static int setup_host(const sph_params* p, sph_system* s) {
     if (!(p->domain_min[d] <= p->domain_max[d])) return SPH_ERR_ARG;
   if (p->dim == 2 && (p->domain_min[2] > 0.0 || p->domain_max[2] < 0.0)) return SPH_ERR_ARG;
   if (p->eos != SPH_EOS_TAIT && p->eos != SPH_EOS_LINEAR) return SPH_ERR_ARG;
+  // the cell factor: the reference's cells (0 or 1) for every system, up to
+  // 2 h for mixed-precision ones (the FP64 path sums in the reference's
+  // neighbour order, which the cells define)
+  const double cf = p->cell_factor == 0.0 ? 1.0 : p->cell_factor;
+  if (!(cf >= 1.0 && cf <= 2.0)) return SPH_ERR_ARG;
+  if (cf != 1.0 && p->precision != SPH_PREC_MIXED) return SPH_ERR_ARG;
   s->params = *p;
-  // structs.jl:64-82
+  // structs.jl:64-82, with cells of size Hc (H unless a mixed system asks
+  // for larger ones)
   const double H = p->h;
+  const double Hc = cf == 1.0 ? H : H * cf;
   long long key_max = 1;
   for (int d = 0; d < 3; ++d) {
-    s->geo.key_phase[d] = (long long)std::floor(p->domain_min[d] / H);
-    s->geo.key_lim[d] = (long long)std::floor(p->domain_max[d] / H) - s->geo.key_phase[d] + 1;
+    s->geo.key_phase[d] = (long long)std::floor(p->domain_min[d] / Hc);
+    s->geo.key_lim[d] = (long long)std::floor(p->domain_max[d] / Hc) - s->geo.key_phase[d] + 1;
     key_max *= s->geo.key_lim[d];
   }
   if (key_max <= 0 || key_max > 0x7fffffffLL - 8)
@@ -488,7 +496,8 @@ static int setup_host(const sph_params* p, sph_system* s) {
     k.dmax[d] = p->domain_max[d];
   }
   const double band = 1.0 / 16384.0;  // 2^-14, see sph_pair64.cu
-  k.hf = (float)H;
+  k.cell = Hc;
+  k.cellf = (float)Hc;
   k.s_lo = (float)(h2 * (1.0 - band));
   k.s_hi = (float)(h2 * (1.0 + band));
   // largest double whose correctly rounded square root is <= H

@@ -70,8 +70,8 @@ __device__ __forceinline__ float4 rel_to(const Geometry& g, const Consts& k, con
                                          int cx, int cy, int cz, int nk) {
   int qx, qy, qz;
   decode_key(g, nk, qx, qy, qz);
-  return make_float4(pi.x - (float)(qx - cx) * k.hf, pi.y - (float)(qy - cy) * k.hf,
-                     pi.z - (float)(qz - cz) * k.hf, 0.f);
+  return make_float4(pi.x - (float)(qx - cx) * k.cellf, pi.y - (float)(qy - cy) * k.cellf,
+                     pi.z - (float)(qz - cz) * k.cellf, 0.f);
 }
 
 // div_L_lambda! (collapse_dry_implicit.jl:140-145) of particle i over its

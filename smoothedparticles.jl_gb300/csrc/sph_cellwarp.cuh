@@ -53,8 +53,8 @@ __device__ __forceinline__ float4 cw_offset(const Geometry& g, const Consts& k, 
                                             int nk) {
   int qx, qy, qz;
   decode_key(g, nk, qx, qy, qz);
-  return make_float4((float)(qx - t.cx) * k.hf, (float)(qy - t.cy) * k.hf,
-                     (float)(qz - t.cz) * k.hf, 0.f);
+  return make_float4((float)(qx - t.cx) * k.cellf, (float)(qy - t.cy) * k.cellf,
+                     (float)(qz - t.cz) * k.cellf, 0.f);
 }
 
 // Fills sh.offs for every neighbour cell (lanes 0..n_diff-1, one each).

@@ -72,7 +72,11 @@ struct Consts {
   // FP32 candidate classification (see the pair kernels): a candidate whose
   // FP32 squared distance lies below s_lo is inside the support, above s_hi
   // outside; in between the FP64 test decides.
-  float hf, s_lo, s_hi;
+  float s_lo, s_hi;
+  // the cell size (the support h, or h times the mixed systems' cell factor)
+  // and its FP32 copy, of the cell keys, origins and neighbour-cell offsets
+  double cell;
+  float cellf;
   // the largest double s with sqrt_rn(s) <= h: r > h  <=>  fl64(r^2 sum) > s_max
   double s_max;
   // folded constants of the FP64 pair arithmetic: m C_w, m C_r, -(alpha c0) h_smooth
@@ -412,7 +416,7 @@ __device__ __forceinline__ long long find_key_point(const Geometry& g, const Con
                                                     const double x[3]) {
   long long ijk[3];
   for (int d = 0; d < 3; ++d) {
-    const double f = floor(x[d] / k.h);
+    const double f = floor(x[d] / k.cell);
     if (!(f >= -9223372036854775808.0 && f < 9223372036854775808.0)) return -1;
     ijk[d] = 1 + (long long)f - g.key_phase[d];
   }

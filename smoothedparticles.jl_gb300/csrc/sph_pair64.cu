@@ -480,9 +480,9 @@ __global__ void __launch_bounds__(128) debug_pairs_kernel(State s, Geometry g, C
     if (nk < 1 || nk > g.key_max) continue;
     int qx, qy, qz;
     decode_key(g, nk, qx, qy, qz);
-    const float ox = (float)(qx - cx) * k.hf;
-    const float oy = (float)(qy - cy) * k.hf;
-    const float oz = (float)(qz - cz) * k.hf;
+    const float ox = (float)(qx - cx) * k.cellf;
+    const float oy = (float)(qy - cy) * k.cellf;
+    const float oz = (float)(qz - cz) * k.cellf;
     for (int q = b.cell_start[nk]; q < b.cell_start[nk + 1]; ++q) {
       const float4 pq = s.pl[q];
       const float dx = (pi4.x - pq.x) - ox;

@@ -142,9 +142,9 @@ __device__ __forceinline__ void tile_run(const State& s, const Geometry& g, cons
   int acx, acy, acz, bcx, bcy, bcz;
   decode_key(g, a, acx, acy, acz);
   decode_key(g, nk, bcx, bcy, bcz);
-  const float ox = (float)(bcx - acx) * k.hf;
-  const float oy = (float)(bcy - acy) * k.hf;
-  const float oz = (float)(bcz - acz) * k.hf;
+  const float ox = (float)(bcx - acx) * k.cellf;
+  const float oy = (float)(bcy - acy) * k.cellf;
+  const float oz = (float)(bcz - acz) * k.cellf;
   const int nA = (na + 31) >> 5, nB = (nb + 31) >> 5;
   int ln = 0;  // pairs buffered
   for (int ia = 0; ia < nA; ++ia) {

@@ -43,6 +43,7 @@ struct SphParams
     col_height::Float64
     vertical_axis::Int32
     eos::Int32           # 0: Tait (P/rho^2 in the force), 1: linear c0^2 (rho - rho0) (P/rho0^2)
+    cell_factor::Float64 # cell size / h: 0 or 1 (the reference's cells); 1..2 for mixed precision
 end
 
 abstract type BuiltinOperator end

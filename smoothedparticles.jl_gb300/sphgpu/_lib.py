@@ -80,6 +80,7 @@ class sph_params(C.Structure):
         ("col_height", C.c_double),
         ("vertical_axis", C.c_int32),
         ("eos", C.c_int32),
+        ("cell_factor", C.c_double),
     ]
 
 
@@ -140,6 +141,8 @@ def make_params(cls, p: dict, precision: int = 0):
         setattr(s, name, float(p[name]))
     s.vertical_axis = int(p["vertical_axis"])
     s.eos = int(p.get("eos", SPH_EOS_TAIT))
+    if any(f[0] == "cell_factor" for f in cls._fields_):
+        s.cell_factor = float(p.get("cell_factor", 0.0))
     return s
 
 

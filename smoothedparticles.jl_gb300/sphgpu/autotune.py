@@ -1,6 +1,12 @@
 """Autotuner of the pair passes' launch shape for batched ensembles.
 
-Two knobs:
+Three knobs:
+
+* the cell size of mixed-precision members (sph_params.cell_factor: cells of
+  1, 1.15 or 1.3 times the support): larger cells hold more of a warp's 32
+  lanes of targets but add candidates; the pair set never changes, the
+  neighbour order (and so the FP32 sums) does.  Chosen per size class on the
+  members' initial states (the systems are rebuilt for each candidate);
 
 * warps per block of the pair passes (2, 4 or 8, i.e. 64, 128 or 256
   threads): how many work items (<= 32 targets of one cell each) share a
@@ -26,6 +32,7 @@ import math
 
 CHOICES = (2, 4, 8)
 THREADS = (32, 64, 128)
+FACTORS = (1.0, 1.15, 1.3)
 
 
 def size_class(n: int) -> int:
@@ -51,6 +58,44 @@ def _classes(systems):
         classes.setdefault(size_class(g.n), []).append(g)
     weight = {c: sum(g.n for g in gs) for c, gs in classes.items()}
     return classes, sorted(classes, key=lambda c: -weight[c])
+
+
+def tune_cell_factor(cases, make, steps: int = 4, factors=FACTORS) -> dict:
+    """Chooses every size class's cell factor by timing the batched graph of
+    all members built by ``make(case, factor)`` (a mixed-precision system at
+    its initial state): the class at each candidate, the other classes at
+    their current choice (one sweep of coordinate descent, the classes with
+    the most particles first).  Returns {("cell", size_class): (factor,
+    {factor: ms})}; the trial systems are closed."""
+    import sphgpu
+    cls = {}
+    for c in cases:
+        cls.setdefault(size_class(c.n), []).append(c)
+    order = sorted(cls, key=lambda k: -sum(c.n for c in cls[k]))
+    choice = {k: 1.0 for k in cls}
+    table = {}
+    for k in order:
+        times = {}
+        for f in factors:
+            trial = dict(choice)
+            trial[k] = f
+            systems = [make(c, trial[size_class(c.n)]) for c in cases]
+            b = sphgpu.Batch(systems)
+            try:
+                times[f] = _time(b, steps)
+            finally:
+                b.close()
+                for g in systems:
+                    g.close()
+        choice[k] = min(times, key=times.get)
+        table[("cell", k)] = (choice[k], times)
+    return table
+
+
+def cell_factors(cases, table: dict) -> list:
+    """Each case's cell factor from a tune_cell_factor table (1 where the
+    table has no entry for its size class)."""
+    return [table.get(("cell", size_class(c.n)), (1.0, None))[0] for c in cases]
 
 
 def tune_batch(systems, steps: int = 4, choices=CHOICES, threads=THREADS) -> dict:
@@ -125,8 +170,9 @@ def describe(table: dict) -> dict:
     choices and the timings behind them."""
     out = {}
     for k, (best, times) in table.items():
-        key = k if isinstance(k, str) else (f"threads@2^{k[1]}" if isinstance(k, tuple)
-                                            else f"warps@2^{k}")
+        key = k if isinstance(k, str) else (f"{'cell' if k[0] == 'cell' else 'threads'}@2^{k[1]}"
+                                            if isinstance(k, tuple) else f"warps@2^{k}")
         out[key] = {"choice": best, "ms_per_step": {str(v): round(t, 4) for v, t in times.items()},
-                    "spread": round(max(times.values()) / min(times.values()) - 1.0, 4)}
+                    "spread": round(max(times.values()) / min(times.values()) - 1.0, 4)
+                    if min(times.values()) > 0 else 0.0}
     return out

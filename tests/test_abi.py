@@ -59,7 +59,7 @@ int main(void) {
 
 def test_invalid_calls_fail_without_gpu(sph_lib):
     from sphgpu import _lib
-    assert sph_lib.sph_abi_version() == 1
+    assert sph_lib.sph_abi_version() == 2
     assert sph_lib.sph_destroy(None) == _lib.SPH_ERR_ARG
     assert sph_lib.sph_last_error(None) == b"null handle"
     p = _lib.sph_params()

@@ -93,3 +93,67 @@ def test_dam_break_shapes_params_match_host_case():
         assert dev.params == host.params
         assert [s["type"] for s in dev.shapes] == [G.FLUID, G.WALL]
         assert dev.shapes[1]["keep_axis"] == (-1 if kw.get("lid") else dim - 1)
+
+
+def test_cell_factor_parameter_host_only(sph_lib):
+    """sph_params.cell_factor (ABI version 2): mixed systems accept 1..2 and
+    hold fewer cells with larger ones; FP64 systems keep the reference's."""
+    import pytest
+    import sphgpu
+    from sphgpu import geometry as G
+    c = G.dam_break(2, 0.01)
+    base = sphgpu.memory_estimate(c.params, 5000, sphgpu.MIXED)
+    larger = sphgpu.memory_estimate(dict(c.params, cell_factor=1.5), 5000, sphgpu.MIXED)
+    assert larger < base
+    assert sphgpu.memory_estimate(dict(c.params, cell_factor=1.0), 5000, sphgpu.MIXED) == base
+    for bad, prec in ((1.5, sphgpu.FP64), (0.9, sphgpu.MIXED), (2.1, sphgpu.MIXED)):
+        with pytest.raises(sphgpu.SphError):
+            sphgpu.memory_estimate(dict(c.params, cell_factor=bad), 5000, prec)
+
+
+def test_tune_cell_factor_coordinate_descent(monkeypatch):
+    """tune_cell_factor on fakes: every class tried at every factor with the
+    other classes at their current choice (largest classes first), the
+    trial systems built by `make` and all closed again."""
+    import sphgpu
+    from sphgpu.geometry import Case  # noqa: F401  (the cases need only .n)
+
+    class FakeCase:
+        def __init__(self, n):
+            self.n = n
+
+    built, closed = [], []
+
+    class FakeSys:
+        def __init__(self, case, f):
+            self.case, self.f = case, f
+            built.append(self)
+
+        def close(self):
+            closed.append(self)
+
+    class FakeBatch:
+        def __init__(self, systems):
+            self.systems = systems
+
+        def close(self):
+            pass
+
+    # cost: class 2^10 prefers 1.15, class 2^12 prefers 1.0
+    def fake_time(batch, steps):
+        t = 1.0
+        for g in batch.systems:
+            c = autotune.size_class(g.case.n)
+            t += abs(g.f - (1.15 if c == 10 else 1.0)) * g.case.n
+        return t
+
+    monkeypatch.setattr(sphgpu, "Batch", FakeBatch)
+    monkeypatch.setattr(autotune, "_time", fake_time)
+    cases = [FakeCase(1500), FakeCase(1100), FakeCase(5000)]
+    table = autotune.tune_cell_factor(cases, FakeSys, steps=2)
+    assert table[("cell", 10)][0] == 1.15 and table[("cell", 12)][0] == 1.0
+    assert set(table[("cell", 10)][1]) == set(autotune.FACTORS)
+    assert len(built) == len(closed) == 2 * len(autotune.FACTORS) * len(cases)
+    assert autotune.cell_factors(cases, table) == [1.15, 1.15, 1.0]
+    d = autotune.describe(table)
+    assert d["cell@2^10"]["choice"] == 1.15

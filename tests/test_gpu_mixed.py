@@ -180,3 +180,51 @@ def test_mixed_error_against_oracle(gpu, oracle_mod, dim, dr):
     assert g.n == o.n
     assert e1["x_over_dr"] <= 1e-6
     g.close()
+
+
+@pytest.mark.parametrize("dim,dr,steps,factor", [(2, 0.02, 0, 1.25), (2, 0.02, 20, 1.6),
+                                                 (3, 0.05, 0, 1.25), (3, 0.05, 4, 2.0)])
+def test_larger_cells_keep_the_pair_set(gpu, oracle_mod, dim, dr, steps, factor):
+    """A mixed system with cells of factor * h (sph_params.cell_factor): the
+    pair set the density pass acts on is still the oracle's (as a set: the
+    neighbour order follows the larger cells), and the fields stay within
+    the mixed path's bounds of the oracle after the initial state."""
+    c = G.dam_break(dim, dr)
+    o, st = _oracle_state_after(oracle_mod, c, steps)
+    ref = o.pairs()
+    ref = ref[st["type"][ref[:, 0]] == G.FLUID]
+    params = dict(c.params, cell_factor=factor)
+    g = sphgpu.ParticleSystem(params, sphgpu.MIXED)
+    g.upload(st["x"], st["v"], type=st["type"])
+    g.create_cell_list()
+    assert g.geometry()["key_max"] < o.geometry()["key_max"]  # fewer, larger cells
+    sphgpu.apply(g, sphgpu.reset_rho)
+    sphgpu.apply(g, sphgpu.find_rho, self=True)
+    hits = g.debug_hits()
+    key = lambda a: a[np.lexsort((a[:, 1], a[:, 0]))]
+    assert hits.shape == ref.shape
+    assert np.array_equal(key(hits), key(ref))
+    g.close()
+
+    g = sphgpu.ParticleSystem(params, sphgpu.MIXED)
+    g.upload(c.x, c.v, type=c.type)
+    o = oracle_mod.from_case(c)
+    g.init_state()
+    o.init_state()
+    s = o.state()
+    fl = s["type"] == G.FLUID
+    assert (np.abs(s["rho"] - g.get("rho"))[fl] / s["rho"][fl]).max() <= 1e-6
+    assert np.abs(s["P"] - g.get("P")).max() / np.abs(s["P"]).max() <= 2e-6
+    assert np.linalg.norm(s["a"] - g.get("a")) / np.linalg.norm(s["a"]) <= 5e-6
+    g.close()
+
+
+def test_cell_factor_limits(gpu):
+    """FP64 systems keep the reference's cells; mixed ones accept 1..2."""
+    c = G.dam_break(2, 0.05)
+    with pytest.raises(sphgpu.SphError):
+        sphgpu.ParticleSystem(dict(c.params, cell_factor=1.25), sphgpu.FP64)
+    for bad in (0.5, 2.5):
+        with pytest.raises(sphgpu.SphError):
+            sphgpu.ParticleSystem(dict(c.params, cell_factor=bad), sphgpu.MIXED)
+    sphgpu.ParticleSystem(dict(c.params, cell_factor=1.0), sphgpu.FP64).close()
