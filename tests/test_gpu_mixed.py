@@ -183,12 +183,17 @@ def test_mixed_error_against_oracle(gpu, oracle_mod, dim, dr):
 
 
 @pytest.mark.parametrize("dim,dr,steps,factor", [(2, 0.02, 0, 1.25), (2, 0.02, 20, 1.6),
-                                                 (3, 0.05, 0, 1.25), (3, 0.05, 4, 2.0)])
+                                                 (2, 0.02, 20, 2.0), (3, 0.05, 0, 1.25),
+                                                 (3, 0.05, 4, 1.2), (3, 0.05, 4, 2.0)])
 def test_larger_cells_keep_the_pair_set(gpu, oracle_mod, dim, dr, steps, factor):
     """A mixed system with cells of factor * h (sph_params.cell_factor): the
     pair set the density pass acts on is still the oracle's (as a set: the
     neighbour order follows the larger cells), and the fields stay within
-    the mixed path's bounds of the oracle after the initial state."""
+    the mixed path's bounds of the oracle after the initial state.  In 3D a
+    factor of 2 puts ~512 particles in a cell, more chunks per work item
+    than the stored hit masks take: those targets traverse in the force pass
+    too (same results), and sph_debug_hits, which lists stored masks only,
+    refuses -- the fields are checked there."""
     c = G.dam_break(dim, dr)
     o, st = _oracle_state_after(oracle_mod, c, steps)
     ref = o.pairs()
@@ -200,10 +205,14 @@ def test_larger_cells_keep_the_pair_set(gpu, oracle_mod, dim, dr, steps, factor)
     assert g.geometry()["key_max"] < o.geometry()["key_max"]  # fewer, larger cells
     sphgpu.apply(g, sphgpu.reset_rho)
     sphgpu.apply(g, sphgpu.find_rho, self=True)
-    hits = g.debug_hits()
-    key = lambda a: a[np.lexsort((a[:, 1], a[:, 0]))]
-    assert hits.shape == ref.shape
-    assert np.array_equal(key(hits), key(ref))
+    if dim == 3 and factor > 1.5:
+        with pytest.raises(sphgpu.SphError):
+            g.debug_hits()
+    else:
+        hits = g.debug_hits()
+        key = lambda a: a[np.lexsort((a[:, 1], a[:, 0]))]
+        assert hits.shape == ref.shape
+        assert np.array_equal(key(hits), key(ref))
     g.close()
 
     g = sphgpu.ParticleSystem(params, sphgpu.MIXED)
