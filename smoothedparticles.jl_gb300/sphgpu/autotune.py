@@ -3,8 +3,8 @@
 Three knobs:
 
 * the cell size of mixed-precision members (sph_params.cell_factor: cells of
-  1, 1.15 or 1.3 times the support): larger cells hold more of a warp's 32
-  lanes of targets but add candidates; the pair set never changes, the
+  1 to 1.3 times the support): larger cells fill more of a warp's 32 lanes
+  of targets and of each 32-candidate chunk but add candidates; the pair set never changes, the
   neighbour order (and so the FP32 sums) does.  Chosen per size class on the
   members' initial states (the systems are rebuilt for each candidate);
 
@@ -32,7 +32,7 @@ import math
 
 CHOICES = (2, 4, 8)
 THREADS = (32, 64, 128)
-FACTORS = (1.0, 1.15, 1.3)
+FACTORS = (1.0, 1.08, 1.15, 1.22, 1.3)
 
 
 def size_class(n: int) -> int:
