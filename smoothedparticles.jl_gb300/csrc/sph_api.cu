@@ -435,10 +435,20 @@ static int setup_host(const sph_params* p, sph_system* s) {
   // for larger ones)
   const double H = p->h;
   const double Hc = cf == 1.0 ? H : H * cf;
+  // Mixed systems shift their grid by 5/16 of a cell.  A lattice whose
+  // spacing divides the cell (h = 4 dr in 3D) otherwise has whole planes of
+  // particles exactly on cell boundaries, which rounding in the first steps
+  // scatters to either side: cells of 65 particles take three work items.
+  // With the shift such planes lie a quarter spacing (h = 4 dr) or a tenth
+  // (h = 4.8 dr) away from every boundary.  The pair set does not depend on
+  // the grid; the FP64 path sums in the reference's cell order and keeps it.
+  double shift[3];
   long long key_max = 1;
   for (int d = 0; d < 3; ++d) {
-    s->geo.key_phase[d] = (long long)std::floor(p->domain_min[d] / Hc);
-    s->geo.key_lim[d] = (long long)std::floor(p->domain_max[d] / Hc) - s->geo.key_phase[d] + 1;
+    shift[d] = p->precision == SPH_PREC_MIXED && d < p->dim ? Hc * (5.0 / 16.0) : 0.0;
+    s->geo.key_phase[d] = (long long)std::floor((p->domain_min[d] - shift[d]) / Hc);
+    s->geo.key_lim[d] =
+        (long long)std::floor((p->domain_max[d] - shift[d]) / Hc) - s->geo.key_phase[d] + 1;
     key_max *= s->geo.key_lim[d];
   }
   if (key_max <= 0 || key_max > 0x7fffffffLL - 8)
@@ -498,6 +508,7 @@ static int setup_host(const sph_params* p, sph_system* s) {
   const double band = 1.0 / 16384.0;  // 2^-14, see sph_pair64.cu
   k.cell = Hc;
   k.cellf = (float)Hc;
+  for (int d = 0; d < 3; ++d) k.shift[d] = shift[d];
   k.s_lo = (float)(h2 * (1.0 - band));
   k.s_hi = (float)(h2 * (1.0 + band));
   // largest double whose correctly rounded square root is <= H
@@ -514,6 +525,7 @@ static int setup_host(const sph_params* p, sph_system* s) {
   std::frexp(span, &e);  // span < 2^e
   k.fx_k = std::max(-1000, std::min(1000, 62 - e));
   k.inv_hf = (float)k.inv_h;
+  k.hf = (float)H;
   k.cwf = (float)k.cw;
   k.crf = (float)k.cr;
   k.massf = (float)k.mass;

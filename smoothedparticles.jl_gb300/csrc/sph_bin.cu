@@ -58,7 +58,8 @@ __device__ __forceinline__ void bin_keys_body(const State& s, const Geometry& g,
   } else {
     long long ijk[3];
 #pragma unroll
-    for (int d = 0; d < 3; ++d) ijk[d] = 1 + (long long)floor(x[d] / k.cell) - g.key_phase[d];
+    for (int d = 0; d < 3; ++d)
+      ijk[d] = 1 + (long long)floor((x[d] - k.shift[d]) / k.cell) - g.key_phase[d];
     const long long kk =
         ijk[0] + g.key_lim[0] * (ijk[1] - 1) + g.key_lim[0] * g.key_lim[1] * (ijk[2] - 1);
     if (kk < 1 || kk > g.key_max) {  // cannot happen for a point inside the box
@@ -229,7 +230,7 @@ __device__ __forceinline__ void bin_gather_body(const State& cur, const State& a
     const double xd = cur.x[d][src];
     alt.x[d][dst] = xd;
     alt.v[d][dst] = cur.v[d][src];
-    const double origin = (double)(g.key_phase[d] + cc[d]) * k.cell;
+    const double origin = (double)(g.key_phase[d] + cc[d]) * k.cell + k.shift[d];
     xl[d] = (float)(xd - origin);
     if (gather_all) {
       alt.a[d][dst] = cur.a[d][src];

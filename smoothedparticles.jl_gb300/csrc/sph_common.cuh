@@ -77,6 +77,11 @@ struct Consts {
   // and its FP32 copy, of the cell keys, origins and neighbour-cell offsets
   double cell;
   float cellf;
+  // the phase of the cell grid per axis: cell i spans [i cell + shift,
+  // (i + 1) cell + shift).  0 (the reference's grid) for FP64 systems; 5/16
+  // of a cell for mixed ones (not along z in 2D), whose results do not
+  // depend on the grid
+  double shift[3];
   // the largest double s with sqrt_rn(s) <= h: r > h  <=>  fl64(r^2 sum) > s_max
   double s_max;
   // folded constants of the FP64 pair arithmetic: m C_w, m C_r, -(alpha c0) h_smooth
@@ -87,7 +92,7 @@ struct Consts {
   // over the domain box
   int fx_k;
   // FP32 copies for the mixed-precision pair arithmetic
-  float inv_hf, cwf, crf, massf, eta2f, alpha_c0f, h_smoothf, rho0f;
+  float inv_hf, hf, cwf, crf, massf, eta2f, alpha_c0f, h_smoothf, rho0f;
   float gf[3];
   // equation of state (SPH_EOS_*) and the linear one's constants c0^2, rho0^2
   int eos;
@@ -416,7 +421,7 @@ __device__ __forceinline__ long long find_key_point(const Geometry& g, const Con
                                                     const double x[3]) {
   long long ijk[3];
   for (int d = 0; d < 3; ++d) {
-    const double f = floor(x[d] / k.cell);
+    const double f = floor((x[d] - k.shift[d]) / k.cell);
     if (!(f >= -9223372036854775808.0 && f < 9223372036854775808.0)) return -1;
     ijk[d] = 1 + (long long)f - g.key_phase[d];
   }
@@ -542,6 +547,11 @@ __device__ __forceinline__ unsigned long long f2_pack(float lo, float hi) {
 __device__ __forceinline__ unsigned long long f2_sub(unsigned long long a, unsigned long long b) {
   unsigned long long r;
   asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(a), "l"(b));
+  return r;
+}
+__device__ __forceinline__ unsigned long long f2_add(unsigned long long a, unsigned long long b) {
+  unsigned long long r;
+  asm("add.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(a), "l"(b));
   return r;
 }
 __device__ __forceinline__ unsigned long long f2_mul(unsigned long long a, unsigned long long b) {

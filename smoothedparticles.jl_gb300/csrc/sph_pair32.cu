@@ -16,12 +16,18 @@
 //
 // Traversal (one warp per work item of <= 32 targets of one cell): every
 // neighbour cell is visited in chunks of 32 candidates, staged into shared
-// memory with coalesced loads.  Per chunk each lane
-//   A. classifies the 32 staged candidates into a hit mask and a band mask
-//      (FP32 distances from broadcast reads),
+// memory with coalesced loads.  The density and wall-pressure traversals
+// test each staged candidate against the extent of the item's targets and
+// take only the pairs of candidates one of which can be within reach (a
+// chunk with none is skipped).  Per chunk each lane
+//   A. classifies those candidates into a hit mask and a band mask (FP32
+//      distances from broadcast reads); the density pass also evaluates the
+//      kernel shape of every one of them here (zero beyond the support), so
+//      all lanes do the same work,
 //   B. resolves band candidates with the FP64 test, all lanes in lockstep,
-//   C. walks its hit mask in candidate order and accumulates from shared
-//      memory -- so each target's sums keep the reference's neighbour order.
+//   C. (wall pressure, force) walks its hit mask in candidate order and
+//      accumulates from shared memory -- so each target's sums keep the
+//      reference's neighbour order.
 // The density pass stores the final hit masks (4 bytes per lane per chunk,
 // written coalesced) in slots counted during the binning; the force pass of
 // the same binning replays the chunk sequence, reads the masks, stages only
@@ -42,6 +48,12 @@ namespace {
 // Chunk table of the force pass's per-lane walk (3D items have ~54 chunks).
 constexpr int kMaxChunks = 128;
 
+// Candidates of a chunk are tested against the extent of the work item's
+// active targets (the density and wall-pressure traversals; the force pass
+// traverses only when its stored masks do not fit and tests every pair).
+template <int OP>
+constexpr bool kCull = OP != SPH_OP_FORCE;
+
 template <int OP>
 struct MxShared {
   static constexpr bool kRec = OP == SPH_OP_FORCE || OP == SPH_OP_WALL_PRESSURE;
@@ -56,6 +68,7 @@ struct MxShared {
   alignas(16) float py[32];
   alignas(16) float pz[32];
   unsigned fluid;              // wall pressure: bit u = candidate u is fluid
+  float box[kCull<OP> ? 6 : 1];  // extent of the item's targets (low x, y, z; high x, y, z)
   float4 offs[27];             // offset of each neighbour cell from the target cell
   int cb[kTab];                // first candidate of each chunk of the item
   unsigned char cc[kTab];      // neighbour-cell number of each chunk
@@ -213,12 +226,63 @@ struct Acc32 {
   }
 };
 
+// The extent of the item's active targets (cell-relative FP32 positions) into
+// sh.box; the caller syncs the warp before it is read.
+template <int OP>
+__device__ __forceinline__ void mx_item_box(MxShared<OP>& sh, int lane, const CwTarget& t) {
+  float lx = t.active ? t.pi4.x : kFar, ly = t.active ? t.pi4.y : kFar;
+  float lz = t.active ? t.pi4.z : kFar;
+  float hx = t.active ? t.pi4.x : -kFar, hy = t.active ? t.pi4.y : -kFar;
+  float hz = t.active ? t.pi4.z : -kFar;
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    lx = fminf(lx, __shfl_xor_sync(0xffffffffu, lx, o));
+    ly = fminf(ly, __shfl_xor_sync(0xffffffffu, ly, o));
+    lz = fminf(lz, __shfl_xor_sync(0xffffffffu, lz, o));
+    hx = fmaxf(hx, __shfl_xor_sync(0xffffffffu, hx, o));
+    hy = fmaxf(hy, __shfl_xor_sync(0xffffffffu, hy, o));
+    hz = fmaxf(hz, __shfl_xor_sync(0xffffffffu, hz, o));
+  }
+  if (lane == 0) {
+    sh.box[0] = lx; sh.box[1] = ly; sh.box[2] = lz;
+    sh.box[3] = hx; sh.box[4] = hy; sh.box[5] = hz;
+  }
+}
+
+// Whether candidate c of a neighbour cell at offset `off` can be within the
+// support of any target of the item.  The box is taken into the neighbour
+// cell's frame as the targets' own positions are (a - off for every target
+// coordinate a), so it holds every target's (ax, ay, az); the squared gap
+// between c and the box is formed with the operations (and so the rounding)
+// of step A's squared distance.  Rounding is monotone, so the gap along every
+// axis is at most |ax - c.x| for every target and the squared gap at most
+// every target's FP32 squared distance: a candidate beyond s_hi here is
+// beyond it for every target.
+template <int DIM, int OP>
+__device__ __forceinline__ bool mx_near_box(const MxShared<OP>& sh, const float4& off,
+                                            const float4& c, float s_hi) {
+  const float gx = fmaxf(fmaxf(__fsub_rn(__fsub_rn(sh.box[0], off.x), c.x),
+                               __fsub_rn(c.x, __fsub_rn(sh.box[3], off.x))), 0.f);
+  const float gy = fmaxf(fmaxf(__fsub_rn(__fsub_rn(sh.box[1], off.y), c.y),
+                               __fsub_rn(c.y, __fsub_rn(sh.box[4], off.y))), 0.f);
+  float g2 = __fmaf_rn(gy, gy, __fmul_rn(gx, gx));
+  if (DIM == 3) {
+    const float gz = fmaxf(fmaxf(__fsub_rn(__fsub_rn(sh.box[2], off.z), c.z),
+                                 __fsub_rn(c.z, __fsub_rn(sh.box[5], off.z))), 0.f);
+    g2 = __fmaf_rn(gz, gz, g2);
+  }
+  return g2 <= s_hi;
+}
+
 // Stages candidates [base, base + m) of one neighbour cell; empty slots get a
 // far-away position and the type of no operator's neighbour.  CLASSIFY: the
-// chunk goes through step A, which also wants the per-axis copies.
-template <int OP, bool CLASSIFY>
-__device__ __forceinline__ void mx_stage(const State& s, MxShared<OP>& sh, int lane, int base,
-                                         int m) {
+// chunk goes through step A, which also wants the per-axis copies; the
+// return value is then the chunk's live pairs: bit 2j set when candidate 2j
+// or 2j + 1 is near the item's box (and, for the wall pressure, fluid), every
+// pair for the force pass.  `off`: the neighbour cell's offset.
+template <int DIM, int OP, bool CLASSIFY>
+__device__ __forceinline__ unsigned mx_stage(const State& s, const Consts& k, MxShared<OP>& sh,
+                                             int lane, int base, int m, const float4& off) {
   __syncwarp();
   float4 c;
   if (MxShared<OP>::kRec) {
@@ -233,8 +297,9 @@ __device__ __forceinline__ void mx_stage(const State& s, MxShared<OP>& sh, int l
     }
   } else {
     c = lane < m ? __ldg(&s.pl[base + lane]) : make_float4(kFar, kFar, kFar, __int_as_float(-1));
-    sh.c0[lane] = c;
+    if (OP != SPH_OP_DENSITY && OP != SPH_OP_DENSITY_REF) sh.c0[lane] = c;
   }
+  unsigned live = 0u;
   if (CLASSIFY) {
     sh.px[lane] = c.x;
     sh.py[lane] = c.y;
@@ -243,45 +308,91 @@ __device__ __forceinline__ void mx_stage(const State& s, MxShared<OP>& sh, int l
       const unsigned f = __ballot_sync(0xffffffffu, !signbit(c.w));
       if (lane == 0) sh.fluid = f;
     }
+    if (kCull<OP>) {
+      bool near = mx_near_box<DIM>(sh, off, c, k.s_hi);
+      if (OP == SPH_OP_WALL_PRESSURE) near = near && !signbit(c.w);
+      live = __ballot_sync(0xffffffffu, near);
+      live = (live | (live >> 1)) & 0x55555555u;
+    } else {
+      live = 0x55555555u;
+    }
   }
   __syncwarp();
+  return live;
 }
 
-// Step A: hit mask (inside or in the band) and band mask of the 32 staged
-// candidates for a target at (ax, ay, az) relative to their cell.  The wall
-// pressure takes fluid neighbours only.  Two candidates per packed FP32x2
-// operation; the decisions are the signs of s_hi - ss (set: beyond the
-// support) and ss - s_lo (set: below the band), exact in FP32, funnel-shifted
-// into the masks from candidate 31 down to candidate 0.
-template <int DIM, int OP>
-__device__ __forceinline__ void mx_classify(const MxShared<OP>& sh, const Consts& k, float ax,
-                                            float ay, float az, unsigned& hit, unsigned& band) {
+// FP32 square root (the hardware approximation; a subnormal or zero square
+// gives 0).
+__device__ __forceinline__ float sqrt_approx(float x) {
+  float r;
+  asm("sqrt.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
+  return r;
+}
+
+// Step A over the live pairs `pl` of the 32 staged candidates (bit 2j: the
+// pair 2j, 2j + 1), for a target at (ax, ay, az) relative to their cell:
+// the hit mask (inside or in the band) and the band mask.  Candidates of the
+// other pairs are beyond the support of every target of the item.  The
+// sixteen pairs are unrolled from pair 15 down; the skip of a pair is the
+// same for the whole warp.  Two candidates per packed FP32x2 operation; the
+// decisions are the signs of ss - s_hi' (s_hi' the float after s_hi; set:
+// ss <= s_hi) and ss - s_lo (set: below the band), exact in FP32,
+// funnel-shifted into the masks (a skipped pair shifts in zeros).  DENS: also
+// the density's kernel shape t^4 (5 - 4t), t = 1 - min(r, h)/h, of every
+// candidate of the live pairs, summed into two FP32 partial sums; beyond the
+// support it is zero up to the rounding of r (|t| < 2^-23), and SELF zeroes
+// the target's own candidate (self_u).
+template <int DIM, int OP, bool DENS, bool SELF>
+__device__ __forceinline__ void mx_step_a(const MxShared<OP>& sh, const Consts& k, float ax,
+                                          float ay, float az, unsigned pl, int self_u,
+                                          unsigned& hit, unsigned& band, float& fc) {
   const unsigned long long cx = f2_pack(ax, ax), cy = f2_pack(ay, ay), cz = f2_pack(az, az);
-  const unsigned long long shi = f2_pack(k.s_hi, k.s_hi), slo = f2_pack(k.s_lo, k.s_lo);
+  const float shi1 = __int_as_float(__float_as_int(k.s_hi) + 1);
+  const unsigned long long shi = f2_pack(shi1, shi1), slo = f2_pack(k.s_lo, k.s_lo);
   const unsigned long long* x2 = reinterpret_cast<const unsigned long long*>(sh.px);
   const unsigned long long* y2 = reinterpret_cast<const unsigned long long*>(sh.py);
   const unsigned long long* z2 = reinterpret_cast<const unsigned long long*>(sh.pz);
-  unsigned out = 0u, low = 0u;  // bit u: candidate u beyond the support / below the band
+  const unsigned long long minvh = f2_pack(-k.inv_hf, -k.inv_hf);
+  const unsigned long long one = f2_pack(1.f, 1.f), five = f2_pack(5.f, 5.f);
+  const unsigned long long m4 = f2_pack(-4.f, -4.f);
+  const unsigned long long keep = (self_u & 1) ? 0x00000000ffffffffull : 0xffffffff00000000ull;
+  unsigned long long acc = 0ull;
+  unsigned in = 0u, low = 0u;  // bit u: candidate u within s_hi / below the band
 #pragma unroll
   for (int i2 = 15; i2 >= 0; --i2) {
-    const unsigned long long dx = f2_sub(cx, x2[i2]);
-    const unsigned long long dy = f2_sub(cy, y2[i2]);
-    unsigned long long ss = f2_fma(dy, dy, f2_mul(dx, dx));
-    if (DIM == 3) {
-      const unsigned long long dz = f2_sub(cz, z2[i2]);
-      ss = f2_fma(dz, dz, ss);
+    if (pl & (1u << (2 * i2))) {
+      const unsigned long long dx = f2_sub(cx, x2[i2]);
+      const unsigned long long dy = f2_sub(cy, y2[i2]);
+      unsigned long long ss = f2_fma(dy, dy, f2_mul(dx, dx));
+      if (DIM == 3) {
+        const unsigned long long dz = f2_sub(cz, z2[i2]);
+        ss = f2_fma(dz, dz, ss);
+      }
+      const unsigned long long dh = f2_sub(ss, shi);
+      const unsigned long long dl = f2_sub(ss, slo);
+      in = __funnelshift_l((unsigned)(dh >> 32), in, 1);
+      in = __funnelshift_l((unsigned)dh, in, 1);
+      low = __funnelshift_l((unsigned)(dl >> 32), low, 1);
+      low = __funnelshift_l((unsigned)dl, low, 1);
+      if (DENS) {
+        const float r1 = fminf(sqrt_approx(__uint_as_float((unsigned)ss)), k.hf);
+        const float r2 = fminf(sqrt_approx(__uint_as_float((unsigned)(ss >> 32))), k.hf);
+        const unsigned long long t = f2_fma(f2_pack(r1, r2), minvh, one);  // 1 - r/h
+        const unsigned long long t2 = f2_mul(t, t);
+        unsigned long long w = f2_mul(f2_mul(t2, t2), f2_fma(m4, t, five));
+        if (SELF && (self_u >> 1) == i2) w &= keep;
+        acc = f2_add(acc, w);
+      }
+    } else {
+      in <<= 2;
+      low <<= 2;
     }
-    const unsigned long long dh = f2_sub(shi, ss);
-    const unsigned long long dl = f2_sub(ss, slo);
-    out = __funnelshift_l((unsigned)(dh >> 32), out, 1);
-    out = __funnelshift_l((unsigned)dh, out, 1);
-    low = __funnelshift_l((unsigned)(dl >> 32), low, 1);
-    low = __funnelshift_l((unsigned)dl, low, 1);
   }
-  unsigned h = ~out;
+  unsigned h = in;
   if (OP == SPH_OP_WALL_PRESSURE) h &= sh.fluid;
   hit = h;
   band = ~low & h;
+  if (DENS) fc = __uint_as_float((unsigned)acc) + __uint_as_float((unsigned)(acc >> 32));
 }
 
 // Step B: the reference's FP64 test for every band candidate, the lanes
@@ -296,46 +407,6 @@ __device__ __forceinline__ void mx_resolve(const State& s, const Consts& k, cons
       band &= band - 1u;
       if (!within_rn<DIM>(s, k, t.xp, base + u)) hit &= ~(1u << u);
     }
-  }
-}
-
-// The density pass's hits of one chunk (bits of `mask`, candidates staged in
-// sh.c0) for a target at (ax, ay, az) relative to their cell: the shape
-// t^4 (5 - 4t), t = max(1 - r/h, 0), of two hits per packed FP32x2 pass
-// (the square roots one by one), added to f0 in hit order.
-template <int DIM, int OP>
-__device__ __forceinline__ void mx_density_hits(const MxShared<OP>& sh, const Consts& k,
-                                                unsigned mask, float ax, float ay, float az,
-                                                float& f0) {
-  const unsigned long long axp = f2_pack(ax, ax), ayp = f2_pack(ay, ay), azp = f2_pack(az, az);
-  const unsigned long long invh = f2_pack(k.inv_hf, k.inv_hf);
-  const unsigned long long one = f2_pack(1.f, 1.f), five = f2_pack(5.f, 5.f);
-  const unsigned long long m4 = f2_pack(-4.f, -4.f);
-  while (mask) {
-    const int u1 = __ffs(mask) - 1;
-    mask &= mask - 1u;
-    const bool two = mask != 0u;
-    const int u2 = two ? __ffs(mask) - 1 : u1;
-    if (two) mask &= mask - 1u;
-    const float4 q1 = sh.c0[u1], q2 = sh.c0[u2];
-    const unsigned long long dx = f2_sub(axp, f2_pack(q1.x, q2.x));
-    const unsigned long long dy = f2_sub(ayp, f2_pack(q1.y, q2.y));
-    unsigned long long ss = f2_fma(dy, dy, f2_mul(dx, dx));
-    if (DIM == 3) {
-      const unsigned long long dz = f2_sub(azp, f2_pack(q1.z, q2.z));
-      ss = f2_fma(dz, dz, ss);
-    }
-    const float s1 = __uint_as_float((unsigned)ss), s2 = __uint_as_float((unsigned)(ss >> 32));
-    const unsigned long long r = f2_pack(fsqrt(s1), fsqrt(s2));
-    const unsigned long long tt = f2_sub(one, f2_mul(r, invh));  // 1 - r/h
-    // 0 beyond the support (x > 1)
-    const unsigned long long t =
-        f2_pack(fmaxf(__uint_as_float((unsigned)tt), 0.f),
-                fmaxf(__uint_as_float((unsigned)(tt >> 32)), 0.f));
-    const unsigned long long t2 = f2_mul(t, t);
-    const unsigned long long w = f2_mul(f2_mul(t2, t2), f2_fma(m4, t, five));
-    f0 += __uint_as_float((unsigned)w);
-    if (two) f0 += __uint_as_float((unsigned)(w >> 32));
   }
 }
 
@@ -431,41 +502,17 @@ __device__ __forceinline__ void mx_walk(const State& s, const BinScratch& b,
   }
 }
 
-// list_mode: 0 traverse; 1 traverse and store the hit masks (density
-// passes); 2 read the masks stored by the density pass of this binning.
-// The item's chunks are shared by `split` warps: this one takes the chunks
-// gi with gi % split == part.
+// The traversal of one item's neighbour cells, chunk by chunk (steps A-C);
+// `read`: masks stored by the density pass are used where they exist.
 template <int DIM, int OP>
-__device__ __forceinline__ void mx_pass(const State& s, const Geometry& g, const Consts& k,
-                                        const BinScratch& b, MxShared<OP>& sh, int lane, int item,
-                                        const CwTarget& t, Acc32<DIM, OP>& a, int list_mode,
-                                        int part, int split) {
-  // this item's mask slots: the binning counted every cell's chunks
-  int ck = -1, nc = 0;
-  if (list_mode != 0 && b.ck_mask) {
-    const int i0 = __ldg(&b.item_off[t.key]);
-    const int ni = __ldg(&b.item_off[t.key + 1]) - i0;
-    const int co = __ldg(&b.chunk_off[t.key]);
-    nc = ni > 0 ? (__ldg(&b.chunk_off[t.key + 1]) - co) / ni : 0;
-    const long long start = (long long)co + (long long)(item - i0) * nc;
-    if (start + nc <= (long long)b.ck_cap) ck = (int)start;
-  }
-  // slots beyond the counted nc (types changed since the binning) are
-  // neither read nor written
-  const bool read = list_mode == 2 && ck >= 0;
-  const bool store = list_mode == 1 && ck >= 0;
-  if (lane < g.n_diff) {
-    const int nk = t.key + g.key_diff[lane];
-    sh.offs[lane] = (nk >= 1 && nk <= g.key_max) ? cw_offset(g, k, t, nk)
-                                                 : make_float4(0.f, 0.f, 0.f, 0.f);
-  }
-  __syncwarp();
-  if constexpr (OP == SPH_OP_FORCE) {
-    if (read && mx_chunk_table(g, b, sh, lane, t, nc)) {
-      mx_walk<DIM>(s, b, sh, lane, t, a, ck, nc, part, split);
-      a.fold();
-      return;
-    }
+__device__ __forceinline__ void mx_traverse(const State& s, const Geometry& g, const Consts& k,
+                                            const BinScratch& b, MxShared<OP>& sh, int lane,
+                                            const CwTarget& t, Acc32<DIM, OP>& a, int ck, int nc,
+                                            bool read, bool store, int part, int split) {
+  constexpr bool kDens = OP == SPH_OP_DENSITY || OP == SPH_OP_DENSITY_REF;
+  if (kCull<OP>) {
+    mx_item_box(sh, lane, t);
+    __syncwarp();
   }
   int gi = 0;         // chunk number in the item's neighbour sequence
   int mine = part;    // the next chunk this warp takes
@@ -487,16 +534,26 @@ __device__ __forceinline__ void mx_pass(const State& s, const Geometry& g, const
         mine += split;
       }
       unsigned mask;
+      float fc = 0.f;  // density: the chunk's FP32 shape sum
       if (read && gi < nc) {
         mask = t.active ? __ldg(&b.ck_mask[((size_t)ck + gi) * 32 + lane]) : 0u;
         ++gi;
         if (!__any_sync(0xffffffffu, mask != 0u)) continue;
-        mx_stage<OP, false>(s, sh, lane, base, m);
+        mx_stage<DIM, OP, false>(s, k, sh, lane, base, m, off);
       } else {
-        mx_stage<OP, true>(s, sh, lane, base, m);
+        const unsigned pl = mx_stage<DIM, OP, true>(s, k, sh, lane, base, m, off);
+        if (pl == 0u) {
+          // no candidate of the chunk is within reach of the item's box
+          if (store && gi < nc) b.ck_mask[((size_t)ck + gi) * 32 + lane] = 0u;
+          ++gi;
+          continue;
+        }
         unsigned band;
-        mx_classify<DIM, OP>(sh, k, ax, ay, az, mask, band);
         const int self_u = t.i - base;  // core.jl:105: p == q is skipped
+        if (__any_sync(0xffffffffu, self_u >= 0 && self_u < 32))
+          mx_step_a<DIM, OP, kDens, true>(sh, k, ax, ay, az, pl, self_u, mask, band, fc);
+        else
+          mx_step_a<DIM, OP, kDens, false>(sh, k, ax, ay, az, pl, self_u, mask, band, fc);
         if (self_u >= 0 && self_u < 32) {
           mask &= ~(1u << self_u);
           band &= ~(1u << self_u);
@@ -513,10 +570,11 @@ __device__ __forceinline__ void mx_pass(const State& s, const Geometry& g, const
         a.nh += hits;
         a.c0 += hits;
       }
-      if constexpr (OP == SPH_OP_DENSITY || OP == SPH_OP_DENSITY_REF) {
-        // the density's kernel shape for two hits per packed FP32x2
-        // evaluation, added to the batch in hit order
-        mx_density_hits<DIM>(sh, k, mask, ax, ay, az, a.f0);
+      if constexpr (kDens) {
+        // the shapes step A summed (a band candidate the FP64 test rejects
+        // lies at r = h within 2^-14 h: its shape is below 1e-16, as are
+        // the others' beyond the support)
+        a.f0 += fc;
       } else {
         while (mask) {
           const int u = __ffs(mask) - 1;
@@ -529,6 +587,45 @@ __device__ __forceinline__ void mx_pass(const State& s, const Geometry& g, const
     }
   }
   a.fold();
+}
+
+// list_mode: 0 traverse; 1 traverse and store the hit masks (density
+// passes); 2 read the masks stored by the density pass of this binning.
+// The item's chunks are shared by `split` warps: this one takes the chunks
+// gi with gi % split == part.
+template <int DIM, int OP>
+__device__ __forceinline__ void mx_pass(const State& s, const Geometry& g, const Consts& k,
+                                        const BinScratch& b, MxShared<OP>& sh, int lane, int item,
+                                        const CwTarget& t, Acc32<DIM, OP>& a, int list_mode,
+                                        int part, int split) {
+  // this item's mask slots: the binning counted every cell's chunks
+  int ck = -1, nc = 0;
+  if (list_mode != 0 && b.ck_mask) {
+    const int i0 = __ldg(&b.item_off[t.key]);
+    const int ni = __ldg(&b.item_off[t.key + 1]) - i0;
+    const int co = __ldg(&b.chunk_off[t.key]);
+    nc = ni > 0 ? (__ldg(&b.chunk_off[t.key + 1]) - co) / ni : 0;
+    const long long start = (long long)co + (long long)(item - i0) * nc;
+    if (start + nc <= (long long)b.ck_cap) ck = (int)start;
+  }
+  // slots beyond the counted nc (types changed since the binning) are
+  // neither read nor written
+  const bool read = OP == SPH_OP_FORCE && list_mode == 2 && ck >= 0;
+  const bool store = list_mode == 1 && ck >= 0;
+  if (lane < g.n_diff) {
+    const int nk = t.key + g.key_diff[lane];
+    sh.offs[lane] = (nk >= 1 && nk <= g.key_max) ? cw_offset(g, k, t, nk)
+                                                 : make_float4(0.f, 0.f, 0.f, 0.f);
+  }
+  __syncwarp();
+  if constexpr (OP == SPH_OP_FORCE) {
+    if (read && mx_chunk_table(g, b, sh, lane, t, nc)) {
+      mx_walk<DIM>(s, b, sh, lane, t, a, ck, nc, part, split);
+      a.fold();
+      return;
+    }
+  }
+  mx_traverse<DIM, OP>(s, g, k, b, sh, lane, t, a, ck, nc, read, store, part, split);
 }
 
 // The FP64 accumulators a warp of a shared item hands to the item's first
