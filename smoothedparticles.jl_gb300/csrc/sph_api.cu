@@ -442,13 +442,20 @@ static int setup_host(const sph_params* p, sph_system* s) {
   // With the shift such planes lie a quarter spacing (h = 4 dr) or a tenth
   // (h = 4.8 dr) away from every boundary.  The pair set does not depend on
   // the grid; the FP64 path sums in the reference's cell order and keeps it.
-  double shift[3];
+  // Mixed systems also take the cell index from a product with 1/cell
+  // (Consts.inv_cell); the key range below uses the same expression.
+  double shift[3] = {0.0, 0.0, 0.0};
+  const double inv_cell = p->precision == SPH_PREC_MIXED ? 1.0 / Hc : 0.0;
+  const auto cell_coord = [&](double x, int d) {
+    const double u = x - shift[d];
+    return inv_cell != 0.0 ? u * inv_cell : u / Hc;
+  };
   long long key_max = 1;
   for (int d = 0; d < 3; ++d) {
     shift[d] = p->precision == SPH_PREC_MIXED && d < p->dim ? Hc * (5.0 / 16.0) : 0.0;
-    s->geo.key_phase[d] = (long long)std::floor((p->domain_min[d] - shift[d]) / Hc);
+    s->geo.key_phase[d] = (long long)std::floor(cell_coord(p->domain_min[d], d));
     s->geo.key_lim[d] =
-        (long long)std::floor((p->domain_max[d] - shift[d]) / Hc) - s->geo.key_phase[d] + 1;
+        (long long)std::floor(cell_coord(p->domain_max[d], d)) - s->geo.key_phase[d] + 1;
     key_max *= s->geo.key_lim[d];
   }
   if (key_max <= 0 || key_max > 0x7fffffffLL - 8)
@@ -509,6 +516,7 @@ static int setup_host(const sph_params* p, sph_system* s) {
   k.cell = Hc;
   k.cellf = (float)Hc;
   for (int d = 0; d < 3; ++d) k.shift[d] = shift[d];
+  k.inv_cell = inv_cell;
   k.s_lo = (float)(h2 * (1.0 - band));
   k.s_hi = (float)(h2 * (1.0 + band));
   // largest double whose correctly rounded square root is <= H

@@ -59,7 +59,7 @@ __device__ __forceinline__ void bin_keys_body(const State& s, const Geometry& g,
     long long ijk[3];
 #pragma unroll
     for (int d = 0; d < 3; ++d)
-      ijk[d] = 1 + (long long)floor((x[d] - k.shift[d]) / k.cell) - g.key_phase[d];
+      ijk[d] = 1 + (long long)floor(cell_coord(k, x[d], d)) - g.key_phase[d];
     const long long kk =
         ijk[0] + g.key_lim[0] * (ijk[1] - 1) + g.key_lim[0] * g.key_lim[1] * (ijk[2] - 1);
     if (kk < 1 || kk > g.key_max) {  // cannot happen for a point inside the box

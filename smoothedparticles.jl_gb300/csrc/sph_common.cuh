@@ -82,6 +82,11 @@ struct Consts {
   // of a cell for mixed ones (not along z in 2D), whose results do not
   // depend on the grid
   double shift[3];
+  // mixed systems: 1 / cell, the cell index being floor((x - shift) inv_cell)
+  // (a product, where the reference's grid takes a division); 0 for FP64
+  // systems.  The key range is computed with the same expression, and the
+  // expression is monotone in x, so every point of the box has a key.
+  double inv_cell;
   // the largest double s with sqrt_rn(s) <= h: r > h  <=>  fl64(r^2 sum) > s_max
   double s_max;
   // folded constants of the FP64 pair arithmetic: m C_w, m C_r, -(alpha c0) h_smooth
@@ -415,13 +420,20 @@ __device__ __forceinline__ void eos_eval(const Consts& k, double rho, double rho
   }
 }
 
+// x in cell units along axis d: the reference's (x - 0) / h for FP64
+// systems, a product with 1/cell for mixed ones (Consts.inv_cell)
+__device__ __forceinline__ double cell_coord(const Consts& k, double x, int d) {
+  const double u = __dsub_rn(x, k.shift[d]);
+  return k.inv_cell != 0.0 ? __dmul_rn(u, k.inv_cell) : __ddiv_rn(u, k.cell);
+}
+
 // structs.jl:97-106 for an arbitrary point: -1 when a coordinate is NaN,
 // infinite or outside the Int64 range (the reference's try/catch).
 __device__ __forceinline__ long long find_key_point(const Geometry& g, const Consts& k,
                                                     const double x[3]) {
   long long ijk[3];
   for (int d = 0; d < 3; ++d) {
-    const double f = floor((x[d] - k.shift[d]) / k.cell);
+    const double f = floor(cell_coord(k, x[d], d));
     if (!(f >= -9223372036854775808.0 && f < 9223372036854775808.0)) return -1;
     ijk[d] = 1 + (long long)f - g.key_phase[d];
   }
