@@ -1,14 +1,15 @@
 // sph_pair32.cu -- mixed-precision pair passes.
 //
-// Same cells, the same neighbour sequence and the same candidate
-// classification as the FP64 passes (FP32 test on cell-relative positions,
-// FP64 band test with round-to-nearest intrinsics), so the set of pairs is
-// identical to the FP64 path for the same positions.  What changes is the
-// arithmetic on a hit:
+// The candidate classification of the FP64 passes (FP32 test on
+// cell-relative positions, FP64 band test with round-to-nearest intrinsics),
+// so the set of pairs is the FP64 path's for the same positions.  The cells
+// are the system's own (the reference's grid offset by 5/16 of a cell, the
+// index from a product with 1/cell: the pair set does not depend on the
+// grid).  What changes is the arithmetic on a hit:
 //   * the separation is the FP32 cell-relative one (x_p - x_q with both
 //     positions within one cell of their origins, accurate to ~2^-21 h);
 //   * kernel values, pressure, viscosity and XSPH terms are FP32, with the
-//     neighbour's (v, P/rho^2, rho) read from a 20-byte FP32 copy;
+//     neighbour's (x, rho, v, P/rho^2) read from a 32-byte FP32 record;
 //   * a lane's hits are summed in FP32 in batches of at most 32 and each
 //     batch is folded into FP64 accumulators;
 //   * positions, the self term, the EOS, the wall-pressure quotient and the
@@ -26,13 +27,12 @@
 //      all lanes do the same work,
 //   B. resolves band candidates with the FP64 test, all lanes in lockstep,
 //   C. (wall pressure, force) walks its hit mask in candidate order and
-//      accumulates from shared memory -- so each target's sums keep the
-//      reference's neighbour order.
+//      accumulates from shared memory, in the target's neighbour order.
 // The density pass stores the final hit masks (4 bytes per lane per chunk,
-// written coalesced) in slots counted during the binning; the force pass of
-// the same binning replays the chunk sequence, reads the masks, stages only
-// chunks with hits and skips steps A and B.  An item whose slots do not fit
-// the mask capacity traverses in both passes.
+// written coalesced) in slots counted during the binning; in the force pass
+// of the same binning every lane walks its own stored masks, chunk by chunk,
+// and loads each hit's record directly (no steps A and B).  An item whose
+// slots do not fit the mask capacity traverses in both passes.
 // Built with FMA contraction (the FP64 band test uses explicit intrinsics;
 // any FP32 evaluation order stays within the classification band's margin).
 #include <algorithm>
@@ -58,9 +58,9 @@ template <int OP>
 struct MxShared {
   static constexpr bool kRec = OP == SPH_OP_FORCE || OP == SPH_OP_WALL_PRESSURE;
   static constexpr int kTab = OP == SPH_OP_FORCE ? kMaxChunks : 1;
-  // staged candidates: density passes stage positions (type bits in .w);
-  // force and wall pressure stage the 32-byte neighbour record
-  float4 c0[32];               // (x, y, z) cell-relative, .w = type / signed rho
+  // staged candidates of the force and wall-pressure traversals: the
+  // 32-byte neighbour record (the density passes read the per-axis copies)
+  float4 c0[kRec ? 32 : 1];    // (x, y, z) cell-relative, .w = signed rho
   float4 c1[kRec ? 32 : 1];    // (vx, vy, vz, P/rho^2)
   // the staged coordinates once more, one array per axis: step A reads two
   // candidates' coordinates as one 64-bit word for the packed FP32x2 tests
@@ -297,7 +297,6 @@ __device__ __forceinline__ unsigned mx_stage(const State& s, const Consts& k, Mx
     }
   } else {
     c = lane < m ? __ldg(&s.pl[base + lane]) : make_float4(kFar, kFar, kFar, __int_as_float(-1));
-    if (OP != SPH_OP_DENSITY && OP != SPH_OP_DENSITY_REF) sh.c0[lane] = c;
   }
   unsigned live = 0u;
   if (CLASSIFY) {
