@@ -107,8 +107,10 @@ typedef struct sph_params {
   double cell_factor;    /* cell size / h: 0 or 1 = the reference's cells of size h
                             (structs.jl:66-68); SPH_PREC_MIXED systems accept
                             1..2 (the pair set does not depend on it; the
-                            neighbour order and the FP32 sums do).  No
-                            reference counterpart; ABI version 2. */
+                            neighbour order and the FP32 sums do).  A mixed
+                            system's grid is also offset by 5/16 of a cell
+                            along each of its axes (sph_geometry reports its
+                            keys).  No reference counterpart; ABI version 2. */
 } sph_params;
 
 /* Equation of state of SPH_OP_EOS and of the step's fused EOS, and the
