@@ -42,8 +42,10 @@ L2_BYTES = 129 * 2**20
 # evaluates every unordered pair ONCE for both of its targets (sph_tile64.cu)
 # and then accumulates each target's row, so its count is per unordered pair
 # (the shared work) plus per directed hit (each target's accumulation); the
-# mixed path evaluates every directed hit in full (sph_pair32.cu), so its count
-# is per directed hit.  3D (2D drops the z terms):
+# mixed path evaluates every directed hit in full (sph_pair32.cu; its density
+# pass also the candidates of the live pairs beyond the support, whose shapes
+# are zero: not counted), so its count is per directed hit.  3D (2D drops the
+# z terms):
 #   FP64 density, per unordered pair (fluid-fluid and fluid-wall):
 #       d 3 + squares 5 + sqrt 1 + t = 1 - r/H 2 + clamp 1 + m W 6       = 18
 #     per directed entry of a fluid target: the row sum 1
