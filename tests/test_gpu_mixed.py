@@ -243,3 +243,40 @@ def test_cell_factor_limits(gpu):
         with pytest.raises(sphgpu.SphError):
             sphgpu.ParticleSystem(dict(c.params, cell_factor=bad), sphgpu.MIXED)
     sphgpu.ParticleSystem(dict(c.params, cell_factor=1.0), sphgpu.FP64).close()
+
+
+@pytest.mark.parametrize("dim,dr", [(2, 0.02), (3, 0.05)])
+def test_mixed_grid_geometry(gpu, dim, dr):
+    """A mixed system's cells (cell factor 1): the reference's grid offset by
+    5/16 of a cell along each of its axes, the index floor((x - s) / h) taken
+    as a product with 1/h, and sph_geometry reports that grid; an FP64
+    system keeps the reference's floor(x / h).  On the 3D dam break's lattice
+    (h = 4 dr) no particle lies within a fifth of a spacing of a mixed cell's
+    boundary, where the reference's grid has whole planes on them."""
+    c = G.dam_break(dim, dr)
+    p = c.params
+    H = p["h"]
+    s = [H * (5.0 / 16.0) if d < dim else 0.0 for d in range(3)]
+    ic = 1.0 / H
+    phase = [int(np.floor((p["domain_min"][d] - s[d]) * ic)) for d in range(3)]
+    lim = [int(np.floor((p["domain_max"][d] - s[d]) * ic)) - phase[d] + 1 for d in range(3)]
+    g = sphgpu.ParticleSystem(p, sphgpu.MIXED)
+    f64 = sphgpu.ParticleSystem(p, sphgpu.FP64)
+    try:
+        geo = g.geometry()
+        assert list(geo["key_phase"]) == phase
+        assert list(geo["key_lim"]) == lim
+        assert geo["key_max"] == lim[0] * lim[1] * lim[2]
+        ref = f64.geometry()
+        assert list(ref["key_phase"]) == [int(np.floor(p["domain_min"][d] / H)) for d in range(3)]
+        if dim == 3:
+            u = (c.x - np.array(s)) * ic
+            frac = u - np.floor(u)
+            gap = np.minimum(frac, 1.0 - frac) * (H / dr)  # in lattice spacings
+            assert gap.min() >= 0.2
+            v = c.x / H
+            on_boundary = np.abs(v - np.round(v)) * (H / dr) < 1e-6
+            assert on_boundary.any()  # the reference's grid: planes on its boundaries
+    finally:
+        g.close()
+        f64.close()
