@@ -88,7 +88,13 @@ __device__ __forceinline__ float kw32(const Consts& k, float r, float t) {
 }
 __device__ __forceinline__ float krdw32(const Consts& k, float t) { return k.crf * (t * t * t); }
 
-__device__ __forceinline__ float fsqrt(float ss) { return ss > 0.f ? ss * rsqrtf(ss) : 0.f; }
+// FP32 square root of a hit's squared distance (the hardware approximation;
+// 0 for 0)
+__device__ __forceinline__ float fsqrt(float ss) {
+  float r;
+  asm("sqrt.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(ss));
+  return r;
+}
 
 // The FP32 neighbour record of particle i: (cell-relative x, y, z, rho with
 // the sign bit set for walls) and (vx, vy, vz, P/rho^2).
